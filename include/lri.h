@@ -1,0 +1,179 @@
+/*
+ * lri.h - C ABI of the GB300 (sm_103a) engine for the per-step hot path of
+ * dynamical low-rank approximation (DLRA): the K/L/S substeps of the
+ * unconventional "BUG" integrator, its rank-adaptive variant and the
+ * projector-splitting (KSL) integrator of LowRankIntegrators.jl.
+ *
+ * Conventions
+ *   - Every matrix is column-major (Julia's layout).  A batch holds `count`
+ *     independent problems ("instances") of uneven sizes; instance i owns an
+ *     n_i x r_cap_i block of U, an r_cap_i x r_cap_i block of S and an
+ *     m_i x r_cap_i block of V inside caller-owned packed device buffers.
+ *     `lri_batch_layout` returns the element offsets; only the leading
+ *     r_i columns (r_i = current rank) are meaningful.
+ *   - Device buffers are passed as raw pointers and stay owned by the caller.
+ *     The library allocates its own workspace once, in lri_batch_create; the
+ *     step calls allocate nothing.
+ *   - A handle is not thread-safe: use one per host thread / stream.
+ *   - Errors are returned as lri_status; kernel-side failures (non-finite
+ *     values, SVD non-convergence, rank overflow) are accumulated in a device
+ *     status word read by lri_batch_status().
+ *   - There is no CPU fallback: without a usable CUDA device every entry point
+ *     that computes returns LRI_ERR_CUDA.
+ *
+ * Reference interfaces replaced (paths are within LowRankIntegrators.jl):
+ *   MatrixDEProblem / MatrixDataProblem        src/primitives.jl:13-30
+ *   init(prob, alg, dt)                         src/integrators/unconventional.jl:109-119,
+ *                                               src/integrators/rank_adaptive_unconventional.jl:94-104,
+ *                                               src/integrators/projector_splitting.jl:107-115
+ *   step!(integrator, alg, dt)                  src/integrators/unconventional.jl:159-164,
+ *                                               src/integrators/rank_adaptive_unconventional.jl:171-180,
+ *                                               src/integrators/projector_splitting.jl:191-211
+ *   set_u!/step! of the substep integrators     src/integrators/unconventional.jl:138-139,146-147,154-155
+ *   update_data! + Δy for data problems         src/integrators/data_integrator.jl:22-28,
+ *                                               src/integrators/unconventional.jl:121-127
+ */
+#ifndef LRI_H
+#define LRI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LRI_API __attribute__((visibility("default")))
+#else
+#define LRI_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LRI_ABI_VERSION 1
+
+typedef enum {
+  LRI_OK = 0,
+  LRI_ERR_ARG = 1,           /* invalid argument (null pointer, bad size, bad enum) */
+  LRI_ERR_UNSUPPORTED = 2,   /* combination not provided by the engine */
+  LRI_ERR_BREAKDOWN = 3,     /* SVD did not converge */
+  LRI_ERR_NONFINITE = 4,     /* NaN/Inf appeared in a factor */
+  LRI_ERR_RANK_OVERFLOW = 5, /* rank-adaptive step needed more than r_cap */
+  LRI_ERR_TIMEOUT = 6,       /* a bounded device wait gave up */
+  LRI_ERR_CUDA = 7,          /* CUDA runtime error or no device */
+  LRI_ERR_STATE = 8          /* call out of order (e.g. step before bind) */
+} lri_status;
+
+typedef enum { LRI_F64 = 0, LRI_F32 = 1 } lri_dtype;
+
+/* Algorithms: UnconventionalAlgorithm (unconventional.jl:13-21),
+ * RankAdaptiveUnconventionalAlgorithm (rank_adaptive_unconventional.jl:15-23),
+ * ProjectorSplitting (projector_splitting.jl:27-41). */
+typedef enum { LRI_ALG_BUG = 0, LRI_ALG_RA_BUG = 1, LRI_ALG_KSL = 2 } lri_alg_kind;
+typedef enum { LRI_KSL_PRIMAL = 0, LRI_KSL_DUAL = 1, LRI_KSL_STRANG = 2 } lri_ksl_order;
+
+/* Flow maps.  The reference accepts any Julia closure F(Y,t) evaluated by
+ * LowRankArithmetic; the engine accepts this fixed menu (no closures):
+ *   ZERO        F = 0
+ *   SYLVESTER   F(X) = A X + X B^T, A (n x n) and B (m x m) tridiagonal,
+ *               each stored as three vectors [sub | diag | sup] (sub[0] and
+ *               sup[last] unused).  diag(theta) X terms fold into A's diagonal.
+ *   BURGERS     F(X) = (Dxx X) diag(nu) + alpha (Dx X).*X + beta Dx(X.*X),
+ *               periodic central differences of spacing h; nu per column.
+ *   DATA        MatrixDataProblem: exact substep flows driven by the snapshot
+ *               increment Δy = A(t+dt) - A(t) (data_integrator.jl:13-16). */
+typedef enum {
+  LRI_OP_ZERO = 0,
+  LRI_OP_SYLVESTER_TRIDIAG = 1,
+  LRI_OP_BURGERS_PERIODIC = 2,
+  LRI_OP_DATA = 3
+} lri_op_kind;
+
+/* Fixed-step explicit Runge-Kutta substep scheme with a sub-diagonal Butcher
+ * tableau (Euler, Heun, midpoint, classic RK4), run nsub times per substep
+ * interval.  Stands in for the reference's DifferentialEquations solver
+ * (default Tsit5, unconventional.jl:18). */
+typedef struct {
+  int32_t nstages;   /* 1..4 */
+  int32_t nsub;      /* >= 1 */
+  double a[4];       /* a[s]: weight of k_{s-1} in stage s input; a[0] unused */
+  double b[4];
+  double c[4];
+} lri_scheme;
+
+typedef struct {
+  int32_t kind;        /* lri_alg_kind */
+  int32_t ksl_order;   /* lri_ksl_order (KSL only) */
+  lri_scheme K_alg, L_alg, S_alg;
+  double tol;          /* rank-adaptive truncation tolerance (absolute) */
+  int32_t r_min;       /* rank-adaptive lower bound (>= 1); no reference counterpart */
+  int32_t reserved;
+} lri_alg_desc;
+
+typedef struct {
+  int32_t dtype;       /* lri_dtype: F64 = plain FP64 form, F32 = fast form */
+  int32_t op;          /* lri_op_kind */
+  int32_t count;       /* number of instances (>= 1) */
+  int32_t reserved;
+  const int64_t* n;      /* host [count]: rows of U */
+  const int64_t* m;      /* host [count]: rows of V */
+  const int64_t* r;      /* host [count]: initial rank */
+  const int64_t* r_cap;  /* host [count]: capacity (rank-adaptive r_max), NULL => r */
+  double burgers_h, burgers_alpha, burgers_beta;
+} lri_batch_desc;
+
+typedef struct lri_batch lri_batch;
+
+/* Library / device information. */
+LRI_API int lri_abi_version(void);
+LRI_API const char* lri_status_str(lri_status s);
+LRI_API lri_status lri_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor);
+
+/* init(prob, alg, dt): validates the shapes, plans the packed layout and
+ * allocates the workspace. */
+LRI_API lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const lri_alg_desc* alg);
+LRI_API lri_status lri_batch_destroy(lri_batch* b);
+
+/* Element offsets of each instance inside the packed buffers (host arrays of
+ * length count, any may be NULL) and the total element counts
+ * totals[0..4] = {U, S, V, operator A, operator B}.  Operator A holds 3*n_i
+ * elements per instance (SYLVESTER) or nothing; operator B holds 3*m_i
+ * (SYLVESTER) or m_i (BURGERS: nu) elements. */
+LRI_API lri_status lri_batch_layout(const lri_batch* b, int64_t* offU, int64_t* offS, int64_t* offV,
+                            int64_t* offA, int64_t* offB, int64_t* totals);
+
+/* Binds the caller's device buffers (dtype of the batch).  U, S, V hold Y0 on
+ * entry and are updated in place by every step, like the reference's
+ * integrator.u (unconventional.jl:151-156).  opA/opB may be NULL for ZERO and
+ * DATA.  Binding resets the cached projections and ranks to the host r. */
+LRI_API lri_status lri_batch_bind(lri_batch* b, void* U, void* S, void* V, const void* opA, const void* opB);
+
+/* DATA problems: device buffer with every instance's first snapshot A(t0)
+ * (packed like lri_batch_layout's "data" region: n_i x m_i column-major,
+ * offsets returned by lri_batch_data_layout).  Copied into the library's
+ * previous-snapshot buffer (unconventional.jl:91-93). */
+LRI_API lri_status lri_batch_data_layout(const lri_batch* b, int64_t* offY, int64_t* total);
+LRI_API lri_status lri_batch_data_init(lri_batch* b, const void* Y0, void* stream);
+
+/* step!(integrator, alg, dt), nsteps times, starting at time t.  For DATA
+ * problems nsteps must be 1 and Ynext points at A(t+dt) for every instance
+ * (same packing as lri_batch_data_init); for other operators Ynext is NULL.
+ * Runs asynchronously on `stream` (cudaStream_t, NULL = legacy default);
+ * multi-step calls run as one captured CUDA graph. */
+LRI_API lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, const void* Ynext,
+                          void* stream);
+
+/* Current ranks (host array of length count; synchronises the stream). */
+LRI_API lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream);
+
+/* Device status word accumulated by the kernels since the last call
+ * (synchronises `stream`, then clears the word). */
+LRI_API lri_status lri_batch_status(lri_batch* b, void* stream);
+
+/* Number of kernel launches one step makes (for launch accounting). */
+LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LRI_H */

@@ -1,0 +1,593 @@
+"""GB300-native engine for the per-step hot path of LowRankIntegrators.jl.
+
+Host-side mirror of the reference's public surface (src/primitives.jl,
+src/integrators/*.jl): problems, algorithm objects, ``init`` / ``step`` /
+``solve`` and the ``SVDLikeRepresentation`` factors.  Every step runs in the
+CUDA library ``liblri_gb300.so`` (include/lri.h) on the current CUDA device;
+this module only moves factors between host and device and drives the time
+loop of src/primitives.jl:68-80.  There is no CPU fallback: without the
+library or a CUDA device every call that computes raises.
+
+The reference accepts an arbitrary Julia closure ``F``; the engine accepts a
+fixed menu of flow maps (``ZeroOperator``, ``SylvesterTridiagOperator``) and
+data streams (``MatrixDataProblem``).  Substeps use a fixed-step explicit
+Runge-Kutta scheme (``RK4(nsub)``, ``Euler(nsub)``, ...) in place of the
+reference's adaptive Tsit5 default.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _native
+from ._native import LriError
+
+__all__ = [
+    "SVDLikeRepresentation", "MatrixDEProblem", "MatrixDataProblem", "DLRSolution", "DLRIntegrator",
+    "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm", "ProjectorSplitting",
+    "PrimalLieTrotter", "DualLieTrotter", "Strang", "SubstepScheme", "Euler", "Heun", "Midpoint", "RK4",
+    "ZeroOperator", "SylvesterTridiagOperator", "Batch", "init", "step", "solve", "solve_ensemble",
+    "LriError", "n_steps",
+]
+
+
+# ---------------------------------------------------------------------------
+# Factors and problems (src/primitives.jl:13-49; containers from LowRankArithmetic)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class SVDLikeRepresentation:
+    """Y = U S V^T (U n x r, S r x r, V m x r), host arrays in float64."""
+    U: np.ndarray
+    S: np.ndarray
+    V: np.ndarray
+
+    @property
+    def rank(self) -> int:
+        return self.S.shape[0]
+
+    @property
+    def shape(self) -> Tuple[int, int]:
+        return (self.U.shape[0], self.V.shape[0])
+
+    def full(self) -> np.ndarray:
+        return self.U @ self.S @ self.V.T
+
+    def copy(self) -> "SVDLikeRepresentation":
+        return SVDLikeRepresentation(self.U.copy(), self.S.copy(), self.V.copy())
+
+
+class ZeroOperator:
+    """F(X, t) = 0."""
+    kind = _native.LRI_OP_ZERO
+
+
+class SylvesterTridiagOperator:
+    """F(X, t) = A X + X B^T (+ diag(theta) X), A and B tridiagonal.
+
+    ``A`` and ``B`` are (sub, diag, sup) triples of length n and m
+    (``sub[0]`` and ``sup[-1]`` are ignored).  ``theta`` (length n) is folded
+    into A's diagonal.
+    """
+    kind = _native.LRI_OP_SYLVESTER_TRIDIAG
+
+    def __init__(self, A, B, theta=None):
+        sub, dia, sup = (np.asarray(x, dtype=np.float64) for x in A)
+        if theta is not None:
+            dia = dia + np.asarray(theta, dtype=np.float64)
+        self.A = (sub, dia, sup)
+        self.B = tuple(np.asarray(x, dtype=np.float64) for x in B)
+
+    def packed(self):
+        return np.concatenate(self.A), np.concatenate(self.B)
+
+
+@dataclass
+class MatrixDEProblem:
+    """dX/dt = F(X, t) on tspan, X(t0) ~ u0 (src/primitives.jl:13-17)."""
+    f: object
+    u0: SVDLikeRepresentation
+    tspan: Tuple[float, float]
+
+
+class MatrixDataProblem:
+    """Low-rank tracking of a data stream (src/primitives.jl:23-30): ``y`` is a
+    callable t -> A(t) or a list of snapshots (then tspan = (1, len(y)) and
+    the step size defaults to 1)."""
+
+    def __init__(self, y, u0: SVDLikeRepresentation, tspan=None):
+        self.y = y
+        self.u0 = u0
+        if tspan is None:
+            if callable(y):
+                raise ValueError("tspan is required when the data stream is a function")
+            tspan = (1, len(y))
+        self.tspan = tspan
+        self.f = None
+
+
+@dataclass
+class DLRSolution:
+    """Solution history (src/primitives.jl:46-49)."""
+    Y: List[Optional[SVDLikeRepresentation]]
+    t: List[float]
+
+
+# ---------------------------------------------------------------------------
+# Substep schemes and algorithms (src/integrators/*.jl)
+# ---------------------------------------------------------------------------
+
+@dataclass(frozen=True)
+class SubstepScheme:
+    """Fixed-step explicit RK scheme with a sub-diagonal tableau, run ``nsub``
+    times per substep interval (stands in for DiffEq's ``Tsit5()``)."""
+    name: str
+    a: Tuple[float, ...]
+    b: Tuple[float, ...]
+    c: Tuple[float, ...]
+    nsub: int = 1
+
+    def with_nsub(self, nsub: int) -> "SubstepScheme":
+        return SubstepScheme(self.name, self.a, self.b, self.c, int(nsub))
+
+    def to_c(self) -> _native.lri_scheme:
+        s = _native.lri_scheme()
+        s.nstages = len(self.b)
+        s.nsub = int(self.nsub)
+        for i in range(len(self.b)):
+            s.a[i] = self.a[i]
+            s.b[i] = self.b[i]
+            s.c[i] = self.c[i]
+        return s
+
+
+def Euler(nsub: int = 1) -> SubstepScheme:
+    return SubstepScheme("Euler", (0.0,), (1.0,), (0.0,), nsub)
+
+
+def Heun(nsub: int = 1) -> SubstepScheme:
+    return SubstepScheme("Heun", (0.0, 1.0), (0.5, 0.5), (0.0, 1.0), nsub)
+
+
+def Midpoint(nsub: int = 1) -> SubstepScheme:
+    return SubstepScheme("Midpoint", (0.0, 0.5), (0.0, 1.0), (0.0, 0.5), nsub)
+
+
+def RK4(nsub: int = 1) -> SubstepScheme:
+    return SubstepScheme("RK4", (0.0, 0.5, 0.5, 1.0), (1 / 6, 1 / 3, 1 / 3, 1 / 6), (0.0, 0.5, 0.5, 1.0), nsub)
+
+
+@dataclass
+class UnconventionalAlgorithm:
+    """BUG integrator (src/integrators/unconventional.jl:13-21)."""
+    K_alg: SubstepScheme = field(default_factory=RK4)
+    L_alg: Optional[SubstepScheme] = None
+    S_alg: Optional[SubstepScheme] = None
+
+    def __post_init__(self):
+        self.L_alg = self.L_alg or self.K_alg
+        self.S_alg = self.S_alg or self.K_alg
+
+
+@dataclass
+class RankAdaptiveUnconventionalAlgorithm:
+    """Rank-adaptive BUG (src/integrators/rank_adaptive_unconventional.jl:15-23).
+    ``rmax`` bounds the rank (and sizes the preallocated buffers); ``rmin`` has
+    no reference counterpart and defaults to 1."""
+    tol: float
+    rmax: int = 32
+    K_alg: SubstepScheme = field(default_factory=RK4)
+    L_alg: Optional[SubstepScheme] = None
+    S_alg: Optional[SubstepScheme] = None
+    rmin: int = 1
+
+    def __post_init__(self):
+        self.L_alg = self.L_alg or self.K_alg
+        self.S_alg = self.S_alg or self.K_alg
+
+
+class PrimalLieTrotter:
+    pass
+
+
+class DualLieTrotter:
+    pass
+
+
+class Strang:
+    pass
+
+
+@dataclass
+class ProjectorSplitting:
+    """KSL integrator (src/integrators/projector_splitting.jl:27-41)."""
+    order: object = field(default_factory=PrimalLieTrotter)
+    K_alg: SubstepScheme = field(default_factory=RK4)
+    L_alg: Optional[SubstepScheme] = None
+    S_alg: Optional[SubstepScheme] = None
+
+    def __post_init__(self):
+        self.L_alg = self.L_alg or self.K_alg
+        self.S_alg = self.S_alg or self.K_alg
+
+
+def _alg_desc(alg) -> _native.lri_alg_desc:
+    d = _native.lri_alg_desc()
+    if isinstance(alg, UnconventionalAlgorithm):
+        d.kind = _native.LRI_ALG_BUG
+    elif isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
+        d.kind = _native.LRI_ALG_RA_BUG
+        d.tol = float(alg.tol)
+        d.r_min = int(alg.rmin)
+    elif isinstance(alg, ProjectorSplitting):
+        d.kind = _native.LRI_ALG_KSL
+        if isinstance(alg.order, PrimalLieTrotter):
+            d.ksl_order = _native.LRI_KSL_PRIMAL
+        elif isinstance(alg.order, DualLieTrotter):
+            d.ksl_order = _native.LRI_KSL_DUAL
+        elif isinstance(alg.order, Strang):
+            d.ksl_order = _native.LRI_KSL_STRANG
+        else:
+            raise TypeError("unknown projector-splitting order")
+    else:
+        raise TypeError(f"unsupported algorithm {type(alg).__name__}")
+    d.K_alg = alg.K_alg.to_c()
+    d.L_alg = alg.L_alg.to_c()
+    d.S_alg = alg.S_alg.to_c()
+    if d.kind != _native.LRI_ALG_RA_BUG:
+        d.r_min = 1
+    return d
+
+
+# ---------------------------------------------------------------------------
+# Device batch: the handle the C ABI works on
+# ---------------------------------------------------------------------------
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("lri_gb300 needs a CUDA device; there is no CPU fallback")
+    return torch
+
+
+class Batch:
+    """A batch of independent DLRA instances advanced together on the GPU.
+
+    Owns the device copies of the packed factors (U, S, V) and operator
+    coefficients, and the C handle (workspace, launch order, CUDA graph).
+    """
+
+    def __init__(self, n: Sequence[int], m: Sequence[int], r: Sequence[int], alg, op_kind: int,
+                 precision: str = "fp64", r_cap: Optional[Sequence[int]] = None):
+        torch = _torch()
+        self.torch = torch
+        self.lib = _native.load()
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.precision = precision
+        self.dtype = torch.float64 if precision == "fp64" else torch.float32
+        self.np_dtype = np.float64 if precision == "fp64" else np.float32
+        self.count = len(n)
+        self.n = np.asarray(n, dtype=np.int64)
+        self.m = np.asarray(m, dtype=np.int64)
+        self.r0 = np.asarray(r, dtype=np.int64)
+        if r_cap is None:
+            r_cap = self.r0
+        self.rcap = np.asarray(r_cap, dtype=np.int64)
+        self.alg = alg
+        self.op_kind = op_kind
+        desc = _native.lri_batch_desc()
+        desc.dtype = _native.LRI_F64 if precision == "fp64" else _native.LRI_F32
+        desc.op = op_kind
+        desc.count = self.count
+        I64P = C.POINTER(C.c_int64)
+        desc.n = self.n.ctypes.data_as(I64P)
+        desc.m = self.m.ctypes.data_as(I64P)
+        desc.r = self.r0.ctypes.data_as(I64P)
+        desc.r_cap = self.rcap.ctypes.data_as(I64P)
+        self._algd = _alg_desc(alg)
+        self.handle = C.c_void_p()
+        _native.check(self.lib.lri_batch_create(C.byref(self.handle), C.byref(desc), C.byref(self._algd)),
+                      "lri_batch_create")
+        cnt = self.count
+        self.offU = np.zeros(cnt, np.int64)
+        self.offS = np.zeros(cnt, np.int64)
+        self.offV = np.zeros(cnt, np.int64)
+        self.offA = np.zeros(cnt, np.int64)
+        self.offB = np.zeros(cnt, np.int64)
+        tot = np.zeros(5, np.int64)
+        _native.check(self.lib.lri_batch_layout(self.handle, *(x.ctypes.data_as(I64P) for x in
+                                                               (self.offU, self.offS, self.offV, self.offA,
+                                                                self.offB, tot))), "lri_batch_layout")
+        self.totals = tot
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        mk = lambda k: torch.zeros(max(int(k), 4), dtype=self.dtype, device=dev)
+        self.U, self.S, self.V = mk(tot[0]), mk(tot[1]), mk(tot[2])
+        self.opA, self.opB = mk(tot[3]), mk(tot[4])
+        self.offY = None
+        if op_kind == _native.LRI_OP_DATA:
+            self.offY = np.zeros(cnt, np.int64)
+            totY = np.zeros(1, np.int64)
+            _native.check(self.lib.lri_batch_data_layout(self.handle, self.offY.ctypes.data_as(I64P),
+                                                         totY.ctypes.data_as(I64P)), "lri_batch_data_layout")
+            self.totY = int(totY[0])
+            self.Ynext = mk(self.totY)
+        self.bound = False
+
+    # -- helpers -----------------------------------------------------------
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.lri_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pack_factors(self, factors: Sequence[SVDLikeRepresentation]):
+        """Host-side packing of per-instance factors into the flat layout."""
+        hU = np.zeros(int(self.U.numel()), self.np_dtype)
+        hS = np.zeros(int(self.S.numel()), self.np_dtype)
+        hV = np.zeros(int(self.V.numel()), self.np_dtype)
+        for i, Y in enumerate(factors):
+            n, m, rc = int(self.n[i]), int(self.m[i]), int(self.rcap[i])
+            r = Y.S.shape[0]
+            if Y.U.shape != (n, r) or Y.V.shape != (m, r) or r > rc:
+                raise ValueError(f"instance {i}: factor shapes do not match the batch")
+            u = np.zeros((n, rc), self.np_dtype)
+            u[:, :r] = Y.U
+            hU[self.offU[i]:self.offU[i] + n * rc] = u.ravel(order="F")
+            s = np.zeros((rc, rc), self.np_dtype)
+            s[:r, :r] = Y.S
+            hS[self.offS[i]:self.offS[i] + rc * rc] = s.ravel(order="F")
+            v = np.zeros((m, rc), self.np_dtype)
+            v[:, :r] = Y.V
+            hV[self.offV[i]:self.offV[i] + m * rc] = v.ravel(order="F")
+        return hU, hS, hV
+
+    def upload(self, factors: Sequence[SVDLikeRepresentation], operators=None):
+        hU, hS, hV = self.pack_factors(factors)
+        t = self.torch
+        self.U.copy_(t.from_numpy(hU))
+        self.S.copy_(t.from_numpy(hS))
+        self.V.copy_(t.from_numpy(hV))
+        if operators is not None and self.op_kind == _native.LRI_OP_SYLVESTER_TRIDIAG:
+            hA = np.zeros(int(self.opA.numel()), self.np_dtype)
+            hB = np.zeros(int(self.opB.numel()), self.np_dtype)
+            for i, op in enumerate(operators):
+                a, b = op.packed()
+                if len(a) != 3 * self.n[i] or len(b) != 3 * self.m[i]:
+                    raise ValueError(f"instance {i}: operator size does not match the batch")
+                hA[self.offA[i]:self.offA[i] + len(a)] = a
+                hB[self.offB[i]:self.offB[i] + len(b)] = b
+            self.opA.copy_(t.from_numpy(hA))
+            self.opB.copy_(t.from_numpy(hB))
+        self.bind()
+
+    def bind(self):
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        _native.check(self.lib.lri_batch_bind(self.handle, ptr(self.U), ptr(self.S), ptr(self.V),
+                                              ptr(self.opA), ptr(self.opB)), "lri_batch_bind")
+        self.bound = True
+
+    def pack_data(self, snapshots: Sequence[np.ndarray]) -> np.ndarray:
+        h = np.zeros(self.totY, self.np_dtype)
+        for i, Y in enumerate(snapshots):
+            n, m = int(self.n[i]), int(self.m[i])
+            Y = np.asarray(Y)
+            if Y.shape != (n, m):
+                raise ValueError(f"instance {i}: snapshot shape {Y.shape} != {(n, m)}")
+            h[self.offY[i]:self.offY[i] + n * m] = Y.ravel(order="F")
+        return h
+
+    def data_init(self, snapshots: Sequence[np.ndarray]):
+        self.Ynext.copy_(self.torch.from_numpy(self.pack_data(snapshots)))
+        _native.check(self.lib.lri_batch_data_init(self.handle, C.c_void_p(self.Ynext.data_ptr()),
+                                                   self._stream()), "lri_batch_data_init")
+
+    def step(self, t: float, dt: float, nsteps: int = 1, next_snapshots=None):
+        """step!(integrator, alg, dt), ``nsteps`` times (asynchronous)."""
+        yptr = None
+        if self.op_kind == _native.LRI_OP_DATA:
+            if next_snapshots is None:
+                raise ValueError("data problems need the next snapshot")
+            if isinstance(next_snapshots, np.ndarray) and next_snapshots.ndim == 1:
+                self.Ynext.copy_(self.torch.from_numpy(next_snapshots.astype(self.np_dtype, copy=False)))
+            else:
+                self.Ynext.copy_(self.torch.from_numpy(self.pack_data(next_snapshots)))
+            yptr = C.c_void_p(self.Ynext.data_ptr())
+        _native.check(self.lib.lri_batch_step(self.handle, float(t), float(dt), int(nsteps), yptr,
+                                              self._stream()), "lri_batch_step")
+
+    def ranks(self) -> np.ndarray:
+        out = np.zeros(self.count, np.int64)
+        _native.check(self.lib.lri_batch_ranks(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64)),
+                                               self._stream()), "lri_batch_ranks")
+        return out
+
+    def check_status(self):
+        _native.check(self.lib.lri_batch_status(self.handle, self._stream()), "device status")
+
+    def download(self) -> List[SVDLikeRepresentation]:
+        ranks = self.ranks()
+        hU = self.U.cpu().numpy().astype(np.float64)
+        hS = self.S.cpu().numpy().astype(np.float64)
+        hV = self.V.cpu().numpy().astype(np.float64)
+        out = []
+        for i in range(self.count):
+            n, m, rc, r = int(self.n[i]), int(self.m[i]), int(self.rcap[i]), int(ranks[i])
+            U = hU[self.offU[i]:self.offU[i] + n * rc].reshape((n, rc), order="F")[:, :r].copy()
+            S = hS[self.offS[i]:self.offS[i] + rc * rc].reshape((rc, rc), order="F")[:r, :r].copy()
+            V = hV[self.offV[i]:self.offV[i] + m * rc].reshape((m, rc), order="F")[:, :r].copy()
+            out.append(SVDLikeRepresentation(U, S, V))
+        return out
+
+
+# ---------------------------------------------------------------------------
+# init / step / solve (src/primitives.jl:54-104; init at unconventional.jl:109-119)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class DLRIntegrator:
+    """src/primitives.jl:54-63, holding the device batch instead of a cache."""
+    u: SVDLikeRepresentation
+    t: float
+    dt: float
+    sol: DLRSolution
+    alg: object
+    batch: Batch
+    prob: object
+    iter: int = 0
+    _snap: int = 0
+
+
+def n_steps(tspan, dt) -> int:
+    """Iterations of the time loop ``while (tf - t)/T > 1e-8; t += dt``
+    (src/primitives.jl:70-74)."""
+    t0, tf = tspan
+    T = tf - t0
+    t = t0
+    k = 0
+    while (tf - t) / T > 1e-8:
+        t += dt
+        k += 1
+    return k
+
+
+def _init_sol(dt, t0, tf, u0) -> DLRSolution:
+    """src/primitives.jl:92-104."""
+    if isinstance(dt, (int, np.integer)) and isinstance(t0, (int, np.integer)):
+        steps = list(range(t0, tf + 1, dt))
+        return DLRSolution([None] * len(steps), [float(s) for s in steps])
+    n = int(math.floor((tf - t0) / dt)) + 1
+    return DLRSolution([None] * n, list(np.linspace(t0, tf, n)))
+
+
+def _op_kind(prob) -> int:
+    if isinstance(prob, MatrixDataProblem):
+        return _native.LRI_OP_DATA
+    f = prob.f
+    if isinstance(f, ZeroOperator):
+        return _native.LRI_OP_ZERO
+    if isinstance(f, SylvesterTridiagOperator):
+        return _native.LRI_OP_SYLVESTER_TRIDIAG
+    raise LriError(2, "flow map is not one of the engine's operators (arbitrary closures are unsupported)")
+
+
+def _data_at(prob: MatrixDataProblem, t):
+    if callable(prob.y):
+        return np.asarray(prob.y(t), dtype=np.float64)
+    idx = int(round(t))
+    if abs(t - idx) > 1e-12:
+        raise TypeError("discrete snapshot data needs an integer time step")
+    return np.asarray(prob.y[idx - 1], dtype=np.float64)
+
+
+def init(prob, alg, dt, precision: str = "fp64") -> DLRIntegrator:
+    t0, tf = prob.tspan
+    if not tf > t0:
+        raise AssertionError("Integration in reverse time direction is not supported")
+    u0 = prob.u0
+    n, m = u0.U.shape[0], u0.V.shape[0]
+    r = u0.S.shape[0]
+    rcap = r
+    if isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
+        rcap = max(r, min(alg.rmax, n // 2, m // 2))
+    b = Batch([n], [m], [r], alg, _op_kind(prob), precision, r_cap=[rcap])
+    b.upload([u0], [prob.f] if isinstance(prob, MatrixDEProblem) else None)
+    if isinstance(prob, MatrixDataProblem):
+        b.data_init([_data_at(prob, t0)])
+    sol = _init_sol(dt, t0, tf, u0)
+    sol.Y[0] = u0.copy()
+    return DLRIntegrator(u0.copy(), t0, dt, sol, alg, b, prob, 0)
+
+
+def step(integ: DLRIntegrator, alg=None, dt=None, sync_factors: bool = True) -> None:
+    """step!(integrator, alg, dt): one step on the device."""
+    dt = integ.dt if dt is None else dt
+    b = integ.batch
+    if isinstance(integ.prob, MatrixDataProblem):
+        b.step(integ.t, dt, 1, [_data_at(integ.prob, integ.t + dt)])
+    else:
+        b.step(integ.t, dt, 1)
+    integ.t += dt
+    integ.iter += 1
+    if sync_factors:
+        b.check_status()
+        integ.u = b.download()[0]
+
+
+def _update_sol(integ: DLRIntegrator) -> None:
+    """src/primitives.jl:82-90."""
+    if integ.iter <= len(integ.sol.Y) - 1:
+        integ.sol.Y[integ.iter] = integ.u.copy()
+        integ.sol.t[integ.iter] = integ.t
+    else:
+        integ.sol.Y.append(integ.u.copy())
+        integ.sol.t.append(integ.t)
+
+
+def solve(prob, alg, dt=None, precision: str = "fp64", save_everystep: bool = True) -> DLRSolution:
+    """solve(prob, alg, dt) (src/primitives.jl:68-80).  With
+    ``save_everystep=False`` only the initial and final factors are kept and
+    DE problems run all steps as one captured CUDA graph."""
+    if dt is None:
+        if not isinstance(prob, MatrixDataProblem) or callable(prob.y):
+            raise ValueError("If the data is not provided as array, integration stepsize needs to be specified")
+        dt = 1
+    integ = init(prob, alg, dt, precision)
+    T = prob.tspan[1] - prob.tspan[0]
+    if not save_everystep and not isinstance(prob, MatrixDataProblem):
+        k = n_steps(prob.tspan, dt)
+        integ.batch.step(integ.t, dt, k)
+        for _ in range(k):
+            integ.t += dt
+        integ.iter = k
+        integ.batch.check_status()
+        integ.u = integ.batch.download()[0]
+        integ.sol.Y = [integ.sol.Y[0], integ.u.copy()]
+        integ.sol.t = [integ.sol.t[0], integ.t]
+        integ.batch.close()
+        return integ.sol
+    while (prob.tspan[1] - integ.t) / T > 1e-8:
+        step(integ, alg, dt, sync_factors=save_everystep)
+        if save_everystep:
+            _update_sol(integ)
+    if not save_everystep:
+        integ.batch.check_status()
+        integ.u = integ.batch.download()[0]
+        integ.sol.Y = [integ.sol.Y[0], integ.u.copy()]
+        integ.sol.t = [integ.sol.t[0], integ.t]
+    integ.batch.close()
+    return integ.sol
+
+
+def solve_ensemble(probs: Sequence[MatrixDEProblem], alg, dt, precision: str = "fp32"
+                   ) -> List[SVDLikeRepresentation]:
+    """Advances many independent MatrixDEProblems with the same tspan and
+    operator kind in one batch; returns the final factors of each."""
+    tspan = probs[0].tspan
+    kinds = {_op_kind(p) for p in probs}
+    if len(kinds) != 1 or any(p.tspan != tspan for p in probs):
+        raise ValueError("ensemble members must share tspan and operator kind")
+    n = [p.u0.U.shape[0] for p in probs]
+    m = [p.u0.V.shape[0] for p in probs]
+    r = [p.u0.S.shape[0] for p in probs]
+    b = Batch(n, m, r, alg, kinds.pop(), precision)
+    b.upload([p.u0 for p in probs], [p.f for p in probs])
+    k = n_steps(tspan, dt)
+    b.step(tspan[0], dt, k)
+    b.check_status()
+    out = b.download()
+    b.close()
+    return out

@@ -1,0 +1,114 @@
+"""ctypes binding of the C ABI in include/lri.h (liblri_gb300.so).
+
+This is the same binding a Julia ``ccall`` shim makes: plain pointers, sizes
+and small structs.  Loading fails loudly when the library or a CUDA device
+is missing; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+from . import _build
+
+LRI_OK = 0
+STATUS_NAMES = {
+    0: "LRI_OK", 1: "LRI_ERR_ARG", 2: "LRI_ERR_UNSUPPORTED", 3: "LRI_ERR_BREAKDOWN",
+    4: "LRI_ERR_NONFINITE", 5: "LRI_ERR_RANK_OVERFLOW", 6: "LRI_ERR_TIMEOUT", 7: "LRI_ERR_CUDA",
+    8: "LRI_ERR_STATE",
+}
+
+LRI_F64, LRI_F32 = 0, 1
+LRI_ALG_BUG, LRI_ALG_RA_BUG, LRI_ALG_KSL = 0, 1, 2
+LRI_KSL_PRIMAL, LRI_KSL_DUAL, LRI_KSL_STRANG = 0, 1, 2
+LRI_OP_ZERO, LRI_OP_SYLVESTER_TRIDIAG, LRI_OP_BURGERS_PERIODIC, LRI_OP_DATA = 0, 1, 2, 3
+
+# Every symbol include/lri.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "lri_abi_version", "lri_status_str", "lri_device_info", "lri_batch_create", "lri_batch_destroy",
+    "lri_batch_layout", "lri_batch_bind", "lri_batch_data_layout", "lri_batch_data_init", "lri_batch_step",
+    "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step",
+]
+
+
+class LriError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        super().__init__(f"{where}: {STATUS_NAMES.get(code, code)}")
+
+
+class lri_scheme(C.Structure):
+    _fields_ = [("nstages", C.c_int32), ("nsub", C.c_int32), ("a", C.c_double * 4),
+                ("b", C.c_double * 4), ("c", C.c_double * 4)]
+
+
+class lri_alg_desc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ksl_order", C.c_int32), ("K_alg", lri_scheme),
+                ("L_alg", lri_scheme), ("S_alg", lri_scheme), ("tol", C.c_double),
+                ("r_min", C.c_int32), ("reserved", C.c_int32)]
+
+
+class lri_batch_desc(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("op", C.c_int32), ("count", C.c_int32), ("reserved", C.c_int32),
+                ("n", C.POINTER(C.c_int64)), ("m", C.POINTER(C.c_int64)), ("r", C.POINTER(C.c_int64)),
+                ("r_cap", C.POINTER(C.c_int64)), ("burgers_h", C.c_double), ("burgers_alpha", C.c_double),
+                ("burgers_beta", C.c_double)]
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def _declare(lib: C.CDLL) -> None:
+    P = C.c_void_p
+    I64P = C.POINTER(C.c_int64)
+    lib.lri_abi_version.restype = C.c_int
+    lib.lri_status_str.restype = C.c_char_p
+    lib.lri_status_str.argtypes = [C.c_int]
+    lib.lri_device_info.restype = C.c_int
+    lib.lri_device_info.argtypes = [C.POINTER(C.c_int)] * 4
+    lib.lri_batch_create.restype = C.c_int
+    lib.lri_batch_create.argtypes = [C.POINTER(P), C.POINTER(lri_batch_desc), C.POINTER(lri_alg_desc)]
+    lib.lri_batch_destroy.restype = C.c_int
+    lib.lri_batch_destroy.argtypes = [P]
+    lib.lri_batch_layout.restype = C.c_int
+    lib.lri_batch_layout.argtypes = [P, I64P, I64P, I64P, I64P, I64P, I64P]
+    lib.lri_batch_bind.restype = C.c_int
+    lib.lri_batch_bind.argtypes = [P, P, P, P, P, P]
+    lib.lri_batch_data_layout.restype = C.c_int
+    lib.lri_batch_data_layout.argtypes = [P, I64P, I64P]
+    lib.lri_batch_data_init.restype = C.c_int
+    lib.lri_batch_data_init.argtypes = [P, P, P]
+    lib.lri_batch_step.restype = C.c_int
+    lib.lri_batch_step.argtypes = [P, C.c_double, C.c_double, C.c_int32, P, P]
+    lib.lri_batch_ranks.restype = C.c_int
+    lib.lri_batch_ranks.argtypes = [P, I64P, P]
+    lib.lri_batch_status.restype = C.c_int
+    lib.lri_batch_status.argtypes = [P, P]
+    lib.lri_batch_launches_per_step.restype = C.c_int32
+    lib.lri_batch_launches_per_step.argtypes = [P]
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads liblri_gb300.so (building it when missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if build_if_missing and _build.is_stale():
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"liblri_gb300.so is missing ({path}); run the build first")
+    lib = C.CDLL(path)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def check(code: int, where: str) -> None:
+    if code != LRI_OK:
+        raise LriError(code, where)

@@ -1,0 +1,600 @@
+// engine.cuh - CTA-level building blocks of the instance engine.
+//
+// One CTA advances one DLRA instance by one full integrator step: the K-, L-
+// and S-substeps, the orthogonalisations and (rank-adaptive) the core SVD
+// and truncation.  Everything here is written for a 256-thread CTA; tall
+// n x r "panels" live in global scratch (L1/L2 resident while the CTA works
+// on them), small r x r matrices in global scratch as well, and every tile
+// product is staged through shared memory with 4x4 register micro-tiles.
+//
+// Matrices are column-major unless stated otherwise.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "engine_api.h"
+
+namespace lri {
+
+constexpr int NT = 256;        // threads per CTA
+constexpr int NW = NT / 32;    // warps per CTA
+constexpr int KC = 32;         // k-chunk of the tile products
+constexpr int TRMAX = 256;     // maximum rows per staged tile
+constexpr int STAGE_ELEMS = 12288;  // shared staging area (elements of T)
+constexpr int WMAX = 64;       // widest panel (columns) handled by the engine
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum: every thread returns the same value.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = T(0);
+#pragma unroll
+  for (int w = 0; w < NW; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ void ld4(const float* p, float v[4]) {
+  float4 x = *reinterpret_cast<const float4*>(p);
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double v[4]) {
+  double2 x = *reinterpret_cast<const double2*>(p);
+  double2 y = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
+
+__device__ __forceinline__ bool is_finite_val(float x) { return isfinite(x); }
+__device__ __forceinline__ bool is_finite_val(double x) { return isfinite(x); }
+
+// Shared-memory workspace of one CTA.
+template <typename T>
+struct Smem {
+  T red[32];
+  T vec[2 * WMAX + 8];
+  T stage[STAGE_ELEMS];
+};
+
+// ---------------------------------------------------------------------------
+// Tile product  OUT(N x c) = X(N x a) * W(a x c)
+//   X is produced row-tile by row-tile by a loader functor:
+//     ldx(xs, i0, rows, k0, kc, TR)  fills xs[kk*TR + ii] = X(i0+ii, k0+kk)
+//     (ii < TR; rows beyond `rows` must be zero)
+//   W by  ldw(ws, k0, kc, ldws, c)    fills ws[kk*ldws + cc] = W(k0+kk, cc)
+//     (cc < ldws; columns beyond c zero)
+//   The epilogue epi(i, cc, value) is called once per valid output element.
+// Ends with __syncthreads().
+// ---------------------------------------------------------------------------
+template <typename T, class LX, class LW, class EPI>
+__device__ void tile_gemm(int N, int a, int c, T* stage, const LX& ldx, const LW& ldw, const EPI& epi) {
+  const int tid = threadIdx.x;
+  const int c4 = (c + 3) >> 2;
+  const int ldws = c4 * 4;
+  int ng = NT / c4;
+  int TR = 4 * ng;
+  if (TR > TRMAX) TR = TRMAX;
+  ng = TR / 4;
+  T* xs = stage;
+  T* ws = stage + TR * KC;
+  const int cg = tid % c4, rg = tid / c4;
+  const bool active = rg < ng;
+  for (int i0 = 0; i0 < N; i0 += TR) {
+    const int rows = min(TR, N - i0);
+    T acc[4][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+    for (int k0 = 0; k0 < a; k0 += KC) {
+      const int kc = min(KC, a - k0);
+      ldx(xs, i0, rows, k0, kc, TR);
+      ldw(ws, k0, kc, ldws, c);
+      __syncthreads();
+      if (active) {
+        for (int kk = 0; kk < kc; ++kk) {
+          T xv[4], wv[4];
+          ld4(xs + kk * TR + 4 * rg, xv);
+          ld4(ws + kk * ldws + 4 * cg, wv);
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], wv[q], acc[p][q]);
+        }
+      }
+      __syncthreads();
+    }
+    if (active) {
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int ii = 4 * rg + p;
+        if (ii < rows) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int cc = 4 * cg + q;
+            if (cc < c) epi(i0 + ii, cc, acc[p][q]);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Loader: plain column-major panel X (ld ldx), columns [col0, col0+a).
+template <typename T>
+struct LoadPanel {
+  const T* X;
+  int ldx;
+  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
+    for (int e = threadIdx.x; e < kc * TR; e += NT) {
+      const int kk = e / TR, ii = e - kk * TR;
+      xs[e] = (ii < rows) ? X[(int64_t)(i0 + ii) + (int64_t)(k0 + kk) * ldx] : T(0);
+    }
+  }
+};
+
+// Loader: [T z | z] for a tridiagonal T (sub, dia, sup each length N,
+// non-periodic: rows -1 and N are zero).  Width 2r.
+template <typename T>
+struct LoadStencilAug {
+  const T* Z;
+  int ldz, N, r;
+  const T* tri;  // [sub | dia | sup]
+  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
+    for (int e = threadIdx.x; e < kc * TR; e += NT) {
+      const int kk = e / TR, ii = e - kk * TR;
+      const int k = k0 + kk;
+      T v = T(0);
+      if (ii < rows) {
+        const int i = i0 + ii;
+        if (k < r) {
+          const T* col = Z + (int64_t)k * ldz;
+          v = tri[N + i] * col[i];
+          if (i > 0) v = fma(tri[i], col[i - 1], v);
+          if (i + 1 < N) v = fma(tri[2 * N + i], col[i + 1], v);
+        } else {
+          v = Z[i + (int64_t)(k - r) * ldz];
+        }
+      }
+      xs[e] = v;
+    }
+  }
+};
+
+// Loader: Δy = Ynext - Yprev restricted to rows (n x m column-major), or its
+// transpose when `trans` (then X is m x n).
+template <typename T>
+struct LoadDelta {
+  const T* Yn;
+  const T* Yp;
+  int n;      // rows of Y (leading dimension)
+  bool trans;
+  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
+    for (int e = threadIdx.x; e < kc * TR; e += NT) {
+      int kk, ii;
+      if (!trans) { kk = e / TR; ii = e - kk * TR; }
+      else { ii = e / kc; kk = e - ii * kc; }  // consecutive threads walk along Y's columns
+      T v = T(0);
+      if (ii < rows) {
+        const int64_t idx = trans ? (int64_t)(k0 + kk) + (int64_t)(i0 + ii) * n
+                                  : (int64_t)(i0 + ii) + (int64_t)(k0 + kk) * n;
+        v = Yn[idx] - Yp[idx];
+      }
+      xs[kk * TR + ii] = v;
+    }
+  }
+};
+
+// W loader: column-major matrix W (ld ldw0) or its transpose.
+template <typename T>
+struct LoadSmall {
+  const T* W;
+  int ld;
+  bool trans;  // true: W(k, c) = M[c + k*ld]
+  __device__ void operator()(T* ws, int k0, int kc, int ldws, int c) const {
+    for (int e = threadIdx.x; e < kc * ldws; e += NT) {
+      const int kk = e / ldws, cc = e - kk * ldws;
+      T v = T(0);
+      if (cc < c) {
+        const int k = k0 + kk;
+        v = trans ? W[cc + (int64_t)k * ld] : W[k + (int64_t)cc * ld];
+      }
+      ws[e] = v;
+    }
+  }
+};
+
+// W loader for the Sylvester K/L rhs: W = [G ; P^T]  (2r x r), G and P r x r
+// column-major with leading dimension ld.
+template <typename T>
+struct LoadGP {
+  const T* G;
+  const T* P;
+  int ld, r;
+  __device__ void operator()(T* ws, int k0, int kc, int ldws, int c) const {
+    for (int e = threadIdx.x; e < kc * ldws; e += NT) {
+      const int kk = e / ldws, cc = e - kk * ldws;
+      T v = T(0);
+      if (cc < c) {
+        const int k = k0 + kk;
+        v = (k < r) ? G[k + (int64_t)cc * ld] : P[cc + (int64_t)(k - r) * ld];
+      }
+      ws[e] = v;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Gram-type reduction  OUT(a x c) = X(N x a)^T * Y(N x c) (a <= 64, c <= 128), written to a
+// column-major destination (ld ldo), optionally scaled and accumulated:
+//   out = alpha * X^T Y + beta * out.
+// X rows come from loader lx(xs, i0, rows, lda_s) writing row-major
+// xs[ii*lda_s + k]; Y likewise.  Ends with __syncthreads().
+// ---------------------------------------------------------------------------
+constexpr int TRG = 32;
+
+template <typename T>
+struct RowLoadPanel {  // row-major staging of a column-major panel
+  const T* X;
+  int ldx, w;
+  __device__ void operator()(T* xs, int i0, int rows, int lds) const {
+    for (int e = threadIdx.x; e < TRG * w; e += NT) {
+      const int k = e / TRG, ii = e - k * TRG;
+      xs[ii * lds + k] = (ii < rows) ? X[(int64_t)(i0 + ii) + (int64_t)k * ldx] : T(0);
+    }
+  }
+};
+
+template <typename T>
+struct RowLoadStencilAug {  // row-major staging of [Z | T Z] (note order), width 2r
+  const T* Z;
+  int ldz, N, r;
+  const T* tri;
+  __device__ void operator()(T* xs, int i0, int rows, int lds) const {
+    for (int e = threadIdx.x; e < TRG * 2 * r; e += NT) {
+      const int k = e / TRG, ii = e - k * TRG;
+      T v = T(0);
+      if (ii < rows) {
+        const int i = i0 + ii;
+        if (k < r) {
+          v = Z[i + (int64_t)k * ldz];
+        } else {
+          const T* col = Z + (int64_t)(k - r) * ldz;
+          v = tri[N + i] * col[i];
+          if (i > 0) v = fma(tri[i], col[i - 1], v);
+          if (i + 1 < N) v = fma(tri[2 * N + i], col[i + 1], v);
+        }
+      }
+      xs[ii * lds + k] = v;
+    }
+  }
+};
+
+template <typename T, class LXr, class LYr>
+__device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LYr& ly, T* out, int ldo,
+                          T alpha, T beta) {
+  const int tid = threadIdx.x;
+  const int a4 = (a + 3) >> 2, c4 = (c + 3) >> 2;
+  const int MT = a4 * c4;
+  const int lxs = a4 * 4 + 4, lys = c4 * 4 + 4;
+  T* xs = stage;
+  T* ys = stage + TRG * lxs;
+  const int splits = (MT >= NT) ? 1 : (NT / MT);
+  const int per = (MT + NT - 1) / NT;  // micro-tiles per thread when splits == 1 (<= 2)
+  T acc[2][16];
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[u][e] = T(0);
+  const int mt0 = (splits > 1) ? (tid % MT) : tid;
+  const int split = (splits > 1) ? (tid / MT) : 0;
+  const bool active = (splits > 1) ? (tid < MT * splits) : true;
+  for (int i0 = 0; i0 < N; i0 += TRG) {
+    const int rows = min(TRG, N - i0);
+    lx(xs, i0, rows, lxs);
+    ly(ys, i0, rows, lys);
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u < per) {
+          const int mt = mt0 + u * NT;
+          if (mt < MT) {
+            const int ma = mt / c4, mc = mt - ma * c4;
+            for (int ii = split; ii < rows; ii += splits) {
+              T xv[4], yv[4];
+              ld4(xs + ii * lxs + 4 * ma, xv);
+              ld4(ys + ii * lys + 4 * mc, yv);
+#pragma unroll
+              for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[u][p * 4 + q] = fma(xv[p], yv[q], acc[u][p * 4 + q]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // combine splits through shared memory (deterministic order)
+  T* part = stage;  // splits * MT * 16 <= NT*16 elements
+  if (splits > 1) {
+    if (active) {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) part[(split * MT + mt0) * 16 + e] = acc[0][e];
+    }
+    __syncthreads();
+    for (int o = tid; o < MT * 16; o += NT) {
+      const int mt = o >> 4, e = o & 15;
+      T s = T(0);
+      for (int sp = 0; sp < splits; ++sp) s += part[(sp * MT + mt) * 16 + e];
+      const int ma = mt / c4, mc = mt - ma * c4;
+      const int ia = 4 * ma + (e >> 2), jc = 4 * mc + (e & 3);
+      if (ia < a && jc < c) {
+        T* d = out + ia + (int64_t)jc * ldo;
+        *d = (beta == T(0)) ? alpha * s : fma(alpha, s, beta * *d);
+      }
+    }
+    __syncthreads();
+  } else {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (u < per) {
+        const int mt = mt0 + u * NT;
+        if (mt < MT) {
+          const int ma = mt / c4, mc = mt - ma * c4;
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int ia = 4 * ma + (e >> 2), jc = 4 * mc + (e & 3);
+            if (ia < a && jc < c) {
+              T* d = out + ia + (int64_t)jc * ldo;
+              *d = (beta == T(0)) ? alpha * acc[u][e] : fma(alpha, acc[u][e], beta * *d);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small dense products on column-major matrices in global scratch:
+//   C(p x s) = alpha * op(A)(p x q) * op(B)(q x s) + beta * C
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ void small_gemm(int p, int q, int s, T alpha, const T* A, int lda, bool ta, const T* B, int ldb,
+                           bool tb, T beta, T* C, int ldc) {
+  for (int o = threadIdx.x; o < p * s; o += NT) {
+    const int i = o % p, j = o / p;
+    T acc = T(0);
+    for (int k = 0; k < q; ++k) {
+      const T av = ta ? A[k + (int64_t)i * lda] : A[i + (int64_t)k * lda];
+      const T bv = tb ? B[j + (int64_t)k * ldb] : B[k + (int64_t)j * ldb];
+      acc = fma(av, bv, acc);
+    }
+    T* d = C + i + (int64_t)j * ldc;
+    *d = (beta == T(0)) ? alpha * acc : fma(alpha, acc, beta * *d);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void copy_mat(int p, int q, const T* A, int lda, T* B, int ldb) {
+  for (int o = threadIdx.x; o < p * q; o += NT) {
+    const int i = o % p, j = o / p;
+    B[i + (int64_t)j * ldb] = A[i + (int64_t)j * lda];
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void zero_mat(int p, int q, T* A, int lda) {
+  for (int o = threadIdx.x; o < p * q; o += NT) {
+    const int i = o % p, j = o / p;
+    A[i + (int64_t)j * lda] = T(0);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Householder QR of the N x W panel A (column-major, ld lda), N >= W, in the
+// LAPACK convention (beta = -sign(alpha) * ||x||, v(k) = 1).  On exit the
+// upper triangle of A holds R and the explicit thin Q (N x W) is written to Q.
+// `sm` provides reduction space (vec needs >= W + 8 entries).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, int ldq, Smem<T>& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T* tau = sm.vec;            // [W]
+  T* wv = sm.vec + WMAX;      // [W]
+  T* wred = sm.stage;         // [NW * W]
+  for (int k = 0; k < W; ++k) {
+    T* colk = A + (int64_t)k * lda;
+    T loc = T(0);
+    for (int i = k + 1 + tid; i < N; i += NT) {
+      const T x = colk[i];
+      loc = fma(x, x, loc);
+    }
+    const T xn2 = block_sum(loc, sm.red);
+    const T alpha = colk[k];
+    T tk = T(0), beta = alpha, scal = T(0);
+    if (xn2 > T(0)) {
+      beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+      tk = (beta - alpha) / beta;
+      scal = T(1) / (alpha - beta);
+    }
+    if (tk != T(0))
+      for (int i = k + 1 + tid; i < N; i += NT) colk[i] *= scal;
+    if (tid == 0) tau[k] = tk;
+    __syncthreads();
+    const int nj = W - k - 1;
+    if (nj > 0 && tk != T(0)) {
+      for (int j = 0; j < nj; ++j) {
+        const T* colj = A + (int64_t)(k + 1 + j) * lda;
+        T p = T(0);
+        for (int i = k + 1 + tid; i < N; i += NT) p = fma(colk[i], colj[i], p);
+        p = warp_sum(p);
+        if (lane == 0) wred[warp * WMAX + j] = p;
+      }
+      __syncthreads();
+      if (tid < nj) {
+        T s = A[k + (int64_t)(k + 1 + tid) * lda];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) s += wred[w * WMAX + tid];
+        wv[tid] = tk * s;
+      }
+      __syncthreads();
+      const int len = N - k;
+      for (int e = tid; e < len * nj; e += NT) {
+        const int j = e / len, ii = e - j * len;
+        const int i = k + ii;
+        const T vi = (ii == 0) ? T(1) : colk[i];
+        A[i + (int64_t)(k + 1 + j) * lda] -= vi * wv[j];
+      }
+      __syncthreads();
+    }
+    if (tid == 0) colk[k] = beta;
+    __syncthreads();
+  }
+  // explicit thin Q by backward accumulation: Q = H_0 ... H_{W-1} [I; 0]
+  for (int e = tid; e < N * W; e += NT) {
+    const int j = e / N, i = e - j * N;
+    Q[i + (int64_t)j * ldq] = (i == j) ? T(1) : T(0);
+  }
+  __syncthreads();
+  for (int k = W - 1; k >= 0; --k) {
+    const T tk = tau[k];
+    if (tk == T(0)) continue;
+    const T* colk = A + (int64_t)k * lda;
+    const int nj = W - k;
+    for (int j = 0; j < nj; ++j) {
+      const T* qj = Q + (int64_t)(k + j) * ldq;
+      T p = (tid == 0) ? qj[k] : T(0);
+      for (int i = k + 1 + tid; i < N; i += NT) p = fma(colk[i], qj[i], p);
+      p = warp_sum(p);
+      if (lane == 0) wred[warp * WMAX + j] = p;
+    }
+    __syncthreads();
+    if (tid < nj) {
+      T s = T(0);
+#pragma unroll
+      for (int w = 0; w < NW; ++w) s += wred[w * WMAX + tid];
+      wv[tid] = tk * s;
+    }
+    __syncthreads();
+    const int len = N - k;
+    for (int e = tid; e < len * nj; e += NT) {
+      const int j = e / len, ii = e - j * len;
+      const int i = k + ii;
+      const T vi = (ii == 0) ? T(1) : colk[i];
+      Q[i + (int64_t)(k + j) * ldq] -= vi * wv[j];
+    }
+    __syncthreads();
+  }
+}
+
+// Copies the upper triangle of the factored panel (R, W x W) to R (ld ldr).
+template <typename T>
+__device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
+  for (int o = threadIdx.x; o < W * W; o += NT) {
+    const int i = o % W, j = o / W;
+    R[i + (int64_t)j * ldr] = (i <= j) ? A[i + (int64_t)j * lda] : T(0);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// One-sided Jacobi SVD of the P x P matrix B (column-major, ld ldb) held in
+// shared memory `a` (P x P, ld P) with right vectors in `v` (P x P).
+// On exit: sigma[j] (descending), a's columns = left singular vectors,
+// v's columns = right singular vectors, both permuted to the sorted order
+// through perm[].  Returns false if it did not converge.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T eps = (sizeof(T) == 4) ? T(1.2e-7) : T(2.3e-16);
+  for (int o = tid; o < P * P; o += NT) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
+  const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
+  bool converged = false;
+  for (int sweep = 0; sweep < 40 && !converged; ++sweep) {
+    if (tid == 0) *flag = 0;
+    __syncthreads();
+    for (int rnd = 0; rnd < Pe - 1; ++rnd) {
+      for (int pr = warp; pr < Pe / 2; pr += NW) {
+        int p, q;
+        if (pr == 0) { p = rnd % (Pe - 1); q = Pe - 1; }
+        else { p = (rnd + pr) % (Pe - 1); q = (rnd - pr + (Pe - 1)) % (Pe - 1); }
+        if (p >= P || q >= P) continue;
+        if (p > q) { int tmp = p; p = q; q = tmp; }
+        T* ap = a + p * P;
+        T* aq = a + q * P;
+        T al = T(0), be = T(0), ga = T(0);
+        for (int i = lane; i < P; i += 32) {
+          const T x = ap[i], y = aq[i];
+          al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
+        }
+        al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+        if (fabs(ga) > eps * sqrt(al * be) && ga != T(0)) {
+          const T zeta = (be - al) / (T(2) * ga);
+          const T tt = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          const T cs = T(1) / sqrt(T(1) + tt * tt);
+          const T sn = cs * tt;
+          for (int i = lane; i < P; i += 32) {
+            const T x = ap[i], y = aq[i];
+            ap[i] = cs * x - sn * y;
+            aq[i] = sn * x + cs * y;
+          }
+          T* vp = v + p * P;
+          T* vq = v + q * P;
+          for (int i = lane; i < P; i += 32) {
+            const T x = vp[i], y = vq[i];
+            vp[i] = cs * x - sn * y;
+            vq[i] = sn * x + cs * y;
+          }
+          if (lane == 0) *flag = 1;
+        }
+      }
+      __syncthreads();
+    }
+    converged = (*flag == 0);
+    __syncthreads();
+  }
+  // singular values = column norms
+  for (int j = warp; j < P; j += NW) {
+    T s = T(0);
+    for (int i = lane; i < P; i += 32) s = fma(a[j * P + i], a[j * P + i], s);
+    s = warp_sum(s);
+    if (lane == 0) sigma[j] = sqrt(s);
+  }
+  __syncthreads();
+  if (tid == 0) {  // selection sort of indices by descending sigma (P <= 128)
+    for (int j = 0; j < P; ++j) perm[j] = j;
+    for (int j = 0; j < P; ++j) {
+      int best = j;
+      for (int k = j + 1; k < P; ++k)
+        if (sigma[perm[k]] > sigma[perm[best]]) best = k;
+      const int tmp = perm[j]; perm[j] = perm[best]; perm[best] = tmp;
+    }
+  }
+  __syncthreads();
+  return converged;
+}
+
+}  // namespace lri

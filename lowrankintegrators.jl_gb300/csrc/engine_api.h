@@ -1,0 +1,65 @@
+// engine_api.h - host/device shared definitions of the instance engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace lri {
+
+enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2 };
+enum KslOrder : int32_t { KSL_PRIMAL = 0, KSL_DUAL = 1, KSL_STRANG = 2 };
+enum OpKind : int32_t { OP_ZERO = 0, OP_SYLVESTER = 1, OP_BURGERS = 2, OP_DATA = 3 };
+
+// Device status bits (OR-ed into the batch status word).
+enum StatusBits : uint32_t {
+  ST_NONFINITE = 1u,
+  ST_SVD_NOCONV = 2u,
+  ST_RANK_OVERFLOW = 4u,
+  ST_BAD_SHAPE = 8u,
+};
+
+struct Scheme {
+  int32_t nstages, nsub;
+  double a[4], b[4], c[4];
+};
+
+// Per-instance descriptor (device resident).
+struct InstDesc {
+  int32_t n, m, rcap, wcap;  // wcap: widest panel (rcap, or 2*rcap for RA)
+  int64_t offU, offS, offV;  // caller buffers
+  int64_t offA, offB;        // operator coefficients
+  int64_t offWK, offWL;      // K-side / L-side panel workspaces
+  int64_t offSmall;          // small-matrix scratch
+  int64_t offY;              // data snapshots (n x m)
+};
+
+template <typename T>
+struct StepArgs {
+  const InstDesc* inst;
+  const int32_t* order;
+  int32_t* rank;
+  int32_t* proj_valid;
+  uint32_t* status;
+  T* U;
+  T* S;
+  T* V;
+  const T* opA;
+  const T* opB;
+  T* work;
+  T* small;
+  T* Yprev;
+  const T* Ynext;
+  double t, dt;
+  int32_t alg, ksl_order, op, r_min;
+  double tol;
+  Scheme sK, sL, sS;
+  double bh, balpha, bbeta;
+};
+
+template <typename T>
+cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream);
+template <typename T>
+size_t step_smem_bytes();
+
+}  // namespace lri

@@ -1,0 +1,467 @@
+// engine.cu - the instance engine: one CTA advances one DLRA instance by one
+// integrator step (BUG, rank-adaptive BUG, or KSL), for a whole batch of
+// independent instances per launch.
+//
+// Reference correspondence (paths within LowRankIntegrators.jl):
+//   bug_step      src/integrators/unconventional.jl:133-157
+//   ra_bug_step   src/integrators/rank_adaptive_unconventional.jl:194-233
+//   ksl_primal    src/integrators/projector_splitting.jl:129-152
+//   ksl_dual      src/integrators/projector_splitting.jl:166-189
+//   Strang        src/integrators/projector_splitting.jl:205-211
+//   data substeps src/integrators/data_integrator.jl:13-16 (u += sign*left'*Δy*right)
+//   K/L/S rhs     src/integrators/unconventional.jl:52-54,62-64,72-74
+#pragma once
+#include "engine.cuh"
+#include "engine_api.h"
+
+namespace lri {
+
+// Workspace layout of one side (rows N): five panels.
+template <typename T>
+struct Side {
+  int N;
+  T* X;            // caller's basis (U or V), ld N
+  const T* tri;    // tridiagonal coefficients of this side's operator (3N)
+  T* PY;           // N x W : substep state / QR panel
+  T* PQ;           // N x W : explicit Q
+  T* PA;           // N x rcap : RK accumulator
+  T* PZ0;          // N x rcap : RK stage input (ping)
+  T* PZ1;          // N x rcap : RK stage input (pong)
+};
+
+template <typename T>
+struct Inst {
+  int n, m, rcap, W, inst;
+  T* U;
+  T* S;
+  T* V;
+  Side<T> k, l;
+  T* small;   // 15 blocks of W*W
+  const T* Yp;
+  const T* Yn;
+  T* Ypw;     // writable previous snapshot
+  __device__ T* blk(int i) const { return small + (int64_t)i * W * W; }
+};
+
+// small-scratch block indices
+enum : int { B_GU = 0, B_GV = 2, B_M = 4, B_N = 5, B_ST = 6, B_SA = 7, B_SZ0 = 8, B_SZ1 = 9, B_SK = 10,
+             B_T1 = 11, B_T2 = 12, B_RK = 13, B_RL = 14, B_COUNT = 15 };
+
+// Projections of a basis X (N x w) needed by the Sylvester rhs:
+//   G = X^T X  (at dst, ld W),  P = X^T (T X)  (at dst + w*W, ld W).
+template <typename T>
+__device__ __noinline__ void projections(const Inst<T>& I, const T* X, int N, int w, const T* tri, T* dst, Smem<T>& sm) {
+  tile_gram<T>(N, w, 2 * w, sm.stage, RowLoadPanel<T>{X, N, w}, RowLoadStencilAug<T>{X, N, N, w, tri}, dst, I.W,
+               T(1), T(0));
+}
+
+// One substep of side `sd` on the panel Y (N x r, ld N), in place.
+//   Sylvester: Y' = T Y G + Y P^T  with (G, P) the projections of the other
+//              side's basis (K: V^T V, V^T B V; L: U^T U, U^T A U).
+//   Data:      Y += Δy Xo (K side) or Δy^T Xo (L side).
+//   Zero:      nothing.
+template <typename T>
+__device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<T>& sd, int side, T* Y, int r,
+                             const T* Gp, const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
+  const int N = sd.N;
+  if (g.op == OP_ZERO) return;
+  if (g.op == OP_DATA) {
+    const int a = (side == 0) ? I.m : I.n;
+    const int ldo = (side == 0) ? I.m : I.n;
+    tile_gemm<T>(N, a, r, sm.stage, LoadDelta<T>{I.Yn, I.Yp, I.n, side == 1}, LoadSmall<T>{Xo, ldo, false},
+                 [&](int i, int cc, T v) { Y[i + (int64_t)cc * N] += v; });
+    return;
+  }
+  // Sylvester tridiagonal
+  const T* G = Gp;
+  const T* P = Gp + (int64_t)r * I.W;
+  const int ns = sc.nstages;
+  const T h = T(dt / sc.nsub);
+  T* Zb[2] = {sd.PZ0, sd.PZ1};
+  T* PA = sd.PA;
+  for (int sub = 0; sub < sc.nsub; ++sub) {
+    for (int s = 0; s < ns; ++s) {
+      const T* Zin = (s == 0) ? Y : Zb[(s - 1) & 1];
+      T* Zout = Zb[s & 1];
+      const T bs = T(sc.b[s]);
+      const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
+      tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{Zin, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
+                   [&](int i, int cc, T kv) {
+                     const int64_t idx = i + (int64_t)cc * N;
+                     if (ns == 1) {
+                       Zout[idx] = fma(h * bs, kv, Y[idx]);
+                     } else if (s == 0) {
+                       PA[idx] = bs * kv;
+                       Zout[idx] = fma(h * an, kv, Y[idx]);
+                     } else if (s + 1 < ns) {
+                       PA[idx] = fma(bs, kv, PA[idx]);
+                       Zout[idx] = fma(h * an, kv, Y[idx]);
+                     } else {
+                       Y[idx] = fma(h, fma(bs, kv, PA[idx]), Y[idx]);
+                     }
+                   });
+      if (ns == 1) copy_mat<T>(N, r, Zout, N, Y, N);
+    }
+  }
+}
+
+// S-substep on the p x q core St (ld W):
+//   Sylvester: S' = sign * (P_U S G_V + G_U S P_V^T)
+//   Data:      S += sign * U^T Δy V   (exact flow)
+template <typename T>
+__device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I, T* St, int p, int q, T sign, const T* GUp,
+                             const T* GVp, const T* Ub, const T* Vb, const Scheme& sc, double dt, Smem<T>& sm) {
+  const int W = I.W;
+  if (g.op == OP_ZERO) return;
+  if (g.op == OP_DATA) {
+    // Z = Δy V (n x q) into the K-side QR panel (free at this point), then St += sign * U^T Z
+    T* Z = I.k.PY;
+    const int n = I.n;
+    tile_gemm<T>(n, I.m, q, sm.stage, LoadDelta<T>{I.Yn, I.Yp, n, false}, LoadSmall<T>{Vb, I.m, false},
+                 [&](int i, int cc, T v) { Z[i + (int64_t)cc * n] = v; });
+    tile_gram<T>(n, p, q, sm.stage, RowLoadPanel<T>{Ub, n, p}, RowLoadPanel<T>{Z, n, q}, St, W, sign, T(1));
+    return;
+  }
+  const T* GU = GUp;
+  const T* PU = GUp + (int64_t)p * W;
+  const T* GV = GVp;
+  const T* PV = GVp + (int64_t)q * W;
+  T* SA = I.blk(B_SA);
+  T* SZ[2] = {I.blk(B_SZ0), I.blk(B_SZ1)};
+  T* SK = I.blk(B_SK);
+  T* T1 = I.blk(B_T1);
+  T* T2 = I.blk(B_T2);
+  const int ns = sc.nstages;
+  const T h = T(dt / sc.nsub);
+  for (int sub = 0; sub < sc.nsub; ++sub) {
+    for (int s = 0; s < ns; ++s) {
+      const T* Z = (s == 0) ? St : SZ[(s - 1) & 1];
+      // SK = sign * (PU (Z GV) + GU (Z PV^T))
+      small_gemm<T>(p, q, q, T(1), Z, W, false, GV, W, false, T(0), T1, W);
+      small_gemm<T>(p, q, q, T(1), Z, W, false, PV, W, true, T(0), T2, W);
+      small_gemm<T>(p, p, q, sign, PU, W, false, T1, W, false, T(0), SK, W);
+      small_gemm<T>(p, p, q, sign, GU, W, false, T2, W, false, T(1), SK, W);
+      const T bs = T(sc.b[s]);
+      const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
+      T* Zout = SZ[s & 1];
+      for (int o = threadIdx.x; o < p * q; o += NT) {
+        const int i = o % p, j = o / p;
+        const int64_t idx = i + (int64_t)j * W;
+        const T kv = SK[idx];
+        if (ns == 1) {
+          St[idx] = fma(h * bs, kv, St[idx]);
+        } else if (s == 0) {
+          SA[idx] = bs * kv;
+          Zout[idx] = fma(h * an, kv, St[idx]);
+        } else if (s + 1 < ns) {
+          SA[idx] = fma(bs, kv, SA[idx]);
+          Zout[idx] = fma(h * an, kv, St[idx]);
+        } else {
+          St[idx] = fma(h, fma(bs, kv, SA[idx]), St[idx]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// K0 = X * C (C = S, or S^T when trans) into panel Y (N x r).
+template <typename T>
+__device__ void form_k0(const Inst<T>& I, const T* X, int N, const T* C, int ldc, bool trans, T* Y, int r,
+                        Smem<T>& sm) {
+  tile_gemm<T>(N, r, r, sm.stage, LoadPanel<T>{X, N}, LoadSmall<T>{C, ldc, trans},
+               [&](int i, int cc, T v) { Y[i + (int64_t)cc * N] = v; });
+}
+
+template <typename T>
+__device__ void check_finite(const StepArgs<T>& g, const T* S, int r, int ld) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int o = threadIdx.x; o < r * r; o += NT)
+    if (!is_finite_val(S[(o % r) + (int64_t)(o / r) * ld])) bad = 1;
+  __syncthreads();
+  if (threadIdx.x == 0 && bad) atomicOr(g.status, ST_NONFINITE);
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// BUG (unconventional integrator) step
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, Smem<T>& sm) {
+  const int n = I.n, m = I.m, W = I.W;
+  T* GU = I.blk(B_GU);
+  T* GV = I.blk(B_GV);
+  T* Mm = I.blk(B_M);
+  T* Nm = I.blk(B_N);
+  T* St = I.blk(B_ST);
+  T* T1 = I.blk(B_T1);
+  const bool sylv = (g.op == OP_SYLVESTER);
+  if (sylv && g.proj_valid[I.inst] == 0) {
+    projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+  }
+  // K step (unconventional.jl:136-142)
+  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
+  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
+  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
+  tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
+  // L step (unconventional.jl:144-150), still with the old U
+  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
+  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
+  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
+  tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
+  // basis swap (unconventional.jl:151-152)
+  copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
+  copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
+  if (sylv) {
+    projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+    if (threadIdx.x == 0) g.proj_valid[I.inst] = 1;
+  }
+  // S step on the new bases (unconventional.jl:154-156): S0 = M S N^T
+  small_gemm<T>(r, r, r, T(1), I.S, I.rcap, false, Nm, W, true, T(0), T1, W);
+  small_gemm<T>(r, r, r, T(1), Mm, W, false, T1, W, false, T(0), St, W);
+  substep_core<T>(g, I, St, r, r, T(1), GU, GV, I.U, I.V, g.sS, g.dt, sm);
+  copy_mat<T>(r, r, St, W, I.S, I.rcap);
+  check_finite<T>(g, I.S, r, I.rcap);
+}
+
+// ---------------------------------------------------------------------------
+// Rank-adaptive BUG step
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ void ra_bug_step(const StepArgs<T>& g, Inst<T>& I, int r, Smem<T>& sm) {
+  const int n = I.n, m = I.m, W = I.W;
+  const int w2 = 2 * r;
+  T* GU = I.blk(B_GU);
+  T* GV = I.blk(B_GV);
+  T* Mm = I.blk(B_M);
+  T* Nm = I.blk(B_N);
+  T* St = I.blk(B_ST);
+  T* T1 = I.blk(B_T1);
+  T* T2 = I.blk(B_T2);
+  const bool sylv = (g.op == OP_SYLVESTER);
+  if (sylv) {
+    projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+  }
+  // K step: Uhat = orth([K1 | U0]) (rank_adaptive_unconventional.jl:197-206)
+  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
+  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
+  copy_mat<T>(n, r, I.U, n, I.k.PY + (int64_t)r * n, n);
+  householder_qr<T>(I.k.PY, n, n, w2, I.k.PQ, n, sm);
+  tile_gram<T>(n, w2, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, w2}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
+  // L step (:208-217)
+  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
+  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
+  copy_mat<T>(m, r, I.V, m, I.l.PY + (int64_t)r * m, m);
+  householder_qr<T>(I.l.PY, m, m, w2, I.l.PQ, m, sm);
+  tile_gram<T>(m, w2, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, w2}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
+  // S step on the augmented bases (:219-220)
+  if (sylv) {
+    projections<T>(I, I.k.PQ, n, w2, I.k.tri, GU, sm);
+    projections<T>(I, I.l.PQ, m, w2, I.l.tri, GV, sm);
+  }
+  small_gemm<T>(r, r, w2, T(1), I.S, I.rcap, false, Nm, W, true, T(0), T1, W);   // S N^T  (r x 2r)
+  small_gemm<T>(w2, r, w2, T(1), Mm, W, false, T1, W, false, T(0), St, W);       // M S N^T (2r x 2r)
+  substep_core<T>(g, I, St, w2, w2, T(1), GU, GV, I.k.PQ, I.l.PQ, g.sS, g.dt, sm);
+  // SVD of the core and truncation (:222-231)
+  T* a = sm.stage;
+  T* v = sm.stage + w2 * w2;
+  int* perm = reinterpret_cast<int*>(sm.stage + 2 * w2 * w2);
+  int* flag = perm + w2 + 1;
+  T* sigma = sm.vec;
+  for (int o = threadIdx.x; o < w2 * w2; o += NT) a[o] = St[(o % w2) + (int64_t)(o / w2) * W];
+  __syncthreads();
+  const bool ok = jacobi_svd<T>(w2, a, v, sigma, perm, flag);
+  __shared__ int r_new_s;
+  if (threadIdx.x == 0) {
+    if (!ok) atomicOr(g.status, ST_SVD_NOCONV);
+    // truncate_to_tolerance: smallest r1 with sum_{j>r1} s_j^2 < tol^2 (at least 1)
+    const double tol2 = g.tol * g.tol;
+    double acc = 0.0;
+    int rr = w2;
+    while (acc < tol2 && rr > 0) {
+      const double s = (double)sigma[perm[rr - 1]];
+      acc += s * s;
+      --rr;
+    }
+    int r1 = rr + 1;
+    if (r1 > I.rcap) r1 = I.rcap;   // min(r_max, .)
+    if (r1 < g.r_min) r1 = g.r_min;
+    if (r1 > w2) r1 = w2;
+    r_new_s = r1;
+  }
+  __syncthreads();
+  const int r1 = r_new_s;
+  // P1 = left vectors (2r x r1) into T1, Q1 = right vectors into T2; sorted
+  // singular values into sm.vec[WMAX..] (the staging area is reused below)
+  T* sig_sorted = sm.vec + WMAX;
+  for (int o = threadIdx.x; o < w2 * r1; o += NT) {
+    const int i = o % w2, j = o / w2;
+    const int pj = perm[j];
+    const T sg = sigma[pj];
+    T1[i + (int64_t)j * W] = (sg > T(0)) ? a[i + pj * w2] / sg : T(0);
+    T2[i + (int64_t)j * W] = v[i + pj * w2];
+  }
+  for (int j = threadIdx.x; j < r1; j += NT) sig_sorted[j] = sigma[perm[j]];
+  __syncthreads();
+  // new factors: U = Uhat P1, V = Vhat Q1, S = diag(sigma) (:224-231)
+  tile_gemm<T>(n, w2, r1, sm.stage, LoadPanel<T>{I.k.PQ, n}, LoadSmall<T>{T1, W, false},
+               [&](int i, int cc, T val) { I.U[i + (int64_t)cc * n] = val; });
+  tile_gemm<T>(m, w2, r1, sm.stage, LoadPanel<T>{I.l.PQ, m}, LoadSmall<T>{T2, W, false},
+               [&](int i, int cc, T val) { I.V[i + (int64_t)cc * m] = val; });
+  // sig_sorted lives in sm.vec, which the products above do not touch
+  for (int o = threadIdx.x; o < I.rcap * I.rcap; o += NT) {
+    const int i = o % I.rcap, j = o / I.rcap;
+    I.S[o] = (i == j && i < r1) ? sig_sorted[i] : T(0);
+  }
+  if (threadIdx.x == 0) g.rank[I.inst] = r1;
+  __syncthreads();
+  check_finite<T>(g, I.S, r1, I.rcap);
+}
+
+// ---------------------------------------------------------------------------
+// Projector-splitting (KSL) half steps
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r, double dt, Smem<T>& sm) {
+  const int n = I.n, m = I.m, W = I.W;
+  T* GU = I.blk(B_GU);
+  T* GV = I.blk(B_GV);
+  T* St = I.blk(B_ST);
+  T* RK = I.blk(B_RK);
+  T* RL = I.blk(B_RL);
+  const bool sylv = (g.op == OP_SYLVESTER);
+  if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+  // K step (projector_splitting.jl:133-138)
+  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
+  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
+  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
+  extract_r<T>(I.k.PY, n, r, RK, W);
+  copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
+  if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+  // S step, backward in time (:141-142; rhs negated at :64)
+  copy_mat<T>(r, r, RK, W, St, W);
+  substep_core<T>(g, I, St, r, r, T(-1), GU, GV, I.U, I.V, g.sS, dt, sm);
+  // L step (:145-151)
+  form_k0<T>(I, I.V, m, St, W, true, I.l.PY, r, sm);
+  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
+  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
+  extract_r<T>(I.l.PY, m, r, RL, W);
+  copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
+  // S = R^T
+  for (int o = threadIdx.x; o < r * r; o += NT) {
+    const int i = o % r, j = o / r;
+    I.S[i + (int64_t)j * I.rcap] = RL[j + (int64_t)i * W];
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, double dt, Smem<T>& sm) {
+  const int n = I.n, m = I.m, W = I.W;
+  T* GU = I.blk(B_GU);
+  T* GV = I.blk(B_GV);
+  T* St = I.blk(B_ST);
+  T* RK = I.blk(B_RK);
+  T* RL = I.blk(B_RL);
+  const bool sylv = (g.op == OP_SYLVESTER);
+  if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+  // L step (projector_splitting.jl:170-175)
+  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
+  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
+  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
+  extract_r<T>(I.l.PY, m, r, RL, W);
+  copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
+  if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+  // S step backward from R^T (:178-179)
+  for (int o = threadIdx.x; o < r * r; o += NT) {
+    const int i = o % r, j = o / r;
+    St[i + (int64_t)j * W] = RL[j + (int64_t)i * W];
+  }
+  __syncthreads();
+  substep_core<T>(g, I, St, r, r, T(-1), GU, GV, I.U, I.V, g.sS, dt, sm);
+  // K step (:182-188)
+  form_k0<T>(I, I.U, n, St, W, false, I.k.PY, r, sm);
+  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
+  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
+  extract_r<T>(I.k.PY, n, r, RK, W);
+  copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
+  copy_mat<T>(r, r, RK, W, I.S, I.rcap);
+}
+
+// ---------------------------------------------------------------------------
+// The step kernel
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(NT, 2) step_kernel(StepArgs<T> g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem<T>& sm = *reinterpret_cast<Smem<T>*>(smem_raw);
+  const int inst = g.order[blockIdx.x];
+  const InstDesc d = g.inst[inst];
+  Inst<T> I;
+  I.n = d.n; I.m = d.m; I.rcap = d.rcap; I.W = d.wcap; I.inst = inst;
+  I.U = g.U + d.offU;
+  I.S = g.S + d.offS;
+  I.V = g.V + d.offV;
+  T* wk = g.work + d.offWK;
+  T* wl = g.work + d.offWL;
+  const int W = d.wcap, rc = d.rcap;
+  I.k = Side<T>{d.n, I.U, g.opA ? g.opA + d.offA : nullptr, wk, wk + (int64_t)d.n * W,
+                wk + (int64_t)d.n * 2 * W, wk + (int64_t)d.n * (2 * W + rc), wk + (int64_t)d.n * (2 * W + 2 * rc)};
+  I.l = Side<T>{d.m, I.V, g.opB ? g.opB + d.offB : nullptr, wl, wl + (int64_t)d.m * W,
+                wl + (int64_t)d.m * 2 * W, wl + (int64_t)d.m * (2 * W + rc), wl + (int64_t)d.m * (2 * W + 2 * rc)};
+  I.small = g.small + d.offSmall;
+  I.Yp = (g.op == OP_DATA) ? g.Yprev + d.offY : nullptr;
+  I.Ypw = (g.op == OP_DATA) ? g.Yprev + d.offY : nullptr;
+  I.Yn = (g.op == OP_DATA) ? g.Ynext + d.offY : nullptr;
+  const int r = g.rank[inst];
+  if (r < 1 || r > d.rcap || (g.alg == ALG_RA_BUG && (2 * r > d.wcap || 2 * r > d.n || 2 * r > d.m))) {
+    if (threadIdx.x == 0) atomicOr(g.status, ST_BAD_SHAPE);
+    return;
+  }
+  if (g.alg == ALG_BUG) {
+    bug_step<T>(g, I, r, sm);
+  } else if (g.alg == ALG_RA_BUG) {
+    ra_bug_step<T>(g, I, r, sm);
+  } else {
+    if (g.ksl_order == KSL_PRIMAL) {
+      ksl_primal<T>(g, I, r, g.dt, sm);
+    } else if (g.ksl_order == KSL_DUAL) {
+      ksl_dual<T>(g, I, r, g.dt, sm);
+    } else {
+      ksl_primal<T>(g, I, r, 0.5 * g.dt, sm);
+      ksl_dual<T>(g, I, r, 0.5 * g.dt, sm);
+    }
+    check_finite<T>(g, I.S, r, I.rcap);
+  }
+  // data problems: yprev <- ycurr (unconventional.jl:125)
+  if (g.op == OP_DATA) {
+    const int64_t nm = (int64_t)d.n * d.m;
+    for (int64_t o = threadIdx.x; o < nm; o += NT) I.Ypw[o] = I.Yn[o];
+  }
+}
+
+template <typename T>
+size_t step_smem_bytes() {
+  return sizeof(Smem<T>);
+}
+
+template <typename T>
+cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream) {
+  const size_t smem = sizeof(Smem<T>);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(step_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  step_kernel<T><<<count, NT, smem, stream>>>(g);
+  return cudaGetLastError();
+}
+
+
+}  // namespace lri

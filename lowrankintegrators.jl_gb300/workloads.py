@@ -1,0 +1,105 @@
+"""Seeded synthetic inputs of the benchmark workloads (host NumPy).
+
+sylvester_256      plain BUG on F(X) = A X + X A^T, A = Laplacian/h^2 - 0.1 I,
+                   n = m = 256, h = 1/257, Dirichlet; X0 = sum_{k<=20} 2^-k u_k v_k^T
+                   (seed 1); Y0 = rank-8 truncated SVD; dt = 1e-4 on [0, 0.1];
+                   RK4 substeps with nsub = 20 (|dt*lambda| ~ 53 needs ~19).
+lyapunov_ensemble  4096 independent F_i(X) = A_i X + X B_i^T; n_i, m_i ~ U{64..1024},
+                   r_i ~ U{4..32}; A_i, B_i tridiagonal, diagonal -2-U[0,1],
+                   off-diagonals U[0.5,1]; X0_i = sum_{k<=r_i} 2^-k u_k v_k^T with
+                   seeded orthonormal u, v (seed 4); dt = 1e-2, 200 steps, RK4 nsub = 1.
+data_rotation      the reference test's stream Y(t) = exp(t W1) e^t D exp(t W2),
+                   N = 100, W skew, D = diag(2^-j) (seeded; the reference's is not).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List, Tuple
+
+import numpy as np
+
+
+def laplacian_tridiag(n: int, h: float, shift: float = 0.0):
+    sub = np.full(n, 1.0 / (h * h))
+    dia = np.full(n, -2.0 / (h * h) - shift)
+    sup = np.full(n, 1.0 / (h * h))
+    return sub, dia, sup
+
+
+def random_orthonormal(rng, n: int, k: int) -> np.ndarray:
+    Q, R = np.linalg.qr(rng.standard_normal((n, k)))
+    return Q * np.sign(np.diag(R))[None, :]
+
+
+@dataclass
+class SylvesterInstance:
+    A: Tuple[np.ndarray, np.ndarray, np.ndarray]
+    B: Tuple[np.ndarray, np.ndarray, np.ndarray]
+    U: np.ndarray
+    S: np.ndarray
+    V: np.ndarray
+
+
+def sylvester_256(seed: int = 1, n: int = 256, r: int = 8, nterms: int = 20):
+    """Returns (instance, dt, tspan, nsub)."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (n + 1)
+    A = laplacian_tridiag(n, h, 0.1)
+    u = random_orthonormal(rng, n, nterms)
+    v = random_orthonormal(rng, n, nterms)
+    s = 2.0 ** -np.arange(1, nterms + 1)
+    X0 = (u * s[None, :]) @ v.T
+    Uf, sf, Vtf = np.linalg.svd(X0)
+    inst = SylvesterInstance(A, A, Uf[:, :r].copy(), np.diag(sf[:r]), Vtf[:r].T.copy())
+    return inst, 1e-4, (0.0, 0.1), 20
+
+
+def lyapunov_ensemble(count: int = 4096, seed: int = 4, nmin: int = 64, nmax: int = 1024, rmin: int = 4,
+                      rmax: int = 32, first: int = 0, limit: int = None) -> List[SylvesterInstance]:
+    """Instances [first, first+limit) of the seeded ensemble (sizes and data
+    of instance i do not depend on which slice is requested)."""
+    rng = np.random.default_rng(seed)
+    n = rng.integers(nmin, nmax + 1, count)
+    m = rng.integers(nmin, nmax + 1, count)
+    r = rng.integers(rmin, rmax + 1, count)
+    seeds = rng.integers(0, 2 ** 63 - 1, count)
+    last = count if limit is None else min(count, first + limit)
+    out = []
+    for i in range(first, last):
+        g = np.random.default_rng(int(seeds[i]))
+        ni, mi, ri = int(n[i]), int(m[i]), int(r[i])
+        A = (g.uniform(0.5, 1.0, ni), -2.0 - g.uniform(0.0, 1.0, ni), g.uniform(0.5, 1.0, ni))
+        B = (g.uniform(0.5, 1.0, mi), -2.0 - g.uniform(0.0, 1.0, mi), g.uniform(0.5, 1.0, mi))
+        U = random_orthonormal(g, ni, ri)
+        V = random_orthonormal(g, mi, ri)
+        S = np.diag(2.0 ** -np.arange(1, ri + 1))
+        out.append(SylvesterInstance(A, B, U, S, V))
+    return out
+
+
+def lyapunov_ensemble_shapes(count: int = 4096, seed: int = 4, nmin: int = 64, nmax: int = 1024, rmin: int = 4,
+                             rmax: int = 32):
+    rng = np.random.default_rng(seed)
+    n = rng.integers(nmin, nmax + 1, count)
+    m = rng.integers(nmin, nmax + 1, count)
+    r = rng.integers(rmin, rmax + 1, count)
+    return n, m, r
+
+
+def skew(rng, N: int) -> np.ndarray:
+    W = rng.standard_normal((N, N))
+    return np.triu(W, 1) - np.triu(W, 1).T
+
+
+def data_rotation(seed: int = 0, N: int = 100):
+    """Returns the stream t -> Y(t) of the reference data test."""
+    from scipy.linalg import expm
+
+    rng = np.random.default_rng(seed)
+    W1, W2 = skew(rng, N), skew(rng, N)
+    D = np.diag(2.0 ** -np.arange(1, N + 1))
+
+    def Y(t):
+        return expm(t * W1) @ (np.exp(t) * D) @ expm(t * W2)
+
+    return Y
