@@ -1,0 +1,442 @@
+"""Benchmark: batched BUG steps/sec on the 4096-instance Lyapunov ensemble.
+
+Workload (one "step" = one BUG step of every instance, one kernel launch):
+  4096 independent F_i(X) = A_i X + X B_i^T, n_i, m_i ~ U{64..1024},
+  r_i ~ U{4..32}, tridiagonal A_i, B_i, X0_i with spectrum 2^-k (seed 4),
+  dt = 1e-2, RK4 substeps (nsub = 1), fast (FP32) form; the plain FP64 form
+  runs the same steps for the speed ratio and the accuracy check.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the reference integrator on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "lowrankintegrators.jl_gb300"))
+
+METRIC = "BUG steps/sec @ <=1e-5 rel. Frobenius err vs FP64 (batched Lyapunov ensemble, 4096 instances)"
+UNIT = "batched steps/s"
+DT = 1e-2
+NSUB = 1
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def algorithmic(shapes, nsub=NSUB, esize=4):
+    """Per batched step: compulsory DRAM bytes (factors and operators read,
+    factors written) and algorithmic flops of the implemented BUG step."""
+    n, m, r = (np.asarray(x, np.float64) for x in shapes)
+    nm = n + m
+    bytes_ = np.sum((2 * nm * r + 2 * r * r + 3 * nm) * esize)
+    flops = np.sum((12 + 16 * nsub) * nm * r * r + (36 * nsub + 5) * nm * r + (4 + 32 * nsub) * r ** 3)
+    return float(bytes_), float(flops)
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (FP64 restatement of the reference integrator),
+# one process per host core over a bounded sample of instances.
+# ---------------------------------------------------------------------------
+
+def _pool_init():
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+
+
+def _cpu_worker(args):
+    idx, steps = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    import workloads
+    from oracle import lri_oracle as O
+    out = 0.0
+    for i in idx:
+        e = workloads.lyapunov_ensemble(first=i, limit=1)[0]
+        p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
+                              (0.0, DT * steps))
+        integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            O.step(integ, integ.alg, DT)
+        out += time.perf_counter() - t0
+    return out
+
+
+def cpu_baseline(count, sample_every, steps, cores=None):
+    """Returns (batched steps/s extrapolated to `count` instances, cores, sample)."""
+    cores = cores or os.cpu_count() or 1
+    sample = list(range(0, count, sample_every))
+    chunks = [sample[k::cores] for k in range(cores)]
+    chunks = [c for c in chunks if c]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(len(chunks), initializer=_pool_init) as pool:
+        busy = pool.map(_cpu_worker, [(c, steps) for c in chunks])
+    wall = time.perf_counter() - t0
+    # instance-steps per second of the whole pool, scaled to the full ensemble
+    inst_steps = len(sample) * steps
+    per_inst_step = sum(busy) / inst_steps            # core-seconds per instance-step
+    batched_per_s = len(chunks) / (per_inst_step * count)
+    desc = (f"{len(sample)} of {count} instances (every {sample_every}th) x {steps} steps, "
+            f"{len(chunks)} processes, {wall:.1f} s wall")
+    return batched_per_s, len(chunks), desc
+
+
+# ---------------------------------------------------------------------------
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    val, cores, desc = cpu_baseline(args.count, args.cpu_sample_every, max(1, min(args.steps, 3)))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / val, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "lyapunov_ensemble_4096", "instances": args.count, "dt": DT,
+                       "scheme": f"RK4(nsub={NSUB})", "algorithm": "BUG"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--fp64-steps", type=int, default=None, help="plain FP64 steps timed (default: all)")
+    ap.add_argument("--cpu-sample-every", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    # CPU baseline first: its spawn pool starts before any GPU work
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args.count, args.cpu_sample_every, 2)
+
+    import torch
+    import __graft_entry__ as ge
+    import workloads
+    lri = ge.load_package()
+    torch.cuda.set_device(local)
+    dev_index = torch.cuda.current_device()
+
+    seed = 4 + rank  # weak scaling: every rank advances its own ensemble
+    insts = workloads.lyapunov_ensemble(count=args.count, seed=seed)
+    shapes = ([e.U.shape[0] for e in insts], [e.V.shape[0] for e in insts], [e.S.shape[0] for e in insts])
+    factors = [lri.SVDLikeRepresentation(e.U, e.S, e.V) for e in insts]
+    ops = [lri.SylvesterTridiagOperator(e.A, e.B) for e in insts]
+    alg = lri.UnconventionalAlgorithm(lri.RK4(NSUB))
+    K, W = args.steps, args.warmup
+    OPK = lri._native.LRI_OP_SYLVESTER_TRIDIAG
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    stream = torch.cuda.current_stream()
+
+    def timed_run(make, k_timed, k_total, sample_clocks=False):
+        """W warm-up steps, k_timed timed steps (CUDA events on the current
+        stream, barrier + synchronize on both sides), then the rest untimed so
+        every form ends at step W + k_total.  Returns (ms, factors, launches,
+        clocks)."""
+        obj = make()
+        t = 0.0
+        for _ in range(W):
+            obj.step(t, DT, 1)
+            t += DT
+        obj.check_status()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sampler = ClockSampler(dev_index) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
+        e0.record(stream)
+        for _ in range(k_timed):
+            obj.step(t, DT, 1)
+            t += DT
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+        barrier()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        for _ in range(k_total - k_timed):
+            obj.step(t, DT, 1)
+            t += DT
+        obj.check_status()
+        launches = k_timed * obj.launches_per_step()
+        ys = obj.download()
+        obj.close()
+        return ms, ys, launches, (sampler.summary() if sampler else None)
+
+    class Single:
+        """one homogeneous batch behind the same interface as MixedEnsemble"""
+
+        def __init__(self, prec):
+            self.b = lri.Batch(*shapes, alg, OPK, prec)
+            self.b.upload(factors, ops)
+
+        def step(self, t, dt, k):
+            self.b.step(t, dt, k)
+
+        def check_status(self):
+            self.b.check_status()
+
+        def launches_per_step(self):
+            return int(self.b.lib.lri_batch_launches_per_step(self.b.handle))
+
+        def download(self):
+            return self.b.download()
+
+        def close(self):
+            self.b.close()
+
+    # headline: the mixed form (FP32 batch for well-conditioned cores,
+    # double-float batch for the rest, two streams)
+    ms, ymix, launches, clocks = timed_run(lambda: lri.MixedEnsemble(factors, ops, alg, OPK), K, K, True)
+    ms_max = max_over_ranks(ms)
+    value = ws * K / (ms_max * 1e-3)
+    kap = np.array([lri.core_condition(Y.S) for Y in factors])
+    n_fp32 = int((kap <= lri.MIXED_KAPPA_MAX).sum())
+    # pure FP32 form and plain FP64 form, same steps
+    ms32, y32, _, _ = timed_run(lambda: Single("fp32"), K, K)
+    k64 = K if args.fp64_steps is None else min(K, args.fp64_steps)
+    ms64, y64, _, _ = timed_run(lambda: Single("fp64"), k64, K)
+    fp64_ms = ms64 / k64
+
+    def rel_errs(ys):
+        return np.array([np.linalg.norm(a.full() - c.full()) / np.linalg.norm(c.full()) for a, c in zip(ys, y64)])
+
+    err_mix = rel_errs(ymix)
+    err_32 = rel_errs(y32)
+    # aggregate over the ensemble: ||[Y_i] - [Y_i^64]||_F / ||[Y_i^64]||_F
+    num = sum(np.linalg.norm(a.full() - c.full()) ** 2 for a, c in zip(ymix, y64))
+    den = sum(np.linalg.norm(c.full()) ** 2 for c in y64)
+    err_mix_agg = float(math.sqrt(num / den))
+
+    # ---------------- accuracy vs the CPU oracle on a sample -----------------
+    oracle_err = None
+    if rank == 0:
+        from oracle import lri_oracle as O
+        sample = list(range(0, args.count, max(1, args.count // 8)))[:8]
+        em, e64 = [], []
+        for i in sample:
+            e = insts[i]
+            p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
+                                  (0.0, DT * (W + K)))
+            integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
+            for _ in range(W + K):
+                O.step(integ, integ.alg, DT)
+            em.append(O.rel_fro_err(ymix[i].full(), integ.u.full()))
+            e64.append(O.rel_fro_err(y64[i].full(), integ.u.full()))
+        oracle_err = {"instances": sample, "mixed_max": float(max(em)), "fp64_max": float(max(e64))}
+
+    # ---------------- e2e through the public API with host buffers -----------------
+    e2e = None
+    if not args.no_e2e:
+        ens = lri.MixedEnsemble(factors, ops, alg, OPK)
+        pinned = []
+        for prec, sel, b, st in ens.parts:
+            hU, hS, hV = b.pack_factors([factors[i] for i in sel])
+            hA = np.zeros(int(b.opA.numel()), b.np_dtype)
+            hB = np.zeros(int(b.opB.numel()), b.np_dtype)
+            for j, i in enumerate(sel):
+                a_, b_ = ops[i].packed()
+                hA[b.offA[j]:b.offA[j] + len(a_)] = a_
+                hB[b.offB[j]:b.offB[j] + len(b_)] = b_
+            src = [torch.from_numpy(x).pin_memory() for x in (hU, hS, hV, hA, hB)]
+            out = [[torch.empty_like(x).pin_memory() for x in src[:3]] for _ in range(2)]
+            pinned.append((b, st, src, out))
+        h2d = sum(int(x.numel()) * x.element_size() for _, _, src, _ in pinned for x in src)
+        d2h = sum(int(x.numel()) * x.element_size() for _, _, src, _ in pinned for x in src[:3])
+
+        def one_solve():
+            for b, st, src, _ in pinned:
+                st.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(st):
+                    for dst, x in zip((b.U, b.S, b.V, b.opA, b.opB), src):
+                        dst.copy_(x, non_blocking=True)
+                    st.synchronize()
+                    b.bind()
+            tt = 0.0
+            for k in range(K):
+                for b, st, src, out in pinned:
+                    with torch.cuda.stream(st):
+                        b.step(tt, DT, 1)
+                        for dst, x in zip(out[k & 1], (b.U, b.S, b.V)):
+                            dst.copy_(x, non_blocking=True)
+                tt += DT
+                for b, st, src, out in pinned:
+                    st.synchronize()  # this step's factors are on the host
+            return tt
+
+        one_solve()  # warm-up solve
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        one_solve()
+        torch.cuda.synchronize()
+        barrier()
+        el = max_over_ranks(time.perf_counter() - t0)
+        ens.check_status()
+        ens.close()
+        e2e = {"value": ws * K / el, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h,
+               "note": "one solve of K steps through the public API: H2D of Y0 and operators from pinned "
+                       "memory, every step's U, S, V read back to pinned host buffers"}
+
+    if rank != 0:
+        return
+    hbm, bf16, src = peaks()
+    alg_bytes, alg_flops = algorithmic(shapes)
+    t_launch = ms / K * 1e-3
+    achieved = alg_bytes / t_launch / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+df32", "data": "synthetic",
+        "config": {"workload": "lyapunov_ensemble_4096", "instances": args.count,
+                   "n_m_range": [64, 1024], "r_range": [4, 32], "dt": DT, "scheme": f"RK4(nsub={NSUB})",
+                   "algorithm": "BUG (UnconventionalAlgorithm)",
+                   "precision": "mixed: FP32 for kappa(S0) <= %.0e (%d instances), double-float for the other %d"
+                                % (lri.MIXED_KAPPA_MAX, n_fp32, args.count - n_fp32),
+                   "instance_steps_per_s": value * args.count,
+                   "l2": "inputs larger than L2: factors %.0f MB + operators + workspace > 129 MB"
+                         % (alg_bytes / 2e6)},
+        "accuracy": {"mixed_vs_fp64_gpu_rel_fro_max": float(err_mix.max()),
+                     "mixed_vs_fp64_gpu_rel_fro_median": float(np.median(err_mix)),
+                     "mixed_vs_fp64_gpu_rel_fro_aggregate": err_mix_agg,
+                     "fp32_only_vs_fp64_gpu_rel_fro_max": float(err_32.max()),
+                     "fp32_only_instances_above_1e-5": int((err_32 > 1e-5).sum()),
+                     "vs_oracle_sample": oracle_err, "steps_compared": W + K},
+        "fp32_only": {"ms_per_step": ms32 / K, "steps_per_s": 1e3 * K / ms32},
+        "plain_fp64": {"ms_per_step": fp64_ms, "steps_per_s": 1e3 / fp64_ms, "timed_steps": k64,
+                       "speedup_mixed_over_fp64": (value / ws) / (1e3 / fp64_ms)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_source": src,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "note": "compulsory bytes per batched step (factors and operators read, factors "
+                             "written) / mixed step time; the kernels are CUDA-core bound: %.3g algorithmic "
+                             "flops per step, %.2f TFLOP/s" % (alg_flops, alg_flops / t_launch / 1e12)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {"value": cpu[0], "unit": UNIT, "cores": cpu[1], "kind": "port", "sample": cpu[2]}
+    if e2e is not None:
+        line["e2e"] = e2e
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

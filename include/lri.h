@@ -63,7 +63,15 @@ typedef enum {
   LRI_ERR_STATE = 8          /* call out of order (e.g. step before bind) */
 } lri_status;
 
-typedef enum { LRI_F64 = 0, LRI_F32 = 1 } lri_dtype;
+/* Precision of a batch.
+ *   LRI_F64  plain FP64: buffers and arithmetic in double.
+ *   LRI_F32  fast form: buffers and arithmetic in float.
+ *   LRI_DF   double-float: buffers in double at the ABI, arithmetic on the
+ *            FP32 units with 48-bit (hi+lo float pair) significands.  The
+ *            engine keeps its own double-float copy of the factors: it is
+ *            loaded by lri_batch_bind and written back to the caller's
+ *            buffers at the end of every lri_batch_step call. */
+typedef enum { LRI_F64 = 0, LRI_F32 = 1, LRI_DF = 2 } lri_dtype;
 
 /* Algorithms: UnconventionalAlgorithm (unconventional.jl:13-21),
  * RankAdaptiveUnconventionalAlgorithm (rank_adaptive_unconventional.jl:15-23),
@@ -110,7 +118,7 @@ typedef struct {
 } lri_alg_desc;
 
 typedef struct {
-  int32_t dtype;       /* lri_dtype: F64 = plain FP64 form, F32 = fast form */
+  int32_t dtype;       /* lri_dtype */
   int32_t op;          /* lri_op_kind */
   int32_t count;       /* number of instances (>= 1) */
   int32_t reserved;
@@ -169,7 +177,7 @@ LRI_API lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream);
  * (synchronises `stream`, then clears the word). */
 LRI_API lri_status lri_batch_status(lri_batch* b, void* stream);
 
-/* Number of kernel launches one step makes (for launch accounting). */
+/* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
 
 #ifdef __cplusplus

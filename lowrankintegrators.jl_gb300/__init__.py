@@ -30,7 +30,8 @@ __all__ = [
     "SVDLikeRepresentation", "MatrixDEProblem", "MatrixDataProblem", "DLRSolution", "DLRIntegrator",
     "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm", "ProjectorSplitting",
     "PrimalLieTrotter", "DualLieTrotter", "Strang", "SubstepScheme", "Euler", "Heun", "Midpoint", "RK4",
-    "ZeroOperator", "SylvesterTridiagOperator", "Batch", "init", "step", "solve", "solve_ensemble",
+    "ZeroOperator", "SylvesterTridiagOperator", "Batch", "MixedEnsemble", "init", "step", "solve",
+    "solve_ensemble", "core_condition",
     "LriError", "n_steps",
 ]
 
@@ -266,11 +267,12 @@ class Batch:
         torch = _torch()
         self.torch = torch
         self.lib = _native.load()
-        if precision not in ("fp64", "fp32"):
-            raise ValueError("precision must be 'fp64' or 'fp32'")
+        if precision not in ("fp64", "fp32", "df"):
+            raise ValueError("precision must be 'fp64', 'fp32' or 'df'")
         self.precision = precision
-        self.dtype = torch.float64 if precision == "fp64" else torch.float32
-        self.np_dtype = np.float64 if precision == "fp64" else np.float32
+        # 'df' (double-float) batches exchange FP64 buffers at the ABI
+        self.dtype = torch.float32 if precision == "fp32" else torch.float64
+        self.np_dtype = np.float32 if precision == "fp32" else np.float64
         self.count = len(n)
         self.n = np.asarray(n, dtype=np.int64)
         self.m = np.asarray(m, dtype=np.int64)
@@ -281,7 +283,7 @@ class Batch:
         self.alg = alg
         self.op_kind = op_kind
         desc = _native.lri_batch_desc()
-        desc.dtype = _native.LRI_F64 if precision == "fp64" else _native.LRI_F32
+        desc.dtype = {"fp64": _native.LRI_F64, "fp32": _native.LRI_F32, "df": _native.LRI_DF}[precision]
         desc.op = op_kind
         desc.count = self.count
         I64P = C.POINTER(C.c_int64)
@@ -572,20 +574,97 @@ def solve(prob, alg, dt=None, precision: str = "fp64", save_everystep: bool = Tr
     return integ.sol
 
 
-def solve_ensemble(probs: Sequence[MatrixDEProblem], alg, dt, precision: str = "fp32"
+def core_condition(S: np.ndarray) -> float:
+    """sigma_max / sigma_min of a core matrix (inf when singular)."""
+    s = np.linalg.svd(np.asarray(S, dtype=np.float64), compute_uv=False)
+    return float(s[0] / s[-1]) if s[-1] > 0 else float("inf")
+
+
+# Fixed-rank BUG amplifies a relative perturbation of the factors by about
+# kappa(S) * dt per step: FP32 factors meet a 1e-5 relative error budget over
+# a few hundred steps only while kappa(S) stays below roughly 1e4.  Beyond
+# that the mixed form runs the instance in double-float.
+MIXED_KAPPA_MAX = 3.0e4
+
+
+class MixedEnsemble:
+    """An ensemble split by core conditioning into an FP32 batch and a
+    double-float batch, stepped concurrently on two CUDA streams."""
+
+    def __init__(self, factors: Sequence[SVDLikeRepresentation], operators, alg, op_kind: int,
+                 kappa_max: float = MIXED_KAPPA_MAX, r_cap=None):
+        torch = _torch()
+        self.torch = torch
+        self.count = len(factors)
+        kap = np.array([core_condition(Y.S) for Y in factors])
+        self.kappa = kap
+        self.parts = []
+        for prec, sel in (("fp32", np.flatnonzero(kap <= kappa_max)), ("df", np.flatnonzero(kap > kappa_max))):
+            if len(sel) == 0:
+                continue
+            fs = [factors[i] for i in sel]
+            ops = None if operators is None else [operators[i] for i in sel]
+            rc = None if r_cap is None else [r_cap[i] for i in sel]
+            b = Batch([Y.U.shape[0] for Y in fs], [Y.V.shape[0] for Y in fs], [Y.S.shape[0] for Y in fs], alg,
+                      op_kind, prec, r_cap=rc)
+            b.upload(fs, ops)
+            self.parts.append((prec, sel, b, torch.cuda.Stream()))
+
+    def step(self, t: float, dt: float, nsteps: int = 1):
+        torch = self.torch
+        cur = torch.cuda.current_stream()
+        for _, _, b, st in self.parts:
+            st.wait_stream(cur)
+            with torch.cuda.stream(st):
+                b.step(t, dt, nsteps)
+        for _, _, b, st in self.parts:
+            cur.wait_stream(st)
+
+    def launches_per_step(self) -> int:
+        return sum(int(b.lib.lri_batch_launches_per_step(b.handle)) for _, _, b, _ in self.parts)
+
+    def check_status(self):
+        for _, _, b, st in self.parts:
+            with self.torch.cuda.stream(st):
+                b.check_status()
+
+    def download(self) -> List[SVDLikeRepresentation]:
+        self.torch.cuda.synchronize()
+        out = [None] * self.count
+        for _, sel, b, _ in self.parts:
+            for i, Y in zip(sel, b.download()):
+                out[i] = Y
+        return out
+
+    def close(self):
+        for _, _, b, _ in self.parts:
+            b.close()
+
+
+def solve_ensemble(probs: Sequence[MatrixDEProblem], alg, dt, precision: str = "mixed"
                    ) -> List[SVDLikeRepresentation]:
     """Advances many independent MatrixDEProblems with the same tspan and
-    operator kind in one batch; returns the final factors of each."""
+    operator kind together; returns the final factors of each.  precision is
+    'fp64', 'fp32', 'df' or 'mixed' (FP32 for well-conditioned cores,
+    double-float for the others)."""
     tspan = probs[0].tspan
     kinds = {_op_kind(p) for p in probs}
     if len(kinds) != 1 or any(p.tspan != tspan for p in probs):
         raise ValueError("ensemble members must share tspan and operator kind")
+    kind = kinds.pop()
+    k = n_steps(tspan, dt)
+    if precision == "mixed":
+        ens = MixedEnsemble([p.u0 for p in probs], [p.f for p in probs], alg, kind)
+        ens.step(tspan[0], dt, k)
+        ens.check_status()
+        out = ens.download()
+        ens.close()
+        return out
     n = [p.u0.U.shape[0] for p in probs]
     m = [p.u0.V.shape[0] for p in probs]
     r = [p.u0.S.shape[0] for p in probs]
-    b = Batch(n, m, r, alg, kinds.pop(), precision)
+    b = Batch(n, m, r, alg, kind, precision)
     b.upload([p.u0 for p in probs], [p.f for p in probs])
-    k = n_steps(tspan, dt)
     b.step(tspan[0], dt, k)
     b.check_status()
     out = b.download()

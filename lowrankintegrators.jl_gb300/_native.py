@@ -19,7 +19,7 @@ STATUS_NAMES = {
     8: "LRI_ERR_STATE",
 }
 
-LRI_F64, LRI_F32 = 0, 1
+LRI_F64, LRI_F32, LRI_DF = 0, 1, 2
 LRI_ALG_BUG, LRI_ALG_RA_BUG, LRI_ALG_KSL = 0, 1, 2
 LRI_KSL_PRIMAL, LRI_KSL_DUAL, LRI_KSL_STRANG = 0, 1, 2
 LRI_OP_ZERO, LRI_OP_SYLVESTER_TRIDIAG, LRI_OP_BURGERS_PERIODIC, LRI_OP_DATA = 0, 1, 2, 3

@@ -38,6 +38,13 @@ struct lri_batch {
   void* d_work = nullptr;
   void* d_small = nullptr;
   void* d_Yprev = nullptr;
+  // double-float batches: the engine's own copies of the factors/operators
+  void* iU = nullptr;
+  void* iS = nullptr;
+  void* iV = nullptr;
+  void* iA = nullptr;
+  void* iB = nullptr;
+  void* iYn = nullptr;
   // bound caller buffers
   void* U = nullptr;
   void* S = nullptr;
@@ -84,21 +91,22 @@ Scheme to_scheme(const lri_scheme& s) {
 
 template <typename T>
 StepArgs<T> make_args(const lri_batch* b, double t, double dt, const void* Ynext) {
+  const bool df = b->desc.dtype == LRI_DF;
   StepArgs<T> g{};
   g.inst = b->d_inst;
   g.order = b->d_order;
   g.rank = b->d_rank;
   g.proj_valid = b->d_proj_valid;
   g.status = b->d_status;
-  g.U = static_cast<T*>(b->U);
-  g.S = static_cast<T*>(b->S);
-  g.V = static_cast<T*>(b->V);
-  g.opA = static_cast<const T*>(b->opA);
-  g.opB = static_cast<const T*>(b->opB);
+  g.U = static_cast<T*>(df ? b->iU : b->U);
+  g.S = static_cast<T*>(df ? b->iS : b->S);
+  g.V = static_cast<T*>(df ? b->iV : b->V);
+  g.opA = static_cast<const T*>(df ? b->iA : b->opA);
+  g.opB = static_cast<const T*>(df ? b->iB : b->opB);
   g.work = static_cast<T*>(b->d_work);
   g.small = static_cast<T*>(b->d_small);
   g.Yprev = static_cast<T*>(b->d_Yprev);
-  g.Ynext = static_cast<const T*>(Ynext);
+  g.Ynext = static_cast<const T*>(df && Ynext ? b->iYn : Ynext);
   g.t = t;
   g.dt = dt;
   g.alg = b->alg.kind;
@@ -118,7 +126,22 @@ StepArgs<T> make_args(const lri_batch* b, double t, double dt, const void* Ynext
 cudaError_t launch_one(const lri_batch* b, double t, double dt, const void* Ynext, cudaStream_t st) {
   const int count = b->desc.count;
   if (b->desc.dtype == LRI_F32) return lri::launch_step<float>(make_args<float>(b, t, dt, Ynext), count, st);
+  if (b->desc.dtype == LRI_DF) {
+    cudaError_t e = cudaSuccess;
+    if (Ynext) e = lri::convert_f64_to_df(static_cast<const double*>(Ynext), b->iYn, b->totY, st);
+    if (e != cudaSuccess) return e;
+    return lri::launch_step<lri::dfloat>(make_args<lri::dfloat>(b, t, dt, Ynext), count, st);
+  }
   return lri::launch_step<double>(make_args<double>(b, t, dt, Ynext), count, st);
+}
+
+// double-float batches: write the engine's factors back to the caller's buffers
+cudaError_t writeback(const lri_batch* b, cudaStream_t st) {
+  if (b->desc.dtype != LRI_DF) return cudaSuccess;
+  cudaError_t e = lri::convert_df_to_f64(b->iU, static_cast<double*>(b->U), b->totU, st);
+  if (e == cudaSuccess) e = lri::convert_df_to_f64(b->iS, static_cast<double*>(b->S), b->totS, st);
+  if (e == cudaSuccess) e = lri::convert_df_to_f64(b->iV, static_cast<double*>(b->V), b->totV, st);
+  return e;
 }
 
 void free_graph(lri_batch* b) {
@@ -164,7 +187,7 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   if (!out || !desc || !alg) return LRI_ERR_ARG;
   *out = nullptr;
   if (desc->count < 1 || !desc->n || !desc->m || !desc->r) return LRI_ERR_ARG;
-  if (desc->dtype != LRI_F32 && desc->dtype != LRI_F64) return LRI_ERR_ARG;
+  if (desc->dtype != LRI_F32 && desc->dtype != LRI_F64 && desc->dtype != LRI_DF) return LRI_ERR_ARG;
   if (desc->op < LRI_OP_ZERO || desc->op > LRI_OP_DATA) return LRI_ERR_ARG;
   if (alg->kind < LRI_ALG_BUG || alg->kind > LRI_ALG_KSL) return LRI_ERR_ARG;
   if (alg->kind == LRI_ALG_KSL && (alg->ksl_order < 0 || alg->ksl_order > 2)) return LRI_ERR_ARG;
@@ -259,6 +282,14 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   alloc(&b->d_work, b->esize * (size_t)b->totWork);
   alloc(&b->d_small, b->esize * (size_t)b->totSmall);
   if (desc->op == LRI_OP_DATA) alloc(&b->d_Yprev, b->esize * (size_t)b->totY);
+  if (desc->dtype == LRI_DF) {
+    alloc(&b->iU, 8 * (size_t)b->totU);
+    alloc(&b->iS, 8 * (size_t)b->totS);
+    alloc(&b->iV, 8 * (size_t)b->totV);
+    alloc(&b->iA, 8 * (size_t)b->totA);
+    alloc(&b->iB, 8 * (size_t)b->totB);
+    if (desc->op == LRI_OP_DATA) alloc(&b->iYn, 8 * (size_t)b->totY);
+  }
   if (e == cudaSuccess) e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_order, b->order.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(uint32_t));
@@ -289,6 +320,12 @@ lri_status lri_batch_destroy(lri_batch* b) {
   cudaFree(b->d_work);
   cudaFree(b->d_small);
   cudaFree(b->d_Yprev);
+  cudaFree(b->iU);
+  cudaFree(b->iS);
+  cudaFree(b->iV);
+  cudaFree(b->iA);
+  cudaFree(b->iB);
+  cudaFree(b->iYn);
   delete b;
   return LRI_OK;
 }
@@ -338,6 +375,15 @@ lri_status lri_batch_bind(lri_batch* b, void* U, void* S, void* V, const void* o
   std::vector<int32_t> r32(b->r.begin(), b->r.end());
   LRI_CUDA(cudaMemcpy(b->d_rank, r32.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice));
   LRI_CUDA(cudaMemset(b->d_proj_valid, 0, sizeof(int32_t) * count));
+  if (b->desc.dtype == LRI_DF) {
+    // load the engine's double-float copy (synchronous, like the rank upload above)
+    LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(U), b->iU, b->totU, 0));
+    LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(S), b->iS, b->totS, 0));
+    LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(V), b->iV, b->totV, 0));
+    if (opA) LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(opA), b->iA, b->totA, 0));
+    if (opB) LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(opB), b->iB, b->totB, 0));
+    LRI_CUDA(cudaDeviceSynchronize());
+  }
   b->bound = true;
   return LRI_OK;
 }
@@ -345,8 +391,12 @@ lri_status lri_batch_bind(lri_batch* b, void* U, void* S, void* V, const void* o
 lri_status lri_batch_data_init(lri_batch* b, const void* Y0, void* stream) {
   if (!b || !Y0) return LRI_ERR_ARG;
   if (b->desc.op != LRI_OP_DATA) return LRI_ERR_STATE;
-  LRI_CUDA(cudaMemcpyAsync(b->d_Yprev, Y0, b->esize * (size_t)b->totY, cudaMemcpyDeviceToDevice,
-                           (cudaStream_t)stream));
+  if (b->desc.dtype == LRI_DF) {
+    LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(Y0), b->d_Yprev, b->totY, (cudaStream_t)stream));
+  } else {
+    LRI_CUDA(cudaMemcpyAsync(b->d_Yprev, Y0, b->esize * (size_t)b->totY, cudaMemcpyDeviceToDevice,
+                             (cudaStream_t)stream));
+  }
   b->data_ready = true;
   return LRI_OK;
 }
@@ -359,10 +409,16 @@ lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, con
   if (b->desc.op == LRI_OP_DATA) {
     if (!b->data_ready) return LRI_ERR_STATE;
     if (!Ynext || nsteps != 1) return LRI_ERR_ARG;
-    return cuda_status(launch_one(b, t, dt, Ynext, st));
+    cudaError_t e = launch_one(b, t, dt, Ynext, st);
+    if (e == cudaSuccess) e = writeback(b, st);
+    return cuda_status(e);
   }
   if (Ynext) return LRI_ERR_ARG;
-  if (nsteps == 1) return cuda_status(launch_one(b, t, dt, nullptr, st));
+  if (nsteps == 1) {
+    cudaError_t e = launch_one(b, t, dt, nullptr, st);
+    if (e == cudaSuccess) e = writeback(b, st);
+    return cuda_status(e);
+  }
   // The engine's operators are autonomous, so a captured graph depends on
   // (nsteps, dt) only and is reused across calls.
   if (!(b->gexec && b->g_steps == nsteps && b->g_dt == dt)) {
@@ -372,6 +428,7 @@ lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, con
     LRI_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = launch_one(b, t + k * dt, dt, nullptr, b->cap_stream);
+    if (e == cudaSuccess) e = writeback(b, b->cap_stream);
     cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &graph);
     if (e != cudaSuccess || e2 != cudaSuccess) {
       if (graph) cudaGraphDestroy(graph);
@@ -414,6 +471,12 @@ lri_status lri_batch_status(lri_batch* b, void* stream) {
   return LRI_OK;
 }
 
-int32_t lri_batch_launches_per_step(const lri_batch* b) { return b ? 1 : 0; }
+int32_t lri_batch_launches_per_step(const lri_batch* b) {
+  if (!b) return 0;
+  // one engine launch; double-float batches add the three write-back
+  // conversions (and one snapshot conversion for data problems) per call
+  if (b->desc.dtype == LRI_DF) return 4 + (b->desc.op == LRI_OP_DATA ? 1 : 0);
+  return 1;
+}
 
 }  // extern "C"

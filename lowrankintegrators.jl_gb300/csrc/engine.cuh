@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.cuh"
 #include "engine_api.h"
 
 namespace lri {
@@ -28,10 +29,22 @@ constexpr int WMAX = 64;       // widest panel (columns) handled by the engine
 // small helpers
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ dfloat shfl_xor(dfloat v, int o) {
+  return dfloat(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+
+// Relative precision used by convergence tests.
+template <typename T> struct Prec;
+template <> struct Prec<float> { static constexpr double eps = 1.2e-7; };
+template <> struct Prec<double> { static constexpr double eps = 2.3e-16; };
+template <> struct Prec<dfloat> { static constexpr double eps = 1.5e-14; };
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) v += shfl_xor(v, o);
   return v;
 }
 
@@ -59,8 +72,15 @@ __device__ __forceinline__ void ld4(const double* p, double v[4]) {
   v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
+__device__ __forceinline__ void ld4(const dfloat* p, dfloat v[4]) {
+  float4 x = *reinterpret_cast<const float4*>(p);
+  float4 y = *reinterpret_cast<const float4*>(p + 2);
+  v[0] = dfloat(x.x, x.y); v[1] = dfloat(x.z, x.w); v[2] = dfloat(y.x, y.y); v[3] = dfloat(y.z, y.w);
+}
+
 __device__ __forceinline__ bool is_finite_val(float x) { return isfinite(x); }
 __device__ __forceinline__ bool is_finite_val(double x) { return isfinite(x); }
+__device__ __forceinline__ bool is_finite_val(dfloat x) { return lri_df::isfinite(x); }
 
 // Shared-memory workspace of one CTA.
 template <typename T>
@@ -529,7 +549,7 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 template <typename T>
 __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const T eps = (sizeof(T) == 4) ? T(1.2e-7) : T(2.3e-16);
+  const T eps = T(Prec<T>::eps);
   for (int o = tid; o < P * P; o += NT) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
   bool converged = false;

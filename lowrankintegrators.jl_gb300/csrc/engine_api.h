@@ -5,7 +5,13 @@
 #include <stddef.h>
 #include <stdint.h>
 
+namespace lri_df {
+struct dfloat;  // double-float value (dfloat.cuh); the host only passes pointers to it
+}  // namespace lri_df
+
 namespace lri {
+
+using lri_df::dfloat;
 
 enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2 };
 enum KslOrder : int32_t { KSL_PRIMAL = 0, KSL_DUAL = 1, KSL_STRANG = 2 };
@@ -59,6 +65,11 @@ struct StepArgs {
 
 template <typename T>
 cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream);
+
+// double <-> double-float conversions of n elements (dfloat storage is a
+// pair of floats, 8 bytes per element)
+cudaError_t convert_f64_to_df(const double* in, void* out, int64_t n, cudaStream_t stream);
+cudaError_t convert_df_to_f64(const void* in, double* out, int64_t n, cudaStream_t stream);
 template <typename T>
 size_t step_smem_bytes();
 

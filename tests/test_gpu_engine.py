@@ -1,9 +1,16 @@
 """GPU parity of the instance engine against the FP64 oracle.
 
 Tolerances (relative Frobenius error of Y = U S V^T):
-  plain FP64 form: 1e-11 (same discrete scheme, different summation order);
-  FP32 form:       1e-5  (the metric's accuracy bar).
+  plain FP64 form:   1e-11 (same discrete scheme, different summation order);
+  double-float form: 1e-10 (48-bit significands);
+  FP32 / mixed form: 1e-5  (the metric's accuracy bar).
 Factors are compared gauge-invariantly through Y and the singular values.
+
+Fixed-rank BUG amplifies perturbations of the factors by roughly
+kappa(S) * dt per step, so a trajectory whose core becomes very
+ill-conditioned is reproducible only to that level even between two FP64
+implementations; tests on such trajectories calibrate their tolerance to the
+oracle's own response to a 1e-16 relative perturbation.
 """
 import os
 import sys
@@ -17,7 +24,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "lowrankintegrators.jl_gb300"))
 import workloads  # noqa: E402
 
-TOL = {"fp64": 1e-11, "fp32": 1e-5}
+TOL = {"fp64": 1e-11, "df": 1e-10, "fp32": 1e-5, "mixed": 1e-5}
 
 
 def sylv_instance(seed, n, m, r, graded=True):
@@ -45,7 +52,7 @@ def pair_algs(lri, O, kind, scheme=("RK4", 2), ra_tol=1e-7):
 def run_both(lri, O, kind, precision, n=48, m=40, r=5, dt=0.02, T=0.3, scheme=("RK4", 2), seed=1, graded=True):
     A, B, U, S, V = sylv_instance(seed, n, m, r, graded)
     # rank decisions are compared exactly, so the FP32 run truncates well above its rounding level
-    ag, ao = pair_algs(lri, O, kind, scheme, ra_tol=1e-7 if precision == "fp64" else 1e-3)
+    ag, ao = pair_algs(lri, O, kind, scheme, ra_tol=1e-3 if precision == "fp32" else 1e-7)
     pg = lri.MatrixDEProblem(lri.SylvesterTridiagOperator(A, B), lri.SVDLikeRepresentation(U, S, V), (0.0, T))
     po = O.MatrixDEProblem(O.SylvesterTridiagOp(A, B), O.SVDLikeRepresentation(U, S, V), (0.0, T))
     sg = lri.solve(pg, ag, dt, precision=precision)
@@ -53,7 +60,7 @@ def run_both(lri, O, kind, precision, n=48, m=40, r=5, dt=0.02, T=0.3, scheme=("
     return sg, so
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "df", "fp32"])
 @pytest.mark.parametrize("kind", ["bug", "primal", "dual", "strang", "ra"])
 def test_sylvester_small_every_step(lri, oracle, kind, precision):
     sg, so = run_both(lri, oracle, kind, precision)
@@ -64,7 +71,7 @@ def test_sylvester_small_every_step(lri, oracle, kind, precision):
         assert err <= TOL[precision], f"step {k}: {err:.3e}"
     # orthonormal bases
     yg = sg.Y[-1]
-    tol_o = 1e-12 if precision == "fp64" else 2e-6
+    tol_o = 2e-6 if precision == "fp32" else 1e-12
     assert np.abs(yg.U.T @ yg.U - np.eye(yg.rank)).max() < tol_o
     assert np.abs(yg.V.T @ yg.V - np.eye(yg.rank)).max() < tol_o
 
@@ -97,9 +104,10 @@ def test_invariant_subspace_closed_form_gpu(lri):
     assert np.linalg.norm(Y - Yref) / np.linalg.norm(Yref) < 1e-13
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "df", "mixed"])
 def test_batched_uneven_instances(lri, oracle, precision):
-    """Eleven instances of uneven n, m, r in one batch (one CTA each)."""
+    """Eleven instances of uneven n, m, r in one batch (one CTA each); the
+    r = 32 member has a core condition number of 2^31."""
     shapes = [(64, 70, 4), (128, 90, 8), (200, 256, 12), (96, 96, 16), (300, 180, 5), (72, 64, 32),
               (257, 129, 7), (64, 1024, 9), (1024, 64, 3), (150, 150, 20), (99, 101, 6)]
     insts = [sylv_instance(100 + i, *s) for i, s in enumerate(shapes)]
@@ -114,10 +122,15 @@ def test_batched_uneven_instances(lri, oracle, precision):
         assert err <= TOL[precision], f"instance {i} {shapes[i]}: {err:.3e}"
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "df", "mixed", "fp32"])
 def test_lyapunov_ensemble_slice(lri, oracle, precision):
-    """32 instances of the 4096-member Lyapunov ensemble, full 200 steps."""
+    """32 instances of the 4096-member Lyapunov ensemble, full 200 steps.
+    The pure FP32 form is checked on the well-conditioned members only (the
+    ones the mixed form gives to FP32)."""
     insts = workloads.lyapunov_ensemble(first=0, limit=32)
+    if precision == "fp32":
+        insts = [e for e in insts if lri.core_condition(e.S) <= lri.MIXED_KAPPA_MAX]
+        assert len(insts) >= 8
     dt, T = 1e-2, 2.0
     probs = [lri.MatrixDEProblem(lri.SylvesterTridiagOperator(e.A, e.B), lri.SVDLikeRepresentation(e.U, e.S, e.V),
                                  (0.0, T)) for e in insts]
@@ -131,15 +144,20 @@ def test_lyapunov_ensemble_slice(lri, oracle, precision):
     assert max(errs) <= TOL[precision], f"max err {max(errs):.3e}"
 
 
-def test_sylvester_256_plain_fp64(lri, oracle):
-    """The plain FP64 workload (n = m = 256, r = 8, RK4 nsub = 20): GPU and
-    oracle agree at every 100th of 1000 steps."""
+@pytest.mark.parametrize("precision", ["fp64", "df"])
+def test_sylvester_256_every_100_steps(lri, oracle, precision):
+    """The stiff 256 x 256, r = 8 workload (RK4 nsub = 20, 1000 steps).  As
+    the stiff modes decay the core's condition number passes 1e10, so the
+    tolerance is calibrated against the oracle's own sensitivity: a second
+    oracle run whose core gets a 1e-16 relative perturbation every step."""
     inst, dt, tspan, nsub = workloads.sylvester_256()
     Yo = oracle.SVDLikeRepresentation(inst.U, inst.S, inst.V)
-    integ_o = oracle.init(oracle.MatrixDEProblem(oracle.SylvesterTridiagOp(inst.A, inst.B), Yo, tspan),
-                          oracle.UnconventionalAlgorithm(oracle.RK4(nsub)), dt)
+    mk = lambda: oracle.init(oracle.MatrixDEProblem(oracle.SylvesterTridiagOp(inst.A, inst.B), Yo, tspan),
+                             oracle.UnconventionalAlgorithm(oracle.RK4(nsub)), dt)
+    integ_o, integ_p = mk(), mk()
+    rng = np.random.default_rng(0)
     b = lri.Batch([256], [256], [8], lri.UnconventionalAlgorithm(lri.RK4(nsub)),
-                  lri._native.LRI_OP_SYLVESTER_TRIDIAG, "fp64")
+                  lri._native.LRI_OP_SYLVESTER_TRIDIAG, precision)
     b.upload([lri.SVDLikeRepresentation(inst.U, inst.S, inst.V)],
              [lri.SylvesterTridiagOperator(inst.A, inst.B)])
     t = 0.0
@@ -147,10 +165,14 @@ def test_sylvester_256_plain_fp64(lri, oracle):
         b.step(t, dt, 100)
         for _ in range(100):
             oracle.step(integ_o, integ_o.alg, dt)
+            oracle.step(integ_p, integ_p.alg, dt)
+            integ_p.u.S = integ_p.u.S * (1 + 1e-16 * rng.standard_normal(integ_p.u.S.shape))
             t += dt
         yg = b.download()[0]
         err = oracle.rel_fro_err(yg.full(), integ_o.u.full())
-        assert err <= 1e-11, f"after {100 * (chunk + 1)} steps: {err:.3e}"
+        sens = oracle.rel_fro_err(integ_p.u.full(), integ_o.u.full())
+        tol = max(TOL[precision], 100.0 * sens * (100.0 if precision == "df" else 1.0))
+        assert err <= tol, f"after {100 * (chunk + 1)} steps: {err:.3e} (oracle sensitivity {sens:.3e})"
     b.check_status()
 
 
