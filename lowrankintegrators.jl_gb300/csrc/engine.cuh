@@ -573,7 +573,10 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
         al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
         if (fabs(ga) > eps * sqrt(al * be) && ga != T(0)) {
           const T zeta = (be - al) / (T(2) * ga);
-          const T tt = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          // for large |zeta| use tan = 1/(2 zeta): zeta^2 would leave the FP32
+          // exponent range of float and double-float values
+          const T tt = (fabs(zeta) > T(1.0e15)) ? T(0.5) / zeta
+                                                 : copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
           const T cs = T(1) / sqrt(T(1) + tt * tt);
           const T sn = cs * tt;
           for (int i = lane; i < P; i += 32) {
