@@ -21,9 +21,15 @@ namespace lri {
 constexpr int NT = 256;        // threads per CTA
 constexpr int NW = NT / 32;    // warps per CTA
 constexpr int KC = 32;         // k-chunk of the tile products
-constexpr int TRMAX = 256;     // maximum rows per staged tile
-constexpr int STAGE_ELEMS = 12288;  // shared staging area (elements of T)
 constexpr int WMAX = 64;       // widest panel (columns) handled by the engine
+
+// Shared staging per CTA: 48 KB for 4-byte types, 66 KB for 8-byte types, so
+// three CTAs fit on an SM either way.  TRMAX (rows per staged tile) is sized
+// so TRMAX*KC + KC*WMAX fits; 8-byte types also hold the 64x64 Jacobi pair.
+template <typename T> struct Stage {
+  static constexpr int TRMAX = (sizeof(T) == 4) ? 256 : 192;
+  static constexpr int ELEMS = (sizeof(T) == 4) ? 12288 : 8448;
+};
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -87,7 +93,7 @@ template <typename T>
 struct Smem {
   T red[32];
   T vec[2 * WMAX + 8];
-  T stage[STAGE_ELEMS];
+  T stage[Stage<T>::ELEMS];
 };
 
 // ---------------------------------------------------------------------------
@@ -107,7 +113,7 @@ __device__ void tile_gemm(int N, int a, int c, T* stage, const LX& ldx, const LW
   const int ldws = c4 * 4;
   int ng = NT / c4;
   int TR = 4 * ng;
-  if (TR > TRMAX) TR = TRMAX;
+  if (TR > Stage<T>::TRMAX) TR = Stage<T>::TRMAX;
   ng = TR / 4;
   T* xs = stage;
   T* ws = stage + TR * KC;
@@ -155,15 +161,29 @@ __device__ void tile_gemm(int N, int a, int c, T* stage, const LX& ldx, const LW
   __syncthreads();
 }
 
-// Loader: plain column-major panel X (ld ldx), columns [col0, col0+a).
+// Loaders fill xs[kk*TR + ii] = X(i0+ii, k0+kk) for kk < kc, ii < TR (zero
+// beyond `rows`).  Each thread owns rows ii = tid, tid+NT, ... and walks the
+// columns in batches of 8 independent loads staged in registers, so a warp
+// keeps many L2 requests in flight (consecutive threads = consecutive rows,
+// coalesced).
+
+// Loader: plain column-major panel X (ld ldx).
 template <typename T>
 struct LoadPanel {
   const T* X;
   int ldx;
-  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
-    for (int e = threadIdx.x; e < kc * TR; e += NT) {
-      const int kk = e / TR, ii = e - kk * TR;
-      xs[e] = (ii < rows) ? X[(int64_t)(i0 + ii) + (int64_t)(k0 + kk) * ldx] : T(0);
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int k0, int kc, int TR) const {
+    for (int ii = threadIdx.x; ii < TR; ii += NT) {
+      const bool ok = ii < rows;
+      const T* src = X + (int64_t)(i0 + ii) + (int64_t)k0 * ldx;
+      for (int kb = 0; kb < kc; kb += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (ok && kb + u < kc) ? src[(int64_t)(kb + u) * ldx] : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kb + u < kc) xs[(kb + u) * TR + ii] = v[u];
+      }
     }
   }
 };
@@ -175,23 +195,40 @@ struct LoadStencilAug {
   const T* Z;
   int ldz, N, r;
   const T* tri;  // [sub | dia | sup]
-  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
-    for (int e = threadIdx.x; e < kc * TR; e += NT) {
-      const int kk = e / TR, ii = e - kk * TR;
-      const int k = k0 + kk;
-      T v = T(0);
-      if (ii < rows) {
-        const int i = i0 + ii;
-        if (k < r) {
-          const T* col = Z + (int64_t)k * ldz;
-          v = tri[N + i] * col[i];
-          if (i > 0) v = fma(tri[i], col[i - 1], v);
-          if (i + 1 < N) v = fma(tri[2 * N + i], col[i + 1], v);
-        } else {
-          v = Z[i + (int64_t)(k - r) * ldz];
-        }
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int k0, int kc, int TR) const {
+    for (int ii = threadIdx.x; ii < TR; ii += NT) {
+      const bool ok = ii < rows;
+      const int i = i0 + ii;
+      T cs = T(0), cd = T(0), cp = T(0);
+      if (ok) {
+        cd = tri[N + i];
+        if (i > 0) cs = tri[i];
+        if (i + 1 < N) cp = tri[2 * N + i];
       }
-      xs[e] = v;
+      const bool has_m = ok && i > 0, has_p = ok && i + 1 < N;
+      for (int kb = 0; kb < kc; kb += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + kb + u;
+          T x = T(0);
+          if (ok && kb + u < kc) {
+            if (k < r) {
+              const T* col = Z + (int64_t)k * ldz;
+              const T zm = has_m ? col[i - 1] : T(0);
+              const T zc = col[i];
+              const T zp = has_p ? col[i + 1] : T(0);
+              x = fma(cs, zm, fma(cp, zp, cd * zc));
+            } else {
+              x = Z[i + (int64_t)(k - r) * ldz];
+            }
+          }
+          v[u] = x;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kb + u < kc) xs[(kb + u) * TR + ii] = v[u];
+      }
     }
   }
 };
@@ -204,7 +241,7 @@ struct LoadDelta {
   const T* Yp;
   int n;      // rows of Y (leading dimension)
   bool trans;
-  __device__ void operator()(T* xs, int i0, int rows, int k0, int kc, int TR) const {
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int k0, int kc, int TR) const {
     for (int e = threadIdx.x; e < kc * TR; e += NT) {
       int kk, ii;
       if (!trans) { kk = e / TR; ii = e - kk * TR; }
@@ -268,14 +305,28 @@ struct LoadGP {
 // ---------------------------------------------------------------------------
 constexpr int TRG = 32;
 
+// Row-major staging loaders for tile_gram: lane = row (TRG = 32 rows, one
+// per lane), warp w takes columns w, w+NW, ... in batches of 4 loads.
 template <typename T>
 struct RowLoadPanel {  // row-major staging of a column-major panel
   const T* X;
   int ldx, w;
-  __device__ void operator()(T* xs, int i0, int rows, int lds) const {
-    for (int e = threadIdx.x; e < TRG * w; e += NT) {
-      const int k = e / TRG, ii = e - k * TRG;
-      xs[ii * lds + k] = (ii < rows) ? X[(int64_t)(i0 + ii) + (int64_t)k * ldx] : T(0);
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int lds) const {
+    const int ii = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const bool ok = ii < rows;
+    const T* src = X + (int64_t)(i0 + ii);
+    for (int kb = wp; kb < w; kb += 4 * NW) {
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        v[u] = (ok && k < w) ? src[(int64_t)k * ldx] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        if (k < w) xs[ii * lds + k] = v[u];
+      }
     }
   }
 };
@@ -285,22 +336,40 @@ struct RowLoadStencilAug {  // row-major staging of [Z | T Z] (note order), widt
   const T* Z;
   int ldz, N, r;
   const T* tri;
-  __device__ void operator()(T* xs, int i0, int rows, int lds) const {
-    for (int e = threadIdx.x; e < TRG * 2 * r; e += NT) {
-      const int k = e / TRG, ii = e - k * TRG;
-      T v = T(0);
-      if (ii < rows) {
-        const int i = i0 + ii;
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int lds) const {
+    const int ii = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const bool ok = ii < rows;
+    const int i = i0 + ii;
+    T cs = T(0), cd = T(0), cp = T(0);
+    if (ok) {
+      cd = tri[N + i];
+      if (i > 0) cs = tri[i];
+      if (i + 1 < N) cp = tri[2 * N + i];
+    }
+    const bool has_m = ok && i > 0, has_p = ok && i + 1 < N;
+    for (int kb = wp; kb < r; kb += 4 * NW) {
+      T v[4], s[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        T zc = T(0), zm = T(0), zp = T(0);
+        if (ok && k < r) {
+          const T* col = Z + (int64_t)k * ldz;
+          zc = col[i];
+          if (has_m) zm = col[i - 1];
+          if (has_p) zp = col[i + 1];
+        }
+        v[u] = zc;
+        s[u] = fma(cs, zm, fma(cp, zp, cd * zc));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
         if (k < r) {
-          v = Z[i + (int64_t)k * ldz];
-        } else {
-          const T* col = Z + (int64_t)(k - r) * ldz;
-          v = tri[N + i] * col[i];
-          if (i > 0) v = fma(tri[i], col[i - 1], v);
-          if (i + 1 < N) v = fma(tri[2 * N + i], col[i + 1], v);
+          xs[ii * lds + k] = v[u];
+          xs[ii * lds + r + k] = s[u];
         }
       }
-      xs[ii * lds + k] = v;
     }
   }
 };
@@ -402,12 +471,22 @@ __device__ __noinline__ void small_gemm(int p, int q, int s, T alpha, const T* A
                            bool tb, T beta, T* C, int ldc) {
   for (int o = threadIdx.x; o < p * s; o += NT) {
     const int i = o % p, j = o / p;
-    T acc = T(0);
-    for (int k = 0; k < q; ++k) {
+    T a4[4] = {T(0), T(0), T(0), T(0)};
+    int k = 0;
+    for (; k + 4 <= q; k += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const T av = ta ? A[(k + u) + (int64_t)i * lda] : A[i + (int64_t)(k + u) * lda];
+        const T bv = tb ? B[j + (int64_t)(k + u) * ldb] : B[(k + u) + (int64_t)j * ldb];
+        a4[u] = fma(av, bv, a4[u]);
+      }
+    }
+    for (; k < q; ++k) {
       const T av = ta ? A[k + (int64_t)i * lda] : A[i + (int64_t)k * lda];
       const T bv = tb ? B[j + (int64_t)k * ldb] : B[k + (int64_t)j * ldb];
-      acc = fma(av, bv, acc);
+      a4[0] = fma(av, bv, a4[0]);
     }
+    const T acc = (a4[0] + a4[1]) + (a4[2] + a4[3]);
     T* d = C + i + (int64_t)j * ldc;
     *d = (beta == T(0)) ? alpha * acc : fma(alpha, acc, beta * *d);
   }
@@ -443,7 +522,7 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* tau = sm.vec;            // [W]
   T* wv = sm.vec + WMAX;      // [W]
-  T* wred = sm.stage;         // [NW * W]
+  T* wred = sm.stage;         // [NW * WMAX]
   for (int k = 0; k < W; ++k) {
     T* colk = A + (int64_t)k * lda;
     T loc = T(0);
@@ -459,43 +538,68 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
       tk = (beta - alpha) / beta;
       scal = T(1) / (alpha - beta);
     }
-    if (tk != T(0))
-      for (int i = k + 1 + tid; i < N; i += NT) colk[i] *= scal;
     if (tid == 0) tau[k] = tk;
-    __syncthreads();
     const int nj = W - k - 1;
     if (nj > 0 && tk != T(0)) {
-      for (int j = 0; j < nj; ++j) {
-        const T* colj = A + (int64_t)(k + 1 + j) * lda;
-        T p = T(0);
-        for (int i = k + 1 + tid; i < N; i += NT) p = fma(colk[i], colj[i], p);
-        p = warp_sum(p);
-        if (lane == 0) wred[warp * WMAX + j] = p;
+      // w_j = A[k,j] + scal * sum_{i>k} x_i A[i,j] with the unscaled x (the
+      // reflector v = [1; scal*x] is written back in the update pass below);
+      // eight columns at a time so the shuffle reductions overlap
+      for (int j0 = 0; j0 < nj; j0 += 8) {
+        T p[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) p[u] = T(0);
+        for (int i = k + 1 + tid; i < N; i += NT) {
+          const T x = colk[i];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (j0 + u < nj) p[u] = fma(x, A[i + (int64_t)(k + 1 + j0 + u) * lda], p[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) p[u] = warp_sum(p[u]);
+        if (lane == 0) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (j0 + u < nj) wred[warp * WMAX + j0 + u] = p[u];
+        }
       }
       __syncthreads();
       if (tid < nj) {
-        T s = A[k + (int64_t)(k + 1 + tid) * lda];
+        T acc = T(0);
 #pragma unroll
-        for (int w = 0; w < NW; ++w) s += wred[w * WMAX + tid];
-        wv[tid] = tk * s;
+        for (int w = 0; w < NW; ++w) acc += wred[w * WMAX + tid];
+        wv[tid] = tk * fma(scal, acc, A[k + (int64_t)(k + 1 + tid) * lda]);
       }
       __syncthreads();
-      const int len = N - k;
-      for (int e = tid; e < len * nj; e += NT) {
-        const int j = e / len, ii = e - j * len;
-        const int i = k + ii;
-        const T vi = (ii == 0) ? T(1) : colk[i];
-        A[i + (int64_t)(k + 1 + j) * lda] -= vi * wv[j];
+      // A[i, k+1:] -= v_i * wv, one row per thread; store v below the diagonal
+      for (int i = k + tid; i < N; i += NT) {
+        T vi = T(1);
+        if (i > k) {
+          vi = colk[i] * scal;
+          colk[i] = vi;
+        }
+        T* row = A + i + (int64_t)(k + 1) * lda;
+        int j = 0;
+        for (; j + 4 <= nj; j += 4) {
+          const T a0 = row[(int64_t)j * lda], a1 = row[(int64_t)(j + 1) * lda];
+          const T a2 = row[(int64_t)(j + 2) * lda], a3 = row[(int64_t)(j + 3) * lda];
+          row[(int64_t)j * lda] = a0 - vi * wv[j];
+          row[(int64_t)(j + 1) * lda] = a1 - vi * wv[j + 1];
+          row[(int64_t)(j + 2) * lda] = a2 - vi * wv[j + 2];
+          row[(int64_t)(j + 3) * lda] = a3 - vi * wv[j + 3];
+        }
+        for (; j < nj; ++j) row[(int64_t)j * lda] -= vi * wv[j];
       }
-      __syncthreads();
+    } else if (tk != T(0)) {
+      for (int i = k + 1 + tid; i < N; i += NT) colk[i] *= scal;
     }
+    __syncthreads();
     if (tid == 0) colk[k] = beta;
     __syncthreads();
   }
   // explicit thin Q by backward accumulation: Q = H_0 ... H_{W-1} [I; 0]
-  for (int e = tid; e < N * W; e += NT) {
-    const int j = e / N, i = e - j * N;
-    Q[i + (int64_t)j * ldq] = (i == j) ? T(1) : T(0);
+  for (int j = 0; j < W; ++j) {
+    T* qj = Q + (int64_t)j * ldq;
+    for (int i = tid; i < N; i += NT) qj[i] = (i == j) ? T(1) : T(0);
   }
   __syncthreads();
   for (int k = W - 1; k >= 0; --k) {
@@ -503,27 +607,45 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
     if (tk == T(0)) continue;
     const T* colk = A + (int64_t)k * lda;
     const int nj = W - k;
-    for (int j = 0; j < nj; ++j) {
-      const T* qj = Q + (int64_t)(k + j) * ldq;
-      T p = (tid == 0) ? qj[k] : T(0);
-      for (int i = k + 1 + tid; i < N; i += NT) p = fma(colk[i], qj[i], p);
-      p = warp_sum(p);
-      if (lane == 0) wred[warp * WMAX + j] = p;
+    for (int j0 = 0; j0 < nj; j0 += 8) {
+      T p[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) p[u] = (tid == 0 && j0 + u < nj) ? Q[k + (int64_t)(k + j0 + u) * ldq] : T(0);
+      for (int i = k + 1 + tid; i < N; i += NT) {
+        const T vi = colk[i];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (j0 + u < nj) p[u] = fma(vi, Q[i + (int64_t)(k + j0 + u) * ldq], p[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) p[u] = warp_sum(p[u]);
+      if (lane == 0) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (j0 + u < nj) wred[warp * WMAX + j0 + u] = p[u];
+      }
     }
     __syncthreads();
     if (tid < nj) {
-      T s = T(0);
+      T acc = T(0);
 #pragma unroll
-      for (int w = 0; w < NW; ++w) s += wred[w * WMAX + tid];
-      wv[tid] = tk * s;
+      for (int w = 0; w < NW; ++w) acc += wred[w * WMAX + tid];
+      wv[tid] = tk * acc;
     }
     __syncthreads();
-    const int len = N - k;
-    for (int e = tid; e < len * nj; e += NT) {
-      const int j = e / len, ii = e - j * len;
-      const int i = k + ii;
-      const T vi = (ii == 0) ? T(1) : colk[i];
-      Q[i + (int64_t)(k + j) * ldq] -= vi * wv[j];
+    for (int i = k + tid; i < N; i += NT) {
+      const T vi = (i == k) ? T(1) : colk[i];
+      T* row = Q + i + (int64_t)k * ldq;
+      int j = 0;
+      for (; j + 4 <= nj; j += 4) {
+        const T q0 = row[(int64_t)j * ldq], q1 = row[(int64_t)(j + 1) * ldq];
+        const T q2 = row[(int64_t)(j + 2) * ldq], q3 = row[(int64_t)(j + 3) * ldq];
+        row[(int64_t)j * ldq] = q0 - vi * wv[j];
+        row[(int64_t)(j + 1) * ldq] = q1 - vi * wv[j + 1];
+        row[(int64_t)(j + 2) * ldq] = q2 - vi * wv[j + 2];
+        row[(int64_t)(j + 3) * ldq] = q3 - vi * wv[j + 3];
+      }
+      for (; j < nj; ++j) row[(int64_t)j * ldq] -= vi * wv[j];
     }
     __syncthreads();
   }

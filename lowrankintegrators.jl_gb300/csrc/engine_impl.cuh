@@ -397,7 +397,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
 // The step kernel
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(NT, 2) step_kernel(StepArgs<T> g) {
+__global__ void __launch_bounds__(NT, 3) step_kernel(StepArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem<T>& sm = *reinterpret_cast<Smem<T>*>(smem_raw);
   const int inst = g.order[blockIdx.x];
