@@ -103,7 +103,9 @@ struct Smem {
 //     (ii < TR; rows beyond `rows` must be zero)
 //   W by  ldw(ws, k0, kc, ldws, c)    fills ws[kk*ldws + cc] = W(k0+kk, cc)
 //     (cc < ldws; columns beyond c zero)
-//   The epilogue epi(i, cc, value) is called once per valid output element.
+//   The epilogue receives each thread's 4x4 block at once:
+//     epi(i, c, acc, nr, nc)  rows i..i+nr-1, columns c..c+nc-1 are valid,
+//   so it can issue all of its loads before any store.
 // Ends with __syncthreads().
 // ---------------------------------------------------------------------------
 template <typename T, class LX, class LW, class EPI>
@@ -144,22 +146,63 @@ __device__ void tile_gemm(int N, int a, int c, T* stage, const LX& ldx, const LW
       }
       __syncthreads();
     }
-    if (active) {
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        const int ii = 4 * rg + p;
-        if (ii < rows) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int cc = 4 * cg + q;
-            if (cc < c) epi(i0 + ii, cc, acc[p][q]);
-          }
-        }
-      }
-    }
+    if (active && 4 * rg < rows && 4 * cg < c) epi(i0 + 4 * rg, 4 * cg, acc, min(4, rows - 4 * rg), min(4, c - 4 * cg));
   }
   __syncthreads();
 }
+
+// Epilogues for tile_gemm.
+template <typename T>
+struct EpiStore {  // out(i, c) = acc
+  T* out;
+  int ld;
+  __device__ void operator()(int i, int c, const T (&acc)[4][4], int nr, int nc) const {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+        if (p < nr && q < nc) out[(int64_t)(i + p) + (int64_t)(c + q) * ld] = acc[p][q];
+  }
+};
+
+template <typename T>
+struct EpiAdd {  // out(i, c) += acc
+  T* out;
+  int ld;
+  __device__ void operator()(int i, int c, const T (&acc)[4][4], int nr, int nc) const {
+    T v[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) v[p][q] = (p < nr && q < nc) ? out[(int64_t)(i + p) + (int64_t)(c + q) * ld] : T(0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+        if (p < nr && q < nc) out[(int64_t)(i + p) + (int64_t)(c + q) * ld] = v[p][q] + acc[p][q];
+  }
+};
+
+// out(i, c) = g * y(i, c) + h * acc   (one Horner step of the substep flow)
+template <typename T>
+struct EpiAxpby {
+  T* out;
+  const T* y;
+  int ld;
+  T g, h;
+  __device__ void operator()(int i, int c, const T (&acc)[4][4], int nr, int nc) const {
+    T v[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) v[p][q] = (p < nr && q < nc) ? y[(int64_t)(i + p) + (int64_t)(c + q) * ld] : T(0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+        if (p < nr && q < nc) out[(int64_t)(i + p) + (int64_t)(c + q) * ld] = fma(h, acc[p][q], g * v[p][q]);
+  }
+};
 
 // Loaders fill xs[kk*TR + ii] = X(i0+ii, k0+kk) for kk < kc, ii < TR (zero
 // beyond `rows`).  Each thread owns rows ii = tid, tid+NT, ... and walks the
@@ -538,18 +581,26 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
       tk = (beta - alpha) / beta;
       scal = T(1) / (alpha - beta);
     }
-    if (tid == 0) tau[k] = tk;
     const int nj = W - k - 1;
-    if (nj > 0 && tk != T(0)) {
+    if (tk != T(0)) {
       // w_j = A[k,j] + scal * sum_{i>k} x_i A[i,j] with the unscaled x (the
       // reflector v = [1; scal*x] is written back in the update pass below);
-      // eight columns at a time so the shuffle reductions overlap
-      for (int j0 = 0; j0 < nj; j0 += 8) {
+      // eight columns at a time so the shuffle reductions overlap.  The same
+      // pass accumulates v^T v from the scaled entries, and tau = 2 / v^T v
+      // is recomputed from it: H = I - tau v v^T is then orthogonal to working
+      // precision even when the squares of a tiny column under- or overflow
+      // the exponent range (float and double-float values).
+      T pvv = T(0);
+      for (int j0 = 0; j0 < max(nj, 1); j0 += 8) {
         T p[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) p[u] = T(0);
         for (int i = k + 1 + tid; i < N; i += NT) {
           const T x = colk[i];
+          if (j0 == 0) {
+            const T vx = x * scal;
+            pvv = fma(vx, vx, pvv);
+          }
 #pragma unroll
           for (int u = 0; u < 8; ++u)
             if (j0 + u < nj) p[u] = fma(x, A[i + (int64_t)(k + 1 + j0 + u) * lda], p[u]);
@@ -562,7 +613,14 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
             if (j0 + u < nj) wred[warp * WMAX + j0 + u] = p[u];
         }
       }
+      pvv = warp_sum(pvv);
+      if (lane == 0) wred[warp * WMAX + WMAX - 1] = pvv;
       __syncthreads();
+      T vv = T(1);
+#pragma unroll
+      for (int w = 0; w < NW; ++w) vv += wred[w * WMAX + WMAX - 1];
+      tk = T(2) / vv;
+      if (tid == 0) tau[k] = tk;
       if (tid < nj) {
         T acc = T(0);
 #pragma unroll
@@ -589,8 +647,8 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
         }
         for (; j < nj; ++j) row[(int64_t)j * lda] -= vi * wv[j];
       }
-    } else if (tk != T(0)) {
-      for (int i = k + 1 + tid; i < N; i += NT) colk[i] *= scal;
+    } else if (tid == 0) {
+      tau[k] = T(0);
     }
     __syncthreads();
     if (tid == 0) colk[k] = beta;

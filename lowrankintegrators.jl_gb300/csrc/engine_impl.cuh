@@ -69,39 +69,45 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
     const int a = (side == 0) ? I.m : I.n;
     const int ldo = (side == 0) ? I.m : I.n;
     tile_gemm<T>(N, a, r, sm.stage, LoadDelta<T>{I.Yn, I.Yp, I.n, side == 1}, LoadSmall<T>{Xo, ldo, false},
-                 [&](int i, int cc, T v) { Y[i + (int64_t)cc * N] += v; });
+                 EpiAdd<T>{Y, N});
     return;
   }
-  // Sylvester tridiagonal
+  // Sylvester tridiagonal: the rhs L(Y) = T Y G + Y P^T is linear and
+  // autonomous, so any explicit RK scheme with a sub-diagonal tableau maps
+  // y -> R(hL) y with the stability polynomial R(z) = 1 + sum_j gamma_j z^j,
+  //   gamma_{j+1} = sum_{s>=j} b_s * a_s a_{s-1} ... a_{s-j+1}.
+  // Horner: w = gamma_ns y;  w = gamma_j y + h L(w) (j = ns-1..1);
+  // y1 = y + h L(w): ns applications of L, as many as the stages, without
+  // an accumulator panel.  (Equal to the stage-by-stage scheme up to
+  // rounding.)
   const T* G = Gp;
   const T* P = Gp + (int64_t)r * I.W;
   const int ns = sc.nstages;
+  double gam[5] = {1.0, 0.0, 0.0, 0.0, 0.0};
+  for (int j = 0; j < ns; ++j) {
+    double gsum = 0.0;
+    for (int st = j; st < ns; ++st) {
+      double prod = sc.b[st];
+      for (int t = st - j + 1; t <= st; ++t) prod *= sc.a[t];
+      gsum += prod;
+    }
+    gam[j + 1] = gsum;
+  }
   const T h = T(dt / sc.nsub);
   T* Zb[2] = {sd.PZ0, sd.PZ1};
-  T* PA = sd.PA;
   for (int sub = 0; sub < sc.nsub; ++sub) {
-    for (int s = 0; s < ns; ++s) {
-      const T* Zin = (s == 0) ? Y : Zb[(s - 1) & 1];
-      T* Zout = Zb[s & 1];
-      const T bs = T(sc.b[s]);
-      const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
-      tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{Zin, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
-                   [&](int i, int cc, T kv) {
-                     const int64_t idx = i + (int64_t)cc * N;
-                     if (ns == 1) {
-                       Zout[idx] = fma(h * bs, kv, Y[idx]);
-                     } else if (s == 0) {
-                       PA[idx] = bs * kv;
-                       Zout[idx] = fma(h * an, kv, Y[idx]);
-                     } else if (s + 1 < ns) {
-                       PA[idx] = fma(bs, kv, PA[idx]);
-                       Zout[idx] = fma(h * an, kv, Y[idx]);
-                     } else {
-                       Y[idx] = fma(h, fma(bs, kv, PA[idx]), Y[idx]);
-                     }
-                   });
-      if (ns == 1) copy_mat<T>(N, r, Zout, N, Y, N);
+    // the first application acts on gamma_ns * y: fold gamma_ns into h
+    const T* win = Y;
+    T hw = h * T(gam[ns]);
+    for (int j = ns - 1; j >= 0; --j) {
+      T* wout = (j == 0) ? ((ns == 1) ? Zb[0] : Y) : Zb[(ns - 1 - j) & 1];
+      const T gj = (j == 0) ? T(1) : T(gam[j]);
+      tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{win, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
+                   EpiAxpby<T>{wout, Y, N, gj, hw});
+      win = wout;
+      hw = h;
     }
+    if (ns == 1) copy_mat<T>(N, r, Zb[0], N, Y, N);
   }
 }
 
@@ -118,7 +124,7 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
     T* Z = I.k.PY;
     const int n = I.n;
     tile_gemm<T>(n, I.m, q, sm.stage, LoadDelta<T>{I.Yn, I.Yp, n, false}, LoadSmall<T>{Vb, I.m, false},
-                 [&](int i, int cc, T v) { Z[i + (int64_t)cc * n] = v; });
+                 EpiStore<T>{Z, n});
     tile_gram<T>(n, p, q, sm.stage, RowLoadPanel<T>{Ub, n, p}, RowLoadPanel<T>{Z, n, q}, St, W, sign, T(1));
     return;
   }
@@ -169,8 +175,7 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
 template <typename T>
 __device__ void form_k0(const Inst<T>& I, const T* X, int N, const T* C, int ldc, bool trans, T* Y, int r,
                         Smem<T>& sm) {
-  tile_gemm<T>(N, r, r, sm.stage, LoadPanel<T>{X, N}, LoadSmall<T>{C, ldc, trans},
-               [&](int i, int cc, T v) { Y[i + (int64_t)cc * N] = v; });
+  tile_gemm<T>(N, r, r, sm.stage, LoadPanel<T>{X, N}, LoadSmall<T>{C, ldc, trans}, EpiStore<T>{Y, N});
 }
 
 template <typename T>
@@ -309,10 +314,8 @@ __device__ __noinline__ void ra_bug_step(const StepArgs<T>& g, Inst<T>& I, int r
   for (int j = threadIdx.x; j < r1; j += NT) sig_sorted[j] = sigma[perm[j]];
   __syncthreads();
   // new factors: U = Uhat P1, V = Vhat Q1, S = diag(sigma) (:224-231)
-  tile_gemm<T>(n, w2, r1, sm.stage, LoadPanel<T>{I.k.PQ, n}, LoadSmall<T>{T1, W, false},
-               [&](int i, int cc, T val) { I.U[i + (int64_t)cc * n] = val; });
-  tile_gemm<T>(m, w2, r1, sm.stage, LoadPanel<T>{I.l.PQ, m}, LoadSmall<T>{T2, W, false},
-               [&](int i, int cc, T val) { I.V[i + (int64_t)cc * m] = val; });
+  tile_gemm<T>(n, w2, r1, sm.stage, LoadPanel<T>{I.k.PQ, n}, LoadSmall<T>{T1, W, false}, EpiStore<T>{I.U, n});
+  tile_gemm<T>(m, w2, r1, sm.stage, LoadPanel<T>{I.l.PQ, m}, LoadSmall<T>{T2, W, false}, EpiStore<T>{I.V, m});
   // sig_sorted lives in sm.vec, which the products above do not touch
   for (int o = threadIdx.x; o < I.rcap * I.rcap; o += NT) {
     const int i = o % I.rcap, j = o / I.rcap;
