@@ -584,7 +584,7 @@ def core_condition(S: np.ndarray) -> float:
 # kappa(S) * dt per step: FP32 factors meet a 1e-5 relative error budget over
 # a few hundred steps only while kappa(S) stays below roughly 1e4.  Beyond
 # that the mixed form runs the instance in double-float.
-MIXED_KAPPA_MAX = 3.0e4
+MIXED_KAPPA_MAX = 1.0e4
 
 
 class MixedEnsemble:

@@ -41,6 +41,12 @@ __device__ __forceinline__ dfloat shfl_xor(dfloat v, int o) {
   return dfloat(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
 }
 
+// The fast forms (FP32 and double-float) take the computed bases as exactly
+// orthonormal, so V^T V = I in the substep right-hand sides; the plain FP64
+// form keeps the Gram factors, as the reference's algebra does.
+template <typename T> struct AssumeOrthonormal { static constexpr bool value = true; };
+template <> struct AssumeOrthonormal<double> { static constexpr bool value = false; };
+
 // Relative precision used by convergence tests.
 template <typename T> struct Prec;
 template <> struct Prec<float> { static constexpr double eps = 1.2e-7; };
@@ -300,6 +306,91 @@ struct LoadDelta {
   }
 };
 
+// One application of the orthonormal-basis Sylvester substep operator:
+//   out = g * y + h * (T z + z P^T)       (N x r, all column-major, ld N)
+// T tridiagonal [sub | dia | sup], P (r x r, ld ldp).  Each row tile of z is
+// staged once with its two halo rows; the stencil and the z P^T product both
+// read shared memory.  out may alias y (never z).  Ends with __syncthreads().
+template <typename T>
+__device__ void tile_sylv(int N, int r, const T* z, const T* tri, const T* P, int ldp, T* out, const T* y, T g, T h,
+                          T* stage) {
+  const int tid = threadIdx.x;
+  const int c4 = (r + 3) >> 2;
+  const int ldw = c4 * 4;
+  int TR = 4 * (NT / c4);
+  if (TR > Stage<T>::TRMAX) TR = Stage<T>::TRMAX;
+  const int ng = TR / 4;
+  const int TH = TR + 4;           // staged rows: i0-1 .. i0+TR (padded to a multiple of 4)
+  T* zs = stage;                   // [r][TH] column-major, zs[k*TH + 1 + ii] = z(i0+ii, k)
+  T* ws = stage + r * TH;          // [r][ldw]  ws[k*ldw + c] = P(c, k) = P^T(k, c)
+  for (int e = tid; e < r * ldw; e += NT) {
+    const int k = e / ldw, c = e - k * ldw;
+    ws[e] = (c < r) ? P[c + (int64_t)k * ldp] : T(0);
+  }
+  const int cg = tid % c4, rg = tid / c4;
+  const bool active = rg < ng;
+  for (int i0 = 0; i0 < N; i0 += TR) {
+    const int rows = min(TR, N - i0);
+    // stage rows i0-1 .. i0+rows (zero outside [0, N))
+    for (int ii = tid; ii < rows + 2; ii += NT) {
+      const int i = i0 - 1 + ii;
+      const bool ok = (i >= 0) && (i < N);
+      for (int kb = 0; kb < r; kb += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (ok && kb + u < r) ? z[i + (int64_t)(kb + u) * N] : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kb + u < r) zs[(kb + u) * TH + ii] = v[u];
+      }
+    }
+    __syncthreads();
+    if (active && 4 * rg < rows && 4 * cg < r) {
+      T acc[4][4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+      for (int k = 0; k < r; ++k) {
+        T xv[4], wv[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) xv[p] = zs[k * TH + 1 + 4 * rg + p];
+        ld4(ws + k * ldw + 4 * cg, wv);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], wv[q], acc[p][q]);
+      }
+      const int nr = min(4, rows - 4 * rg), nc = min(4, r - 4 * cg);
+      T yv[4][4], cs[4], cd[4], cp[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int i = i0 + 4 * rg + p;
+        const bool okr = p < nr;
+        cd[p] = okr ? tri[N + i] : T(0);
+        cs[p] = (okr && i > 0) ? tri[i] : T(0);
+        cp[p] = (okr && i + 1 < N) ? tri[2 * N + i] : T(0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) yv[p][q] = (okr && q < nc) ? y[(int64_t)i + (int64_t)(4 * cg + q) * N] : T(0);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (q < nc) {
+          const T* zc = zs + (4 * cg + q) * TH + 4 * rg;  // zc[p] = z(i0+4rg+p-1)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            if (p < nr) {
+              const T tz = fma(cs[p], zc[p], fma(cp[p], zc[p + 2], cd[p] * zc[p + 1]));
+              out[(int64_t)(i0 + 4 * rg + p) + (int64_t)(4 * cg + q) * N] = fma(h, tz + acc[p][q], g * yv[p][q]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // W loader: column-major matrix W (ld ldw0) or its transpose.
 template <typename T>
 struct LoadSmall {
@@ -412,6 +503,45 @@ struct RowLoadStencilAug {  // row-major staging of [Z | T Z] (note order), widt
           xs[ii * lds + k] = v[u];
           xs[ii * lds + r + k] = s[u];
         }
+      }
+    }
+  }
+};
+
+template <typename T>
+struct RowLoadStencil {  // row-major staging of T Z, width r
+  const T* Z;
+  int ldz, N, r;
+  const T* tri;
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int lds) const {
+    const int ii = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const bool ok = ii < rows;
+    const int i = i0 + ii;
+    T cs = T(0), cd = T(0), cp = T(0);
+    if (ok) {
+      cd = tri[N + i];
+      if (i > 0) cs = tri[i];
+      if (i + 1 < N) cp = tri[2 * N + i];
+    }
+    const bool has_m = ok && i > 0, has_p = ok && i + 1 < N;
+    for (int kb = wp; kb < r; kb += 4 * NW) {
+      T s4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        T zc = T(0), zm = T(0), zp = T(0);
+        if (ok && k < r) {
+          const T* col = Z + (int64_t)k * ldz;
+          zc = col[i];
+          if (has_m) zm = col[i - 1];
+          if (has_p) zp = col[i + 1];
+        }
+        s4[u] = fma(cs, zm, fma(cp, zp, cd * zc));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        if (k < r) xs[ii * lds + k] = s4[u];
       }
     }
   }
@@ -556,12 +686,14 @@ __device__ void zero_mat(int p, int q, T* A, int lda) {
 
 // ---------------------------------------------------------------------------
 // Householder QR of the N x W panel A (column-major, ld lda), N >= W, in the
-// LAPACK convention (beta = -sign(alpha) * ||x||, v(k) = 1).  On exit the
-// upper triangle of A holds R and the explicit thin Q (N x W) is written to Q.
-// `sm` provides reduction space (vec needs >= W + 8 entries).
+// LAPACK convention (beta = -sign(alpha) * ||x||, v(k) = 1).  hh_factor
+// leaves R in the upper triangle, the reflectors below it and tau in
+// sm.vec[0..W); hh_form_q writes the explicit thin Q to a separate panel,
+// hh_form_q_inplace overwrites A with Q (LAPACK org2r order).  The
+// reductions use sm.stage[0 .. NW*WMAX).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, int ldq, Smem<T>& sm) {
+__device__ __noinline__ void hh_factor(T* A, int lda, int N, int W, Smem<T>& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* tau = sm.vec;            // [W]
   T* wv = sm.vec + WMAX;      // [W]
@@ -654,7 +786,16 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
     if (tid == 0) colk[k] = beta;
     __syncthreads();
   }
-  // explicit thin Q by backward accumulation: Q = H_0 ... H_{W-1} [I; 0]
+}
+
+// Explicit thin Q into a separate panel by backward accumulation:
+// Q = H_0 ... H_{W-1} [I; 0], reflectors and tau from hh_factor.
+template <typename T>
+__device__ __noinline__ void hh_form_q(const T* A, int lda, int N, int W, T* Q, int ldq, Smem<T>& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T* tau = sm.vec;
+  T* wv = sm.vec + WMAX;
+  T* wred = sm.stage;
   for (int j = 0; j < W; ++j) {
     T* qj = Q + (int64_t)j * ldq;
     for (int i = tid; i < N; i += NT) qj[i] = (i == j) ? T(1) : T(0);
@@ -704,6 +845,66 @@ __device__ __noinline__ void householder_qr(T* A, int lda, int N, int W, T* Q, i
         row[(int64_t)(j + 3) * ldq] = q3 - vi * wv[j + 3];
       }
       for (; j < nj; ++j) row[(int64_t)j * ldq] -= vi * wv[j];
+    }
+    __syncthreads();
+  }
+}
+
+// Q = H_0 ... H_{W-1} [I; 0] formed in place over the reflectors (org2r):
+// for k = W-1..0 apply H_k to A[k:, k+1:] (whose rows < k+1 are already
+// zero), then set column k to H_k e_k.
+template <typename T>
+__device__ __noinline__ void hh_form_q_inplace(T* A, int lda, int N, int W, Smem<T>& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T* tau = sm.vec;
+  T* wv = sm.vec + WMAX;
+  T* wred = sm.stage;
+  for (int k = W - 1; k >= 0; --k) {
+    const T tk = tau[k];
+    T* colk = A + (int64_t)k * lda;
+    const int nj = W - 1 - k;
+    if (nj > 0 && tk != T(0)) {
+      // w_j = A[k, j] + sum_{i>k} v_i A[i, j]   (A[k, j] is zero here)
+      for (int j0 = 0; j0 < nj; j0 += 8) {
+        T p[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) p[u] = T(0);
+        for (int i = k + 1 + tid; i < N; i += NT) {
+          const T vi = colk[i];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (j0 + u < nj) p[u] = fma(vi, A[i + (int64_t)(k + 1 + j0 + u) * lda], p[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) p[u] = warp_sum(p[u]);
+        if (lane == 0) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (j0 + u < nj) wred[warp * WMAX + j0 + u] = p[u];
+        }
+      }
+      __syncthreads();
+      if (tid < nj) {
+        T acc = T(0);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) acc += wred[w * WMAX + tid];
+        wv[tid] = tk * acc;
+      }
+      __syncthreads();
+      for (int i = k + tid; i < N; i += NT) {
+        const T vi = (i == k) ? T(1) : colk[i];
+        T* row = A + i + (int64_t)(k + 1) * lda;
+        for (int j = 0; j < nj; ++j) row[(int64_t)j * lda] -= vi * wv[j];
+      }
+      __syncthreads();
+    }
+    // column k = H_k e_k = e_k - tau v
+    for (int i = tid; i < N; i += NT) {
+      T x;
+      if (i < k) x = T(0);
+      else if (i == k) x = T(1) - tk;
+      else x = -(tk * colk[i]);
+      colk[i] = x;
     }
     __syncthreads();
   }

@@ -49,10 +49,41 @@ enum : int { B_GU = 0, B_GV = 2, B_M = 4, B_N = 5, B_ST = 6, B_SA = 7, B_SZ0 = 8
 
 // Projections of a basis X (N x w) needed by the Sylvester rhs:
 //   G = X^T X  (at dst, ld W),  P = X^T (T X)  (at dst + w*W, ld W).
+// (The fast forms take G = I and compute P only.)
 template <typename T>
 __device__ __noinline__ void projections(const Inst<T>& I, const T* X, int N, int w, const T* tri, T* dst, Smem<T>& sm) {
-  tile_gram<T>(N, w, 2 * w, sm.stage, RowLoadPanel<T>{X, N, w}, RowLoadStencilAug<T>{X, N, N, w, tri}, dst, I.W,
-               T(1), T(0));
+  if (AssumeOrthonormal<T>::value) {
+    tile_gram<T>(N, w, w, sm.stage, RowLoadPanel<T>{X, N, w}, RowLoadStencil<T>{X, N, N, w, tri},
+                 dst + (int64_t)w * I.W, I.W, T(1), T(0));
+  } else {
+    tile_gram<T>(N, w, 2 * w, sm.stage, RowLoadPanel<T>{X, N, w}, RowLoadStencilAug<T>{X, N, N, w, tri}, dst, I.W,
+                 T(1), T(0));
+  }
+}
+
+// Orthonormalises the N x W panel Kp (global): the explicit Q goes to Qdst
+// (ld N) and, when R is given, the triangular factor to R (ld ldr).  The
+// panel is factored in shared memory when it fits in the staging area
+// (which the QR does not otherwise use), else in place in global memory.
+template <typename T>
+__device__ __noinline__ void qr_panel(T* Kp, int N, int W, T* Qdst, T* R, int ldr, Smem<T>& sm) {
+  const int off = NW * WMAX;  // hh_* keep their reduction scratch below this offset
+  if ((int64_t)N * W <= (int64_t)(Stage<T>::ELEMS - off)) {
+    T* A = sm.stage + off;
+    for (int j = 0; j < W; ++j)
+      for (int i = threadIdx.x; i < N; i += NT) A[i + j * N] = Kp[i + (int64_t)j * N];
+    __syncthreads();
+    hh_factor<T>(A, N, N, W, sm);
+    if (R) extract_r<T>(A, N, W, R, ldr);
+    hh_form_q_inplace<T>(A, N, N, W, sm);
+    for (int j = 0; j < W; ++j)
+      for (int i = threadIdx.x; i < N; i += NT) Qdst[i + (int64_t)j * N] = A[i + j * N];
+    __syncthreads();
+  } else {
+    hh_factor<T>(Kp, N, N, W, sm);
+    if (R) extract_r<T>(Kp, N, W, R, ldr);
+    hh_form_q<T>(Kp, N, N, W, Qdst, N, sm);
+  }
 }
 
 // One substep of side `sd` on the panel Y (N x r, ld N), in place.
@@ -83,6 +114,7 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
   const T* G = Gp;
   const T* P = Gp + (int64_t)r * I.W;
   const int ns = sc.nstages;
+  constexpr bool ortho = AssumeOrthonormal<T>::value;
   double gam[5] = {1.0, 0.0, 0.0, 0.0, 0.0};
   for (int j = 0; j < ns; ++j) {
     double gsum = 0.0;
@@ -102,8 +134,12 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
     for (int j = ns - 1; j >= 0; --j) {
       T* wout = (j == 0) ? ((ns == 1) ? Zb[0] : Y) : Zb[(ns - 1 - j) & 1];
       const T gj = (j == 0) ? T(1) : T(gam[j]);
-      tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{win, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
-                   EpiAxpby<T>{wout, Y, N, gj, hw});
+      if (ortho) {
+        tile_sylv<T>(N, r, win, sd.tri, P, I.W, wout, Y, gj, hw, sm.stage);
+      } else {
+        tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{win, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
+                     EpiAxpby<T>{wout, Y, N, gj, hw});
+      }
       win = wout;
       hw = h;
     }
@@ -142,11 +178,17 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
   for (int sub = 0; sub < sc.nsub; ++sub) {
     for (int s = 0; s < ns; ++s) {
       const T* Z = (s == 0) ? St : SZ[(s - 1) & 1];
-      // SK = sign * (PU (Z GV) + GU (Z PV^T))
-      small_gemm<T>(p, q, q, T(1), Z, W, false, GV, W, false, T(0), T1, W);
-      small_gemm<T>(p, q, q, T(1), Z, W, false, PV, W, true, T(0), T2, W);
-      small_gemm<T>(p, p, q, sign, PU, W, false, T1, W, false, T(0), SK, W);
-      small_gemm<T>(p, p, q, sign, GU, W, false, T2, W, false, T(1), SK, W);
+      if (AssumeOrthonormal<T>::value) {
+        // SK = sign * (PU Z + Z PV^T)
+        small_gemm<T>(p, p, q, sign, PU, W, false, Z, W, false, T(0), SK, W);
+        small_gemm<T>(p, q, q, sign, Z, W, false, PV, W, true, T(1), SK, W);
+      } else {
+        // SK = sign * (PU (Z GV) + GU (Z PV^T))
+        small_gemm<T>(p, q, q, T(1), Z, W, false, GV, W, false, T(0), T1, W);
+        small_gemm<T>(p, q, q, T(1), Z, W, false, PV, W, true, T(0), T2, W);
+        small_gemm<T>(p, p, q, sign, PU, W, false, T1, W, false, T(0), SK, W);
+        small_gemm<T>(p, p, q, sign, GU, W, false, T2, W, false, T(1), SK, W);
+      }
       const T bs = T(sc.b[s]);
       const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
       T* Zout = SZ[s & 1];
@@ -210,12 +252,12 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   // K step (unconventional.jl:136-142)
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
-  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
+  qr_panel<T>(I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
   tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
   // L step (unconventional.jl:144-150), still with the old U
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
-  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
+  qr_panel<T>(I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
   tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
   // basis swap (unconventional.jl:151-152)
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
@@ -256,13 +298,13 @@ __device__ __noinline__ void ra_bug_step(const StepArgs<T>& g, Inst<T>& I, int r
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
   copy_mat<T>(n, r, I.U, n, I.k.PY + (int64_t)r * n, n);
-  householder_qr<T>(I.k.PY, n, n, w2, I.k.PQ, n, sm);
+  qr_panel<T>(I.k.PY, n, w2, I.k.PQ, nullptr, 0, sm);
   tile_gram<T>(n, w2, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, w2}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
   // L step (:208-217)
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
   copy_mat<T>(m, r, I.V, m, I.l.PY + (int64_t)r * m, m);
-  householder_qr<T>(I.l.PY, m, m, w2, I.l.PQ, m, sm);
+  qr_panel<T>(I.l.PY, m, w2, I.l.PQ, nullptr, 0, sm);
   tile_gram<T>(m, w2, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, w2}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
   // S step on the augmented bases (:219-220)
   if (sylv) {
@@ -342,8 +384,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   // K step (projector_splitting.jl:133-138)
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
-  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
-  extract_r<T>(I.k.PY, n, r, RK, W);
+  qr_panel<T>(I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
   // S step, backward in time (:141-142; rhs negated at :64)
@@ -352,8 +393,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   // L step (:145-151)
   form_k0<T>(I, I.V, m, St, W, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
-  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
-  extract_r<T>(I.l.PY, m, r, RL, W);
+  qr_panel<T>(I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   // S = R^T
   for (int o = threadIdx.x; o < r * r; o += NT) {
@@ -376,8 +416,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   // L step (projector_splitting.jl:170-175)
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
-  householder_qr<T>(I.l.PY, m, m, r, I.l.PQ, m, sm);
-  extract_r<T>(I.l.PY, m, r, RL, W);
+  qr_panel<T>(I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
   // S step backward from R^T (:178-179)
@@ -390,8 +429,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   // K step (:182-188)
   form_k0<T>(I, I.U, n, St, W, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
-  householder_qr<T>(I.k.PY, n, n, r, I.k.PQ, n, sm);
-  extract_r<T>(I.k.PY, n, r, RK, W);
+  qr_panel<T>(I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   copy_mat<T>(r, r, RK, W, I.S, I.rcap);
 }
