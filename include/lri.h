@@ -177,6 +177,31 @@ LRI_API lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream);
  * (synchronises `stream`, then clears the word). */
 LRI_API lri_status lri_batch_status(lri_batch* b, void* stream);
 
+/* Allocation-free BUG step (no counterpart in the reference).  For callers
+ * that cannot call cudaMalloc - their device memory is owned by another
+ * allocator, or their time loop must not trigger the device-wide
+ * synchronisation of cudaMalloc/cudaFree - this advances ONE instance of
+ * F(X) = A X + X B^T (tridiagonal A, B as in LRI_OP_SYLVESTER_TRIDIAG) by
+ * nsteps BUG steps with the step kernel of lri_batch_step, using a fixed
+ * 4 MiB scratch array compiled into the library (held by every GPU that loads
+ * it until the process exits) instead of allocated workspace.
+ *   dtype   LRI_F64 or LRI_F32 (LRI_DF: LRI_ERR_UNSUPPORTED)
+ *   U (n x r), S (r x r), V (m x r)  caller's device buffers, column-major,
+ *           updated in place; A (3n), B (3m) device coefficient vectors
+ *   Sizes whose workspace exceeds the scratch, elem_size * (5r(n+m) + 15r^2)
+ *   + 256 bytes > 4 MiB (for example n + m > 3200 at r = 32 in FP64), are
+ *   rejected with LRI_ERR_ARG.
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array and leave their
+ * contents in it (the call clears what must start at zero), so calls whose
+ * work overlaps on the GPU (other streams, other host threads) race.
+ * status_out (host pointer, optional): when given, the call waits for its
+ * steps and stores LRI_OK or LRI_ERR_NONFINITE there. */
+LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int64_t r, void* U, void* S, void* V,
+                                        const void* A, const void* B, double dt, int32_t nsteps,
+                                        const lri_scheme* scheme, void* stream, int32_t* status_out);
+
 /* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
 
