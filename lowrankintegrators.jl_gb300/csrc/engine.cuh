@@ -910,6 +910,179 @@ __device__ __noinline__ void hh_form_q_inplace(T* A, int lda, int N, int W, Smem
   }
 }
 
+// ---------------------------------------------------------------------------
+// Cholesky-based QR pieces for the fast forms (FP32 and double-float).
+// ---------------------------------------------------------------------------
+
+// acc + x*y accumulated in double-float: exact FP32 products (TwoProduct)
+// for float inputs, double-float FMA for double-float inputs.
+__device__ __forceinline__ dfloat acc_mul(dfloat acc, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);
+  const dfloat s = lri_df::two_sum(acc.hi, p);
+  return lri_df::fast_two_sum(s.hi, s.lo + (acc.lo + e));
+}
+__device__ __forceinline__ dfloat acc_mul(dfloat acc, dfloat x, dfloat y) { return fma(x, y, acc); }
+__device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.0f); }
+__device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
+__device__ __forceinline__ void from_df(dfloat x, float& y) { y = x.hi + x.lo; }
+__device__ __forceinline__ void from_df(dfloat x, dfloat& y) { y = x; }
+
+// G = X^T X (W x W, W <= 64) accumulated in double-float; X is N x W
+// (column-major, ld ldx, type T), G column-major with ld ldg.
+template <typename T>
+__device__ __noinline__ void gram_df(int N, int W, const T* X, int ldx, dfloat* G, int ldg, T* stage) {
+  const int tid = threadIdx.x;
+  const int w4 = (W + 3) >> 2;
+  const int MT = w4 * w4;                 // <= 256 = NT
+  const int splits = NT / MT;
+  const int lds = w4 * 4 + 4;
+  T* xs = stage;
+  const int mt = tid % MT, split = tid / MT;
+  const bool active = split < splits;
+  const int ma = mt / w4, mc = mt - ma * w4;
+  dfloat acc[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) acc[e] = dfloat(0.0f, 0.0f);
+  for (int i0 = 0; i0 < N; i0 += TRG) {
+    const int rows = min(TRG, N - i0);
+    RowLoadPanel<T>{X, ldx, W}(xs, i0, rows, lds);
+    __syncthreads();
+    if (active) {
+      for (int ii = split; ii < rows; ii += splits) {
+        T xa[4], xb[4];
+        ld4(xs + ii * lds + 4 * ma, xa);
+        ld4(xs + ii * lds + 4 * mc, xb);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p * 4 + q] = acc_mul(acc[p * 4 + q], xa[p], xb[q]);
+      }
+    }
+    __syncthreads();
+  }
+  dfloat* part = reinterpret_cast<dfloat*>(stage);  // splits * MT * 16 <= 4096 values
+  if (active) {
+#pragma unroll
+    for (int e = 0; e < 16; ++e) part[(split * MT + mt) * 16 + e] = acc[e];
+  }
+  __syncthreads();
+  for (int o = tid; o < MT * 16; o += NT) {
+    const int m2 = o >> 4, e = o & 15;
+    dfloat sum = part[m2 * 16 + e];
+    for (int sp = 1; sp < splits; ++sp) sum += part[(sp * MT + m2) * 16 + e];
+    const int a2 = m2 / w4, c2 = m2 - a2 * w4;
+    const int ia = 4 * a2 + (e >> 2), jc = 4 * c2 + (e & 3);
+    if (ia < W && jc < W) G[ia + (int64_t)jc * ldg] = sum;
+  }
+  __syncthreads();
+}
+
+// In-place upper Cholesky G = R^T R of a W x W double-float matrix (ld ldg),
+// optionally shifted first: G + shift * trace(G) * I.  Returns false on a
+// non-positive pivot (G is then unusable).
+static __device__ __noinline__ bool chol_df(int W, dfloat* G, int ldg, double shift_rel) {
+  const int tid = threadIdx.x;
+  __shared__ int bad;
+  if (tid == 0) {
+    bad = 0;
+    if (shift_rel > 0.0) {
+      dfloat tr(0.0f, 0.0f);
+      for (int j = 0; j < W; ++j) tr += G[j + (int64_t)j * ldg];
+      const dfloat sh = tr * dfloat(shift_rel);
+      for (int j = 0; j < W; ++j) G[j + (int64_t)j * ldg] += sh;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < W; ++k) {
+    if (tid == 0) {
+      dfloat d = G[k + (int64_t)k * ldg];
+      if (!(d.hi > 0.0f)) {
+        bad = 1;
+        d = dfloat(1.0f, 0.0f);
+      }
+      G[k + (int64_t)k * ldg] = sqrt(d);
+    }
+    __syncthreads();
+    const dfloat inv = dfloat(1.0f, 0.0f) / G[k + (int64_t)k * ldg];
+    for (int j = k + 1 + tid; j < W; j += NT) G[k + (int64_t)j * ldg] = G[k + (int64_t)j * ldg] * inv;
+    __syncthreads();
+    const int cnt = W - k - 1;
+    for (int e = tid; e < cnt * cnt; e += NT) {
+      const int i = k + 1 + e % cnt, j = k + 1 + e / cnt;
+      if (i <= j) G[i + (int64_t)j * ldg] = fma(-G[k + (int64_t)i * ldg], G[k + (int64_t)j * ldg], G[i + (int64_t)j * ldg]);
+    }
+    __syncthreads();
+  }
+  const bool ok = (bad == 0);
+  __syncthreads();
+  return ok;
+}
+
+// K <- K R^{-1} row by row (forward substitution, backward stable), R upper
+// triangular W x W double-float (ld ldr); K is N x W (T, ld N).  Row tiles are
+// staged in shared memory with one row per thread.
+template <typename T>
+__device__ __noinline__ void trsm_rows(int N, int W, T* K, const dfloat* R, int ldr, T* stage, T* invd) {
+  const int tid = threadIdx.x;
+  T* Rs = stage;  // W x W upper triangle
+  for (int e = tid; e < W * W; e += NT) {
+    const int i = e % W, j = e / W;
+    T v;
+    from_df((i <= j) ? R[i + (int64_t)j * ldr] : dfloat(0.0f, 0.0f), v);
+    Rs[e] = v;
+  }
+  for (int j = tid; j < W; j += NT) {
+    T v;
+    from_df(dfloat(1.0f, 0.0f) / R[j + (int64_t)j * ldr], v);
+    invd[j] = v;
+  }
+  int TR = (Stage<T>::ELEMS - W * W) / W;
+  if (TR > NT) TR = NT;
+  TR &= ~31;
+  T* ks = stage + W * W;  // [W][TR]
+  __syncthreads();
+  for (int i0 = 0; i0 < N; i0 += TR) {
+    const int rows = min(TR, N - i0);
+    for (int ii = tid; ii < rows; ii += NT) {
+      const T* src = K + i0 + ii;
+      for (int kb = 0; kb < W; kb += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (kb + u < W) ? src[(int64_t)(kb + u) * N] : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kb + u < W) ks[(kb + u) * TR + ii] = v[u];
+      }
+    }
+    __syncthreads();
+    if (tid < rows) {
+      for (int j = 0; j < W; ++j) {
+        T sacc = ks[j * TR + tid];
+        for (int i = 0; i < j; ++i) sacc = fma(-ks[i * TR + tid], Rs[i + j * W], sacc);
+        ks[j * TR + tid] = sacc * invd[j];
+      }
+    }
+    __syncthreads();
+    for (int ii = tid; ii < rows; ii += NT) {
+      T* dst = K + i0 + ii;
+      for (int j = 0; j < W; ++j) dst[(int64_t)j * N] = ks[j * TR + ii];
+    }
+    __syncthreads();
+  }
+}
+
+// C = A B for upper triangular W x W double-float matrices (ld W each).
+static __device__ __noinline__ void tri_mul_df(int W, const dfloat* A, const dfloat* B, dfloat* C) {
+  for (int e = threadIdx.x; e < W * W; e += NT) {
+    const int i = e % W, j = e / W;
+    dfloat acc(0.0f, 0.0f);
+    for (int k = i; k <= j; ++k) acc = fma(A[i + k * W], B[k + j * W], acc);
+    C[e] = (i <= j) ? acc : dfloat(0.0f, 0.0f);
+  }
+  __syncthreads();
+}
+
 // Copies the upper triangle of the factored panel (R, W x W) to R (ld ldr).
 template <typename T>
 __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {

@@ -86,6 +86,68 @@ __device__ __noinline__ void qr_panel(T* Kp, int N, int W, T* Qdst, T* R, int ld
   }
 }
 
+// CholeskyQR orthonormalisation of the fast forms: two passes for FP32 (the
+// Gram accumulated in double-float from exact products keeps
+// kappa^2 * u far below 1 for the FP32 class), three for double-float with
+// the first pass shifted (Fukaya, Kannan, Nakatsukasa, Zhang, Yamamoto,
+// SIAM J. Sci. Comput. 2020), stable up to kappa(K) ~ 1e11.  K <- K R^{-1} is
+// a row-wise triangular solve, so the residual stays O(u ||K||).  Returns
+// false (K unchanged, or restored) on a Cholesky breakdown; the caller then
+// falls back to Householder.
+template <typename T>
+__device__ __noinline__ bool cholqr_panel(const Inst<T>& I, T* K, int N, int W, T* Qdst, T* R, int ldr,
+                                          Smem<T>& sm) {
+  dfloat* G = reinterpret_cast<dfloat*>(I.blk(B_SA));
+  dfloat* Racc = reinterpret_cast<dfloat*>(I.blk(B_SZ1));
+  dfloat* Rtmp = reinterpret_cast<dfloat*>(I.blk(B_T1));
+  const bool shifted = sizeof(T) != sizeof(float);
+  const int npass = shifted ? 3 : 2;
+  // 11 (N W + W (W+1)) u with u = 2^-44 for the double-float arithmetic
+  const double shift = shifted ? 11.0 * ((double)N * W + (double)W * (W + 1)) * 5.7e-14 : 0.0;
+  if (R) copy_mat<T>(N, W, K, N, Qdst, N);  // backup of K for a late fallback
+  for (int pass = 0; pass < npass; ++pass) {
+    gram_df<T>(N, W, K, N, G, W, sm.stage);
+    if (!chol_df(W, G, W, pass == 0 ? shift : 0.0)) {
+      if (pass > 0 && R) copy_mat<T>(N, W, Qdst, N, K, N);
+      return false;
+    }
+    trsm_rows<T>(N, W, K, G, W, sm.stage, sm.vec);
+    if (R) {
+      if (pass == 0) {
+        for (int e = threadIdx.x; e < W * W; e += NT) Racc[e] = ((e % W) <= (e / W)) ? G[e] : dfloat(0.0f, 0.0f);
+        __syncthreads();
+      } else {
+        tri_mul_df(W, G, Racc, Rtmp);
+        for (int e = threadIdx.x; e < W * W; e += NT) Racc[e] = Rtmp[e];
+        __syncthreads();
+      }
+    }
+  }
+  copy_mat<T>(N, W, K, N, Qdst, N);
+  if (R) {
+    for (int e = threadIdx.x; e < W * W; e += NT) {
+      const int i = e % W, j = e / W;
+      T v;
+      from_df(Racc[e], v);
+      R[i + (int64_t)j * ldr] = v;
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// Orthonormal basis of an N x W panel for BUG and KSL: CholeskyQR in the fast
+// forms, Householder QR (the reference's LAPACK algorithm) in plain FP64 and
+// as the fallback.
+template <typename T>
+__device__ __noinline__ void orth_panel(const Inst<T>& I, T* Kp, int N, int W, T* Qdst, T* R, int ldr,
+                                        Smem<T>& sm) {
+  if constexpr (AssumeOrthonormal<T>::value) {
+    if (cholqr_panel<T>(I, Kp, N, W, Qdst, R, ldr, sm)) return;
+  }
+  qr_panel<T>(Kp, N, W, Qdst, R, ldr, sm);
+}
+
 // One substep of side `sd` on the panel Y (N x r, ld N), in place.
 //   Sylvester: Y' = T Y G + Y P^T  with (G, P) the projections of the other
 //              side's basis (K: V^T V, V^T B V; L: U^T U, U^T A U).
@@ -252,12 +314,12 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   // K step (unconventional.jl:136-142)
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
-  qr_panel<T>(I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
+  orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
   tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
   // L step (unconventional.jl:144-150), still with the old U
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
-  qr_panel<T>(I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
+  orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
   tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
   // basis swap (unconventional.jl:151-152)
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
@@ -384,7 +446,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   // K step (projector_splitting.jl:133-138)
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
-  qr_panel<T>(I.k.PY, n, r, I.k.PQ, RK, W, sm);
+  orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
   // S step, backward in time (:141-142; rhs negated at :64)
@@ -393,7 +455,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   // L step (:145-151)
   form_k0<T>(I, I.V, m, St, W, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
-  qr_panel<T>(I.l.PY, m, r, I.l.PQ, RL, W, sm);
+  orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   // S = R^T
   for (int o = threadIdx.x; o < r * r; o += NT) {
@@ -416,7 +478,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   // L step (projector_splitting.jl:170-175)
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
-  qr_panel<T>(I.l.PY, m, r, I.l.PQ, RL, W, sm);
+  orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
   // S step backward from R^T (:178-179)
@@ -429,7 +491,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   // K step (:182-188)
   form_k0<T>(I, I.U, n, St, W, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
-  qr_panel<T>(I.k.PY, n, r, I.k.PQ, RK, W, sm);
+  orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   copy_mat<T>(r, r, RK, W, I.S, I.rcap);
 }
