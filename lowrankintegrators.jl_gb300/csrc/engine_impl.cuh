@@ -36,11 +36,14 @@ struct Inst {
   T* S;
   T* V;
   Side<T> k, l;
-  T* small;   // 15 blocks of W*W
+  T* small;   // 15 blocks of W*W elements, each block 16-byte aligned
   const T* Yp;
   const T* Yn;
   T* Ypw;     // writable previous snapshot
-  __device__ T* blk(int i) const { return small + (int64_t)i * W * W; }
+  // block stride: W*W rounded up to 4 elements, so a block can also hold
+  // double-float values in a float batch (8-byte aligned)
+  __device__ int64_t bstride() const { return ((int64_t)W * W + 3) & ~int64_t(3); }
+  __device__ T* blk(int i) const { return small + (int64_t)i * bstride(); }
 };
 
 // small-scratch block indices
