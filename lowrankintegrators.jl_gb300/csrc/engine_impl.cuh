@@ -139,13 +139,15 @@ __device__ __noinline__ bool cholqr_panel(const Inst<T>& I, T* K, int N, int W, 
   return true;
 }
 
-// Orthonormal basis of an N x W panel for BUG and KSL: CholeskyQR in the fast
-// forms, Householder QR (the reference's LAPACK algorithm) in plain FP64 and
-// as the fallback.
+// Orthonormal basis of an N x W panel for BUG and KSL: shifted CholeskyQR3 in
+// double-float, Householder QR (the reference's LAPACK algorithm) in FP32,
+// plain FP64 and as the fallback.  (FP32 keeps Householder: the FP32 step's
+// error budget is set by its reductions, and Householder's orthogonality
+// error is the smaller of the two.)
 template <typename T>
 __device__ __noinline__ void orth_panel(const Inst<T>& I, T* Kp, int N, int W, T* Qdst, T* R, int ldr,
                                         Smem<T>& sm) {
-  if constexpr (AssumeOrthonormal<T>::value) {
+  if constexpr (AssumeOrthonormal<T>::value && sizeof(T) == 8) {
     if (cholqr_panel<T>(I, Kp, N, W, Qdst, R, ldr, sm)) return;
   }
   qr_panel<T>(Kp, N, W, Qdst, R, ldr, sm);
