@@ -53,6 +53,15 @@ template <> struct Prec<float> { static constexpr double eps = 1.2e-7; };
 template <> struct Prec<double> { static constexpr double eps = 2.3e-16; };
 template <> struct Prec<dfloat> { static constexpr double eps = 1.5e-14; };
 
+// Multiply-accumulate of the long inner loops (deferred renormalisation for
+// double-float, plain FMA otherwise) and the matching final renormalisation.
+__device__ __forceinline__ float fma_acc(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_acc(double a, double b, double c) { return ::fma(a, b, c); }
+__device__ __forceinline__ float renorm(float a) { return a; }
+__device__ __forceinline__ double renorm(double a) { return a; }
+using lri_df::fma_acc;
+using lri_df::renorm;
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -147,11 +156,15 @@ __device__ void tile_gemm(int N, int a, int c, T* stage, const LX& ldx, const LW
 #pragma unroll
           for (int p = 0; p < 4; ++p)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], wv[q], acc[p][q]);
+            for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
         }
       }
       __syncthreads();
     }
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = renorm(acc[p][q]);
     if (active && 4 * rg < rows && 4 * cg < c) epi(i0 + 4 * rg, 4 * cg, acc, min(4, rows - 4 * rg), min(4, c - 4 * cg));
   }
   __syncthreads();
@@ -359,8 +372,12 @@ __device__ void tile_sylv(int N, int r, const T* z, const T* tri, const T* P, in
 #pragma unroll
         for (int p = 0; p < 4; ++p)
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], wv[q], acc[p][q]);
+          for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
       }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = renorm(acc[p][q]);
       const int nr = min(4, rows - 4 * rg), nc = min(4, r - 4 * cg);
       T yv[4][4], cs[4], cd[4], cp[4];
 #pragma unroll
@@ -585,7 +602,7 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
 #pragma unroll
               for (int p = 0; p < 4; ++p)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[u][p * 4 + q] = fma(xv[p], yv[q], acc[u][p * 4 + q]);
+                for (int q = 0; q < 4; ++q) acc[u][p * 4 + q] = fma_acc(xv[p], yv[q], acc[u][p * 4 + q]);
             }
           }
         }
@@ -593,6 +610,10 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
     }
     __syncthreads();
   }
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[u][e] = renorm(acc[u][e]);
   // combine splits through shared memory (deterministic order)
   T* part = stage;  // splits * MT * 16 <= NT*16 elements
   if (splits > 1) {
@@ -1058,9 +1079,16 @@ __device__ __noinline__ void trsm_rows(int N, int W, T* K, const dfloat* R, int 
     __syncthreads();
     if (tid < rows) {
       for (int j = 0; j < W; ++j) {
-        T sacc = ks[j * TR + tid];
-        for (int i = 0; i < j; ++i) sacc = fma(-ks[i * TR + tid], Rs[i + j * W], sacc);
-        ks[j * TR + tid] = sacc * invd[j];
+        // x_j = (k_j - sum_{i<j} x_i R_ij) / R_jj with four independent partial sums
+        T s4[4] = {T(0), T(0), T(0), T(0)};
+        int i = 0;
+        for (; i + 4 <= j; i += 4) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) s4[u] = fma_acc(ks[(i + u) * TR + tid], Rs[(i + u) + j * W], s4[u]);
+        }
+        for (; i < j; ++i) s4[0] = fma_acc(ks[i * TR + tid], Rs[i + j * W], s4[0]);
+        const T dot = renorm(renorm(s4[0]) + renorm(s4[1])) + renorm(renorm(s4[2]) + renorm(s4[3]));
+        ks[j * TR + tid] = (ks[j * TR + tid] - dot) * invd[j];
       }
     }
     __syncthreads();

@@ -103,14 +103,38 @@ __device__ __noinline__ bool cholqr_panel(const Inst<T>& I, T* K, int N, int W, 
   dfloat* G = reinterpret_cast<dfloat*>(I.blk(B_SA));
   dfloat* Racc = reinterpret_cast<dfloat*>(I.blk(B_SZ1));
   dfloat* Rtmp = reinterpret_cast<dfloat*>(I.blk(B_T1));
-  const bool shifted = sizeof(T) != sizeof(float);
-  const int npass = shifted ? 3 : 2;
+  const bool shiftable = sizeof(T) != sizeof(float);
+  int npass = 2;
   // 11 (N W + W (W+1)) u with u = 2^-44 for the double-float arithmetic
-  const double shift = shifted ? 11.0 * ((double)N * W + (double)W * (W + 1)) * 5.7e-14 : 0.0;
+  const double shift = shiftable ? 11.0 * ((double)N * W + (double)W * (W + 1)) * 5.7e-14 : 0.0;
   if (R) copy_mat<T>(N, W, K, N, Qdst, N);  // backup of K for a late fallback
   for (int pass = 0; pass < npass; ++pass) {
     gram_df<T>(N, W, K, N, G, W, sm.stage);
-    if (!chol_df(W, G, W, pass == 0 ? shift : 0.0)) {
+    bool ok;
+    if (pass == 0 && shiftable) {
+      // plain CholeskyQR2 suffices while kappa(K)^2 u << 1; the spread of the
+      // Cholesky diagonal bounds kappa(K) from below.  Beyond 1e6 (or on a
+      // breakdown) restart from the saved Gram with the shift, three passes.
+      for (int e = threadIdx.x; e < W * W; e += NT) Rtmp[e] = G[e];
+      __syncthreads();
+      ok = chol_df(W, G, W, 0.0);
+      float dmax = 0.0f, dmin = 3.0e38f;
+      for (int j = 0; j < W; ++j) {
+        const float d = G[j + (int64_t)j * W].hi;
+        dmax = fmaxf(dmax, d);
+        dmin = fminf(dmin, d);
+      }
+      if (!ok || !(dmin > 0.0f) || dmax > 1.0e6f * dmin) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < W * W; e += NT) G[e] = Rtmp[e];
+        __syncthreads();
+        ok = chol_df(W, G, W, shift);
+        npass = 3;
+      }
+    } else {
+      ok = chol_df(W, G, W, 0.0);
+    }
+    if (!ok) {
       if (pass > 0 && R) copy_mat<T>(N, W, Qdst, N, K, N);
       return false;
     }
