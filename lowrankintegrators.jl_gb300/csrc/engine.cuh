@@ -526,6 +526,55 @@ struct RowLoadStencilAug {  // row-major staging of [Z | T Z] (note order), widt
 };
 
 template <typename T>
+struct RowLoadPanelStencil {  // row-major staging of [Y | T Z] (Y width r, T Z width r)
+  const T* Y;
+  int ldy;
+  const T* Z;
+  int ldz, N, r;
+  const T* tri;
+  __device__ void operator()(T* __restrict__ xs, int i0, int rows, int lds) const {
+    RowLoadPanelShifted(xs, i0, rows, lds);
+  }
+  __device__ void RowLoadPanelShifted(T* __restrict__ xs, int i0, int rows, int lds) const {
+    const int ii = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const bool ok = ii < rows;
+    const int i = i0 + ii;
+    T cs = T(0), cd = T(0), cp = T(0);
+    if (ok) {
+      cd = tri[N + i];
+      if (i > 0) cs = tri[i];
+      if (i + 1 < N) cp = tri[2 * N + i];
+    }
+    const bool has_m = ok && i > 0, has_p = ok && i + 1 < N;
+    for (int kb = wp; kb < r; kb += 4 * NW) {
+      T yv[4], s4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        T zc = T(0), zm = T(0), zp = T(0), y = T(0);
+        if (ok && k < r) {
+          const T* col = Z + (int64_t)k * ldz;
+          zc = col[i];
+          if (has_m) zm = col[i - 1];
+          if (has_p) zp = col[i + 1];
+          y = Y[i + (int64_t)k * ldy];
+        }
+        yv[u] = y;
+        s4[u] = fma(cs, zm, fma(cp, zp, cd * zc));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + u * NW;
+        if (k < r) {
+          xs[ii * lds + k] = yv[u];
+          xs[ii * lds + r + k] = s4[u];
+        }
+      }
+    }
+  }
+};
+
+template <typename T>
 struct RowLoadStencil {  // row-major staging of T Z, width r
   const T* Z;
   int ldz, N, r;
@@ -564,9 +613,11 @@ struct RowLoadStencil {  // row-major staging of T Z, width r
   }
 };
 
+// Columns [csplit, c) of the result may go to a second destination out2
+// (column csplit of the result is column 0 of out2, same ld).
 template <typename T, class LXr, class LYr>
 __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LYr& ly, T* out, int ldo,
-                          T alpha, T beta) {
+                          T alpha, T beta, T* out2 = nullptr, int csplit = 1 << 30) {
   const int tid = threadIdx.x;
   const int a4 = (a + 3) >> 2, c4 = (c + 3) >> 2;
   const int MT = a4 * c4;
@@ -629,7 +680,7 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
       const int ma = mt / c4, mc = mt - ma * c4;
       const int ia = 4 * ma + (e >> 2), jc = 4 * mc + (e & 3);
       if (ia < a && jc < c) {
-        T* d = out + ia + (int64_t)jc * ldo;
+        T* d = (jc < csplit) ? out + ia + (int64_t)jc * ldo : out2 + ia + (int64_t)(jc - csplit) * ldo;
         *d = (beta == T(0)) ? alpha * s : fma(alpha, s, beta * *d);
       }
     }
@@ -645,7 +696,7 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
           for (int e = 0; e < 16; ++e) {
             const int ia = 4 * ma + (e >> 2), jc = 4 * mc + (e & 3);
             if (ia < a && jc < c) {
-              T* d = out + ia + (int64_t)jc * ldo;
+              T* d = (jc < csplit) ? out + ia + (int64_t)jc * ldo : out2 + ia + (int64_t)(jc - csplit) * ldo;
               *d = (beta == T(0)) ? alpha * acc[u][e] : fma(alpha, acc[u][e], beta * *d);
             }
           }

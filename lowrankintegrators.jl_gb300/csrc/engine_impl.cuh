@@ -264,6 +264,26 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
   T* SK = I.blk(B_SK);
   T* T1 = I.blk(B_T1);
   T* T2 = I.blk(B_T2);
+  // Orthonormal forms: stage P_U, P_V, the state and the four work
+  // matrices in shared memory when they fit (the products then read shared
+  // memory instead of L1/L2).
+  T* Sg = St;
+  if (AssumeOrthonormal<T>::value && 7 * W * W <= Stage<T>::ELEMS) {
+    T* base = sm.stage;
+    T* PUs = base;
+    T* PVs = base + W * W;
+    T* Ss = base + 2 * W * W;
+    copy_mat<T>(p, p, PU, W, PUs, W);
+    copy_mat<T>(q, q, PV, W, PVs, W);
+    copy_mat<T>(p, q, St, W, Ss, W);
+    PU = PUs;
+    PV = PVs;
+    St = Ss;
+    SZ[0] = base + 3 * W * W;
+    SZ[1] = base + 4 * W * W;
+    SK = base + 5 * W * W;
+    SA = base + 6 * W * W;
+  }
   const int ns = sc.nstages;
   const T h = T(dt / sc.nsub);
   for (int sub = 0; sub < sc.nsub; ++sub) {
@@ -302,6 +322,7 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
       __syncthreads();
     }
   }
+  if (St != Sg) copy_mat<T>(p, q, St, W, Sg, W);
 }
 
 // K0 = X * C (C = S, or S^T when trans) into panel Y (N x r).
@@ -336,6 +357,11 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   T* St = I.blk(B_ST);
   T* T1 = I.blk(B_T1);
   const bool sylv = (g.op == OP_SYLVESTER);
+  // fast forms: fuse the basis change M (resp. N) with the projection of the
+  // new basis, written to the otherwise unused KSL blocks until the swap
+  const bool fuse = sylv && AssumeOrthonormal<T>::value && 2 * r <= 128;
+  T* PUn = I.blk(B_RK);
+  T* PVn = I.blk(B_RL);
   if (sylv && g.proj_valid[I.inst] == 0) {
     projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
     projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
@@ -344,16 +370,31 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
   substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
   orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
-  tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
+  if (fuse) {
+    // one pass over Q_K: [M | P_U(new)] = Q_K^T [U0 | A Q_K]
+    tile_gram<T>(n, r, 2 * r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r},
+                 RowLoadPanelStencil<T>{I.U, n, I.k.PQ, n, n, r, I.k.tri}, Mm, W, T(1), T(0), PUn, r);
+  } else {
+    tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
+  }
   // L step (unconventional.jl:144-150), still with the old U
   form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
   substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
   orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
-  tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
+  if (fuse) {
+    tile_gram<T>(m, r, 2 * r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r},
+                 RowLoadPanelStencil<T>{I.V, m, I.l.PQ, m, m, r, I.l.tri}, Nm, W, T(1), T(0), PVn, r);
+  } else {
+    tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
+  }
   // basis swap (unconventional.jl:151-152)
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
-  if (sylv) {
+  if (fuse) {
+    copy_mat<T>(r, r, PUn, W, GU + (int64_t)r * W, W);
+    copy_mat<T>(r, r, PVn, W, GV + (int64_t)r * W, W);
+    if (threadIdx.x == 0) g.proj_valid[I.inst] = 1;
+  } else if (sylv) {
     projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
     projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
     if (threadIdx.x == 0) g.proj_valid[I.inst] = 1;
