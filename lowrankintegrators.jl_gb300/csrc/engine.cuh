@@ -408,6 +408,177 @@ __device__ void tile_sylv(int N, int r, const T* z, const T* tri, const T* P, in
   }
 }
 
+// Coefficients of the stability polynomial R(z) = sum_j gam[j] z^j of an
+// explicit RK scheme with a sub-diagonal tableau (gam[0] = 1):
+//   gam[j+1] = sum_{s>=j} b_s * a_s a_{s-1} ... a_{s-j+1}.
+__device__ inline void horner_coeffs(const Scheme& sc, double gam[5]) {
+  gam[0] = 1.0;
+  for (int j = 1; j < 5; ++j) gam[j] = 0.0;
+  for (int j = 0; j < sc.nstages; ++j) {
+    double gsum = 0.0;
+    for (int st = j; st < sc.nstages; ++st) {
+      double prod = sc.b[st];
+      for (int t = st - j + 1; t <= st; ++t) prod *= sc.a[t];
+      gsum += prod;
+    }
+    gam[j + 1] = gsum;
+  }
+}
+
+// Fused K (or L) substep of the orthonormal-basis Sylvester flow, one row
+// tile at a time entirely in shared memory:
+//   y = X C  (X = U or V, C = S or S^T),  then H = ns*nsub Horner applications
+//   w <- g_j y + h (T w + w P^T),  out = R(hL) y   (rows of this tile)
+// The tile is staged with H halo rows on each side (zero outside [0, N), the
+// operator's boundary); every application recomputes the halo region, whose
+// valid part shrinks by one row per application, so after H applications
+// rows [H, H+TR) are exact.  Global traffic: X read once, out written once.
+// gam[0..ns] are the Horner coefficients of the stability polynomial.
+// Returns false (nothing done) when the tile does not fit the staging area.
+template <typename T>
+__device__ bool fused_substep(int N, int r, const T* X, int ldx, const T* C, int ldc, bool transC, const T* tri,
+                              const T* P, int ldp, const double* gam, int ns, int nsub, T h, T* out, T* stage) {
+  const int tid = threadIdx.x;
+  const int H = ns * nsub;
+  const int c4 = (r + 3) >> 2;
+  const int ldw = c4 * 4;
+  // three tiles of TH rows (multiple of 4) plus C and P^T fill the staging
+  // area; TR = TH - 2H output rows per tile (multiple of 4, <= 256)
+  int TH = ((Stage<T>::ELEMS - 2 * r * ldw) / (3 * r)) & ~3;
+  if (TH > 256 + 2 * H + 3) TH = (256 + 2 * H + 3) & ~3;
+  const int TR = (TH - 2 * H) & ~3;
+  if (TR < 16) return false;
+  T* bufA = stage;
+  T* bufB = bufA + r * TH;
+  T* bufC = bufB + r * TH;
+  T* Cs = bufC + r * TH;   // Cs[k*ldw + c] = C(k, c)
+  T* Ws = Cs + r * ldw;    // Ws[k*ldw + c] = P(c, k)
+  for (int e = tid; e < r * ldw; e += NT) {
+    const int k = e / ldw, c = e - k * ldw;
+    T cv = T(0), wv = T(0);
+    if (c < r) {
+      cv = transC ? C[c + (int64_t)k * ldc] : C[k + (int64_t)c * ldc];
+      wv = P[c + (int64_t)k * ldp];
+    }
+    Cs[e] = cv;
+    Ws[e] = wv;
+  }
+  const int rg4 = TH / 4;
+  const int nmt = rg4 * c4;  // micro-tiles per tile product
+  for (int i0 = 0; i0 < N; i0 += TR) {
+    const int g0 = i0 - H;  // global row of local row 0
+    // stage X rows [g0, g0 + TH) into bufA (zero outside [0, N))
+    for (int ii = tid; ii < TH; ii += NT) {
+      const int i = g0 + ii;
+      const bool ok = (i >= 0) && (i < N);
+      for (int kb = 0; kb < r; kb += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (ok && kb + u < r) ? X[i + (int64_t)(kb + u) * ldx] : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kb + u < r) bufA[(kb + u) * TH + ii] = v[u];
+      }
+    }
+    __syncthreads();
+    // y = X C into bufB
+    for (int mt = tid; mt < nmt; mt += NT) {
+      const int rg = mt / c4, cg = mt - rg * c4;
+      T acc[4][4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+      for (int k = 0; k < r; ++k) {
+        T xv[4], wv[4];
+        ld4(bufA + k * TH + 4 * rg, xv);
+        ld4(Cs + k * ldw + 4 * cg, wv);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (4 * cg + q < r)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) bufB[(4 * cg + q) * TH + 4 * rg + p] = renorm(acc[p][q]);
+    }
+    __syncthreads();
+    // Horner applications: win -> wout, y stays in bufB
+    const T* y = bufB;
+    const T* win = bufB;
+    T* wbuf[2] = {bufC, bufA};
+    int app = 0;
+    for (int sub = 0; sub < nsub; ++sub) {
+      T hw = h * T(gam[ns]);
+      for (int j = ns - 1; j >= 0; --j, ++app) {
+        T* wout = wbuf[app & 1];
+        const T gj = (j == 0) ? T(1) : T(gam[j]);
+        // the substep's base for later substeps is its own result: y is
+        // replaced by wout after each complete substep (below)
+        for (int mt = tid; mt < nmt; mt += NT) {
+          const int rg = mt / c4, cg = mt - rg * c4;
+          T acc[4][4];
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+          for (int k = 0; k < r; ++k) {
+            T xv[4], wv[4];
+            ld4(win + k * TH + 4 * rg, xv);
+            ld4(Ws + k * ldw + 4 * cg, wv);
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+              for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
+          }
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const int li = 4 * rg + p;
+            const int i = g0 + li;
+            const bool inside = (i >= 0) && (i < N);
+            T cs = T(0), cd = T(0), cp = T(0);
+            if (inside) {
+              cd = tri[N + i];
+              if (i > 0) cs = tri[i];
+              if (i + 1 < N) cp = tri[2 * N + i];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int c = 4 * cg + q;
+              if (c < r) {
+                const T* wc = win + c * TH;
+                const T zm = (li > 0) ? wc[li - 1] : T(0);
+                const T zp = (li + 1 < TH) ? wc[li + 1] : T(0);
+                const T tz = fma(cs, zm, fma(cp, zp, cd * wc[li]));
+                const T v = fma(hw, tz + renorm(acc[p][q]), gj * y[c * TH + li]);
+                wout[c * TH + li] = inside ? v : T(0);
+              }
+            }
+          }
+        }
+        __syncthreads();
+        win = wout;
+        hw = h;
+      }
+      if (sub + 1 < nsub) {
+        // next substep starts from this one's result: copy it into bufB (y)
+        T* yb = bufB;
+        for (int e = tid; e < r * TH; e += NT) yb[e] = win[e];
+        __syncthreads();
+        win = bufB;
+      }
+    }
+    // rows [H, H + TR) of the last result are exact
+    const int rows = min(TR, N - i0);
+    for (int c = 0; c < r; ++c)
+      for (int ii = tid; ii < rows; ii += NT) out[(int64_t)(i0 + ii) + (int64_t)c * N] = win[c * TH + H + ii];
+    __syncthreads();
+  }
+  return true;
+}
+
 // W loader: column-major matrix W (ld ldw0) or its transpose.
 template <typename T>
 struct LoadSmall {

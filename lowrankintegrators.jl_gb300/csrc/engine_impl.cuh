@@ -206,16 +206,8 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
   const T* P = Gp + (int64_t)r * I.W;
   const int ns = sc.nstages;
   constexpr bool ortho = AssumeOrthonormal<T>::value;
-  double gam[5] = {1.0, 0.0, 0.0, 0.0, 0.0};
-  for (int j = 0; j < ns; ++j) {
-    double gsum = 0.0;
-    for (int st = j; st < ns; ++st) {
-      double prod = sc.b[st];
-      for (int t = st - j + 1; t <= st; ++t) prod *= sc.a[t];
-      gsum += prod;
-    }
-    gam[j + 1] = gsum;
-  }
+  double gam[5];
+  horner_coeffs(sc, gam);
   const T h = T(dt / sc.nsub);
   T* Zb[2] = {sd.PZ0, sd.PZ1};
   for (int sub = 0; sub < sc.nsub; ++sub) {
@@ -332,6 +324,28 @@ __device__ void form_k0(const Inst<T>& I, const T* X, int N, const T* C, int ldc
   tile_gemm<T>(N, r, r, sm.stage, LoadPanel<T>{X, N}, LoadSmall<T>{C, ldc, trans}, EpiStore<T>{Y, N});
 }
 
+// K0 = X C followed by the substep, into the panel Y (N x r): fused in
+// shared memory for the orthonormal-basis Sylvester flow when the tile fits,
+// else the panel product and the panel-by-panel substep.
+template <typename T>
+__device__ __noinline__ void k_step(const StepArgs<T>& g, const Inst<T>& I, const Side<T>& sd, int side,
+                                    const T* X, const T* C, int ldc, bool transC, T* Y, int r, const T* Gp,
+                                    const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
+  const int N = sd.N;
+  if constexpr (AssumeOrthonormal<T>::value) {
+    if (g.op == OP_SYLVESTER && sc.nstages * sc.nsub <= 8) {
+      double gam[5];
+      horner_coeffs(sc, gam);
+      const T* P = Gp + (int64_t)r * I.W;
+      if (fused_substep<T>(N, r, X, N, C, ldc, transC, sd.tri, P, I.W, gam, sc.nstages, sc.nsub,
+                           T(dt / sc.nsub), Y, sm.stage))
+        return;
+    }
+  }
+  form_k0<T>(I, X, N, C, ldc, transC, Y, r, sm);
+  substep_side<T>(g, I, sd, side, Y, r, Gp, Xo, sc, dt, sm);
+}
+
 template <typename T>
 __device__ void check_finite(const StepArgs<T>& g, const T* S, int r, int ld) {
   __shared__ int bad;
@@ -367,8 +381,7 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
     projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
   }
   // K step (unconventional.jl:136-142)
-  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
-  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
+  k_step<T>(g, I, I.k, 0, I.U, I.S, I.rcap, false, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
   orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
   if (fuse) {
     // one pass over Q_K: [M | P_U(new)] = Q_K^T [U0 | A Q_K]
@@ -378,8 +391,7 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
     tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
   }
   // L step (unconventional.jl:144-150), still with the old U
-  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
-  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
+  k_step<T>(g, I, I.l, 1, I.V, I.S, I.rcap, true, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
   orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
   if (fuse) {
     tile_gram<T>(m, r, 2 * r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r},
@@ -427,14 +439,12 @@ __device__ __noinline__ void ra_bug_step(const StepArgs<T>& g, Inst<T>& I, int r
     projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
   }
   // K step: Uhat = orth([K1 | U0]) (rank_adaptive_unconventional.jl:197-206)
-  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
-  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
+  k_step<T>(g, I, I.k, 0, I.U, I.S, I.rcap, false, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
   copy_mat<T>(n, r, I.U, n, I.k.PY + (int64_t)r * n, n);
   qr_panel<T>(I.k.PY, n, w2, I.k.PQ, nullptr, 0, sm);
   tile_gram<T>(n, w2, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, w2}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
   // L step (:208-217)
-  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
-  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
+  k_step<T>(g, I, I.l, 1, I.V, I.S, I.rcap, true, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
   copy_mat<T>(m, r, I.V, m, I.l.PY + (int64_t)r * m, m);
   qr_panel<T>(I.l.PY, m, w2, I.l.PQ, nullptr, 0, sm);
   tile_gram<T>(m, w2, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, w2}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
@@ -514,8 +524,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   const bool sylv = (g.op == OP_SYLVESTER);
   if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
   // K step (projector_splitting.jl:133-138)
-  form_k0<T>(I, I.U, n, I.S, I.rcap, false, I.k.PY, r, sm);
-  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
+  k_step<T>(g, I, I.k, 0, I.U, I.S, I.rcap, false, I.k.PY, r, GV, I.V, g.sK, dt, sm);
   orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
@@ -523,8 +532,7 @@ __device__ __noinline__ void ksl_primal(const StepArgs<T>& g, Inst<T>& I, int r,
   copy_mat<T>(r, r, RK, W, St, W);
   substep_core<T>(g, I, St, r, r, T(-1), GU, GV, I.U, I.V, g.sS, dt, sm);
   // L step (:145-151)
-  form_k0<T>(I, I.V, m, St, W, true, I.l.PY, r, sm);
-  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
+  k_step<T>(g, I, I.l, 1, I.V, St, W, true, I.l.PY, r, GU, I.U, g.sL, dt, sm);
   orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   // S = R^T
@@ -546,8 +554,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   const bool sylv = (g.op == OP_SYLVESTER);
   if (sylv) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
   // L step (projector_splitting.jl:170-175)
-  form_k0<T>(I, I.V, m, I.S, I.rcap, true, I.l.PY, r, sm);
-  substep_side<T>(g, I, I.l, 1, I.l.PY, r, GU, I.U, g.sL, dt, sm);
+  k_step<T>(g, I, I.l, 1, I.V, I.S, I.rcap, true, I.l.PY, r, GU, I.U, g.sL, dt, sm);
   orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, RL, W, sm);
   copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
   if (sylv) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
@@ -559,8 +566,7 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
   __syncthreads();
   substep_core<T>(g, I, St, r, r, T(-1), GU, GV, I.U, I.V, g.sS, dt, sm);
   // K step (:182-188)
-  form_k0<T>(I, I.U, n, St, W, false, I.k.PY, r, sm);
-  substep_side<T>(g, I, I.k, 0, I.k.PY, r, GV, I.V, g.sK, dt, sm);
+  k_step<T>(g, I, I.k, 0, I.U, St, W, false, I.k.PY, r, GV, I.V, g.sK, dt, sm);
   orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, RK, W, sm);
   copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
   copy_mat<T>(r, r, RK, W, I.S, I.rcap);
