@@ -408,6 +408,35 @@ __device__ void tile_sylv(int N, int r, const T* z, const T* tri, const T* P, in
   }
 }
 
+// acc = sum_{k in [k0,k1)} x(4rg.., k) w(k, 4cg..) with x column-major
+// (ld ldx) and w row-major (ld ldw), both in shared memory.
+template <typename T>
+__device__ __forceinline__ void micro_mm(const T* x, int ldx, const T* w, int ldw, int rg, int cg, int k0, int k1,
+                                         T (&acc)[4][4]) {
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+  for (int k = k0; k < k1; ++k) {
+    T xv[4], wv[4];
+    ld4(x + k * ldx + 4 * rg, xv);
+    ld4(w + k * ldw + 4 * cg, wv);
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
+  }
+}
+
+// Adds the accumulators of lanes 2j and 2j+1 (both end with the sum).
+template <typename T>
+__device__ __forceinline__ void pair_sum(T (&acc)[4][4]) {
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = acc[p][q] + shfl_xor(acc[p][q], 1);
+}
+
 // Coefficients of the stability polynomial R(z) = sum_j gam[j] z^j of an
 // explicit RK scheme with a sub-diagonal tableau (gam[0] = 1):
 //   gam[j+1] = sum_{s>=j} b_s * a_s a_{s-1} ... a_{s-j+1}.
@@ -465,6 +494,10 @@ __device__ bool fused_substep(int N, int r, const T* X, int ldx, const T* C, int
   }
   const int rg4 = TH / 4;
   const int nmt = rg4 * c4;  // micro-tiles per tile product
+  // with at most NT/2 micro-tiles, lane pairs split the k-sum of each one
+  // (one pass per product: every thread runs the shuffle of pair_sum)
+  const int ks = (2 * nmt <= NT) ? 2 : 1;
+  const int kh = (r + ks - 1) / ks;
   for (int i0 = 0; i0 < N; i0 += TR) {
     const int g0 = i0 - H;  // global row of local row 0
     // stage X rows [g0, g0 + TH) into bufA (zero outside [0, N))
@@ -481,28 +514,22 @@ __device__ bool fused_substep(int N, int r, const T* X, int ldx, const T* C, int
       }
     }
     __syncthreads();
-    // y = X C into bufB
-    for (int mt = tid; mt < nmt; mt += NT) {
+    // y = X C into bufB.  With ks == 2 every thread runs exactly one
+    // iteration (nmt * 2 <= NT), so all lanes reach the pair shuffle.
+    for (int t2 = tid; t2 < ((ks == 2) ? NT : nmt); t2 += NT) {
+      const bool act = t2 < nmt * ks;
+      const int mt = act ? t2 / ks : 0, half = t2 % ks;
       const int rg = mt / c4, cg = mt - rg * c4;
       T acc[4][4];
+      micro_mm<T>(bufA, TH, Cs, ldw, rg, cg, act ? half * kh : 0, act ? min(r, (half + 1) * kh) : 0, acc);
+      if (ks == 2) pair_sum(acc);
+      if (act && half == 0) {
 #pragma unroll
-      for (int p = 0; p < 4; ++p)
+        for (int q = 0; q < 4; ++q)
+          if (4 * cg + q < r)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
-      for (int k = 0; k < r; ++k) {
-        T xv[4], wv[4];
-        ld4(bufA + k * TH + 4 * rg, xv);
-        ld4(Cs + k * ldw + 4 * cg, wv);
-#pragma unroll
-        for (int p = 0; p < 4; ++p)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
+            for (int p = 0; p < 4; ++p) bufB[(4 * cg + q) * TH + 4 * rg + p] = renorm(acc[p][q]);
       }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (4 * cg + q < r)
-#pragma unroll
-          for (int p = 0; p < 4; ++p) bufB[(4 * cg + q) * TH + 4 * rg + p] = renorm(acc[p][q]);
     }
     __syncthreads();
     // Horner applications: win -> wout, y stays in bufB
@@ -517,22 +544,14 @@ __device__ bool fused_substep(int N, int r, const T* X, int ldx, const T* C, int
         const T gj = (j == 0) ? T(1) : T(gam[j]);
         // the substep's base for later substeps is its own result: y is
         // replaced by wout after each complete substep (below)
-        for (int mt = tid; mt < nmt; mt += NT) {
+        for (int t2 = tid; t2 < ((ks == 2) ? NT : nmt); t2 += NT) {
+          const bool act = t2 < nmt * ks;
+          const int mt = act ? t2 / ks : 0, half = t2 % ks;
           const int rg = mt / c4, cg = mt - rg * c4;
           T acc[4][4];
-#pragma unroll
-          for (int p = 0; p < 4; ++p)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
-          for (int k = 0; k < r; ++k) {
-            T xv[4], wv[4];
-            ld4(win + k * TH + 4 * rg, xv);
-            ld4(Ws + k * ldw + 4 * cg, wv);
-#pragma unroll
-            for (int p = 0; p < 4; ++p)
-#pragma unroll
-              for (int q = 0; q < 4; ++q) acc[p][q] = fma_acc(xv[p], wv[q], acc[p][q]);
-          }
+          micro_mm<T>(win, TH, Ws, ldw, rg, cg, act ? half * kh : 0, act ? min(r, (half + 1) * kh) : 0, acc);
+          if (ks == 2) pair_sum(acc);
+          if (!act || half != 0) continue;
 #pragma unroll
           for (int p = 0; p < 4; ++p) {
             const int li = 4 * rg + p;
