@@ -170,6 +170,11 @@ LRI_API lri_status lri_batch_data_init(lri_batch* b, const void* Y0, void* strea
 LRI_API lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, const void* Ynext,
                           void* stream);
 
+/* Builds (without running) the CUDA graph that lri_batch_step uses for a
+ * call with this (dt, nsteps), so the first such call does not pay for the
+ * capture.  No counterpart in the reference. */
+LRI_API lri_status lri_batch_prepare(lri_batch* b, double dt, int32_t nsteps);
+
 /* Current ranks (host array of length count; synchronises the stream). */
 LRI_API lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream);
 

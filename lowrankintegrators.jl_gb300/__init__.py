@@ -411,6 +411,21 @@ class Batch:
         _native.check(self.lib.lri_batch_step(self.handle, float(t), float(dt), int(nsteps), yptr,
                                               self._stream()), "lri_batch_step")
 
+    def prepare(self, dt: float, nsteps: int):
+        """Builds the CUDA graph of an nsteps-step call ahead of time."""
+        if nsteps > 1 and self.op_kind != _native.LRI_OP_DATA:
+            _native.check(self.lib.lri_batch_prepare(self.handle, float(dt), int(nsteps)), "lri_batch_prepare")
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.lri_batch_launches_per_step(self.handle))
+
+    def launches(self, nsteps: int) -> int:
+        """Kernel launches of one step(t, dt, nsteps) call: the per-step
+        engine launches, plus the double-float write-back once per call."""
+        per = self.launches_per_step()
+        wb = 3 if self.precision == "df" else 0
+        return nsteps * (per - wb) + wb
+
     def ranks(self) -> np.ndarray:
         out = np.zeros(self.count, np.int64)
         _native.check(self.lib.lri_batch_ranks(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64)),
@@ -622,6 +637,13 @@ class MixedEnsemble:
 
     def launches_per_step(self) -> int:
         return sum(int(b.lib.lri_batch_launches_per_step(b.handle)) for _, _, b, _ in self.parts)
+
+    def launches(self, nsteps: int) -> int:
+        return sum(b.launches(nsteps) for _, _, b, _ in self.parts)
+
+    def prepare(self, dt: float, nsteps: int):
+        for _, _, b, _ in self.parts:
+            b.prepare(dt, nsteps)
 
     def check_status(self):
         for _, _, b, st in self.parts:

@@ -419,32 +419,39 @@ lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, con
     if (e == cudaSuccess) e = writeback(b, st);
     return cuda_status(e);
   }
+  const lri_status ps = lri_batch_prepare(b, dt, nsteps);
+  if (ps != LRI_OK) return ps;
+  return cuda_status(cudaGraphLaunch(b->gexec, st));
+}
+
+lri_status lri_batch_prepare(lri_batch* b, double dt, int32_t nsteps) {
+  if (!b || nsteps < 2 || !std::isfinite(dt)) return LRI_ERR_ARG;
+  if (!b->bound) return LRI_ERR_STATE;
+  if (b->desc.op == LRI_OP_DATA) return LRI_ERR_UNSUPPORTED;
   // The engine's operators are autonomous, so a captured graph depends on
   // (nsteps, dt) only and is reused across calls.
-  if (!(b->gexec && b->g_steps == nsteps && b->g_dt == dt)) {
-    free_graph(b);
-    // make sure the kernel attribute is set outside of capture
-    cudaGraph_t graph = nullptr;
-    LRI_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = launch_one(b, t + k * dt, dt, nullptr, b->cap_stream);
-    if (e == cudaSuccess) e = writeback(b, b->cap_stream);
-    cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &graph);
-    if (e != cudaSuccess || e2 != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      cudaGetLastError();
-      return LRI_ERR_CUDA;
-    }
-    e = cudaGraphInstantiate(&b->gexec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-      b->gexec = nullptr;
-      return LRI_ERR_CUDA;
-    }
-    b->g_steps = nsteps;
-    b->g_dt = dt;
+  if (b->gexec && b->g_steps == nsteps && b->g_dt == dt) return LRI_OK;
+  free_graph(b);
+  cudaGraph_t graph = nullptr;
+  LRI_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = launch_one(b, k * dt, dt, nullptr, b->cap_stream);
+  if (e == cudaSuccess) e = writeback(b, b->cap_stream);
+  cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return LRI_ERR_CUDA;
   }
-  return cuda_status(cudaGraphLaunch(b->gexec, st));
+  e = cudaGraphInstantiate(&b->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    b->gexec = nullptr;
+    return LRI_ERR_CUDA;
+  }
+  b->g_steps = nsteps;
+  b->g_dt = dt;
+  return LRI_OK;
 }
 
 lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream) {

@@ -332,7 +332,9 @@ __device__ __noinline__ void k_step(const StepArgs<T>& g, const Inst<T>& I, cons
                                     const T* X, const T* C, int ldc, bool transC, T* Y, int r, const T* Gp,
                                     const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
   const int N = sd.N;
-  if constexpr (AssumeOrthonormal<T>::value) {
+  // (float only: for double-float the halo recomputation costs more
+  // arithmetic than the saved panel passes are worth)
+  if constexpr (AssumeOrthonormal<T>::value && sizeof(T) == 4) {
     if (g.op == OP_SYLVESTER && sc.nstages * sc.nsub <= 8) {
       double gam[5];
       horner_coeffs(sc, gam);

@@ -90,6 +90,7 @@ def test_create_rejects_bad_scheme_and_unsupported(lri):
     # null arguments
     assert lib.lri_batch_create(None, C.byref(d), C.byref(a)) == 1
     assert lib.lri_batch_step(None, 0.0, 0.1, 1, None, None) == 1
+    assert lib.lri_batch_prepare(None, 0.1, 5) == 1
     assert lib.lri_batch_destroy(None) == 1
 
 

@@ -122,6 +122,33 @@ def test_batched_uneven_instances(lri, oracle, precision):
         assert err <= TOL[precision], f"instance {i} {shapes[i]}: {err:.3e}"
 
 
+@pytest.mark.parametrize("precision", ["fp64", "df", "fp32"])
+def test_prepared_graph_matches_single_steps(lri, precision):
+    """lri_batch_prepare builds the graph of a multi-step call ahead of time;
+    running it must give what the same steps give as single-step calls."""
+    shapes = [(64, 70, 4), (128, 90, 8), (96, 96, 16)]
+    insts = [sylv_instance(300 + i, *s, graded=False) for i, s in enumerate(shapes)]
+    alg = lri.UnconventionalAlgorithm(lri.RK4(1))
+    nat = lri._native
+    ys = []
+    for graph in (False, True):
+        b = lri.Batch([s[0] for s in shapes], [s[1] for s in shapes], [s[2] for s in shapes], alg,
+                      nat.LRI_OP_SYLVESTER_TRIDIAG, precision)
+        b.upload([lri.SVDLikeRepresentation(U, S, V) for (A, B, U, S, V) in insts],
+                 [lri.SylvesterTridiagOperator(A, B) for (A, B, U, S, V) in insts])
+        if graph:
+            b.prepare(1e-2, 9)
+            b.step(0.0, 1e-2, 9)
+        else:
+            for k in range(9):
+                b.step(k * 1e-2, 1e-2, 1)
+        b.check_status()
+        ys.append([f.full() for f in b.download()])
+        b.close()
+    for y1, y2 in zip(*ys):
+        assert np.linalg.norm(y1 - y2) <= 1e-13 * np.linalg.norm(y1)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "df", "mixed", "fp32"])
 def test_lyapunov_ensemble_slice(lri, oracle, precision):
     """32 instances of the 4096-member Lyapunov ensemble, full 200 steps.
