@@ -848,6 +848,10 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
           }
         }
       }
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int e = 0; e < 16; ++e) acc[u][e] = renorm(acc[u][e]);
     }
     __syncthreads();
   }
@@ -1185,24 +1189,35 @@ __device__ __forceinline__ dfloat acc_mul(dfloat acc, float x, float y) {
   return lri_df::fast_two_sum(s.hi, s.lo + (acc.lo + e));
 }
 __device__ __forceinline__ dfloat acc_mul(dfloat acc, dfloat x, dfloat y) { return fma(x, y, acc); }
+// the same without the final renormalisation (renorm() before reading)
+__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, float x, float y) { return acc_mul(acc, x, y); }
+__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, dfloat x, dfloat y) { return lri_df::fma_acc(x, y, acc); }
 __device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.0f); }
 __device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
 __device__ __forceinline__ void from_df(dfloat x, float& y) { y = x.hi + x.lo; }
 __device__ __forceinline__ void from_df(dfloat x, dfloat& y) { y = x; }
 
 // G = X^T X (W x W, W <= 64) accumulated in double-float; X is N x W
-// (column-major, ld ldx, type T), G column-major with ld ldg.
+// (column-major, ld ldx, type T), G column-major with ld ldg.  Only the 4x4
+// micro-tiles on and above the diagonal are accumulated (the lower ones are
+// their transposes), with a renormalisation after every staged row chunk.
 template <typename T>
 __device__ __noinline__ void gram_df(int N, int W, const T* X, int ldx, dfloat* G, int ldg, T* stage) {
   const int tid = threadIdx.x;
   const int w4 = (W + 3) >> 2;
-  const int MT = w4 * w4;                 // <= 256 = NT
+  const int MT = w4 * (w4 + 1) / 2;       // <= 136 <= NT
   const int splits = NT / MT;
   const int lds = w4 * 4 + 4;
   T* xs = stage;
   const int mt = tid % MT, split = tid / MT;
   const bool active = split < splits;
-  const int ma = mt / w4, mc = mt - ma * w4;
+  // micro-tile mt -> (ma, mc) with ma <= mc, row-major over the upper triangle
+  int ma = 0, rem = mt;
+  while (rem >= w4 - ma) {
+    rem -= w4 - ma;
+    ++ma;
+  }
+  const int mc = ma + rem;
   dfloat acc[16];
 #pragma unroll
   for (int e = 0; e < 16; ++e) acc[e] = dfloat(0.0f, 0.0f);
@@ -1218,8 +1233,10 @@ __device__ __noinline__ void gram_df(int N, int W, const T* X, int ldx, dfloat* 
 #pragma unroll
         for (int p = 0; p < 4; ++p)
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc[p * 4 + q] = acc_mul(acc[p * 4 + q], xa[p], xb[q]);
+          for (int q = 0; q < 4; ++q) acc[p * 4 + q] = acc_mul_acc(acc[p * 4 + q], xa[p], xb[q]);
       }
+#pragma unroll
+      for (int e = 0; e < 16; ++e) acc[e] = renorm(acc[e]);
     }
     __syncthreads();
   }
@@ -1233,9 +1250,17 @@ __device__ __noinline__ void gram_df(int N, int W, const T* X, int ldx, dfloat* 
     const int m2 = o >> 4, e = o & 15;
     dfloat sum = part[m2 * 16 + e];
     for (int sp = 1; sp < splits; ++sp) sum += part[(sp * MT + m2) * 16 + e];
-    const int a2 = m2 / w4, c2 = m2 - a2 * w4;
+    int a2 = 0, r2 = m2;
+    while (r2 >= w4 - a2) {
+      r2 -= w4 - a2;
+      ++a2;
+    }
+    const int c2 = a2 + r2;
     const int ia = 4 * a2 + (e >> 2), jc = 4 * c2 + (e & 3);
-    if (ia < W && jc < W) G[ia + (int64_t)jc * ldg] = sum;
+    if (ia < W && jc < W) {
+      G[ia + (int64_t)jc * ldg] = sum;
+      if (a2 != c2) G[jc + (int64_t)ia * ldg] = sum;
+    }
   }
   __syncthreads();
 }
