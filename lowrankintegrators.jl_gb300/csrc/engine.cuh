@@ -805,9 +805,12 @@ struct RowLoadStencil {  // row-major staging of T Z, width r
 
 // Columns [csplit, c) of the result may go to a second destination out2
 // (column csplit of the result is column 0 of out2, same ld).
-template <typename T, class LXr, class LYr>
-__device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LYr& ly, T* out, int ldo,
-                          T alpha, T beta, T* out2 = nullptr, int csplit = 1 << 30) {
+// PER = micro-tiles per thread (1 when a4 * c4 <= NT, else 2); separate
+// non-inlined instances so the common one-tile case keeps half the
+// accumulators in registers.
+template <typename T, int PER, class LXr, class LYr>
+__device__ __noinline__ void tile_gram_impl(int N, int a, int c, T* stage, const LXr lx, const LYr ly, T* out,
+                                            int ldo, T alpha, T beta, T* out2, int csplit) {
   const int tid = threadIdx.x;
   const int a4 = (a + 3) >> 2, c4 = (c + 3) >> 2;
   const int MT = a4 * c4;
@@ -815,10 +818,10 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
   T* xs = stage;
   T* ys = stage + TRG * lxs;
   const int splits = (MT >= NT) ? 1 : (NT / MT);
-  const int per = (MT + NT - 1) / NT;  // micro-tiles per thread when splits == 1 (<= 2)
-  T acc[2][16];
+  const int per = PER;
+  T acc[PER][16];
 #pragma unroll
-  for (int u = 0; u < 2; ++u)
+  for (int u = 0; u < PER; ++u)
 #pragma unroll
     for (int e = 0; e < 16; ++e) acc[u][e] = T(0);
   const int mt0 = (splits > 1) ? (tid % MT) : tid;
@@ -831,7 +834,7 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
     __syncthreads();
     if (active) {
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < PER; ++u) {
         if (u < per) {
           const int mt = mt0 + u * NT;
           if (mt < MT) {
@@ -849,14 +852,14 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
         }
       }
 #pragma unroll
-      for (int u = 0; u < 2; ++u)
+      for (int u = 0; u < PER; ++u)
 #pragma unroll
         for (int e = 0; e < 16; ++e) acc[u][e] = renorm(acc[u][e]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int u = 0; u < 2; ++u)
+  for (int u = 0; u < PER; ++u)
 #pragma unroll
     for (int e = 0; e < 16; ++e) acc[u][e] = renorm(acc[u][e]);
   // combine splits through shared memory (deterministic order)
@@ -881,7 +884,7 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
     __syncthreads();
   } else {
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < PER; ++u) {
       if (u < per) {
         const int mt = mt0 + u * NT;
         if (mt < MT) {
@@ -899,6 +902,15 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
     }
     __syncthreads();
   }
+}
+
+template <typename T, class LXr, class LYr>
+__device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LYr& ly, T* out, int ldo,
+                          T alpha, T beta, T* out2 = nullptr, int csplit = 1 << 30) {
+  if (((a + 3) >> 2) * ((c + 3) >> 2) <= NT)
+    tile_gram_impl<T, 1, LXr, LYr>(N, a, c, stage, lx, ly, out, ldo, alpha, beta, out2, csplit);
+  else
+    tile_gram_impl<T, 2, LXr, LYr>(N, a, c, stage, lx, ly, out, ldo, alpha, beta, out2, csplit);
 }
 
 // ---------------------------------------------------------------------------
@@ -1267,94 +1279,113 @@ __device__ __noinline__ void gram_df(int N, int W, const T* X, int ldx, dfloat* 
 
 // In-place upper Cholesky G = R^T R of a W x W double-float matrix (ld ldg),
 // optionally shifted first: G + shift * trace(G) * I.  Returns false on a
-// non-positive pivot (G is then unusable).
-static __device__ __noinline__ bool chol_df(int W, dfloat* G, int ldg, double shift_rel) {
+// non-positive pivot (G is then unusable).  The factorisation runs in the
+// shared buffer gs (W*W values) with two block barriers per column: every
+// thread forms the pivot itself (no broadcast), then the trailing update is
+// spread over the block.  The lower triangle of G keeps its input values.
+static __device__ __noinline__ bool chol_df(int W, dfloat* G, int ldg, double shift_rel, dfloat* gs) {
   const int tid = threadIdx.x;
-  __shared__ int bad;
-  if (tid == 0) {
-    bad = 0;
-    if (shift_rel > 0.0) {
-      dfloat tr(0.0f, 0.0f);
-      for (int j = 0; j < W; ++j) tr += G[j + (int64_t)j * ldg];
-      const dfloat sh = tr * dfloat(shift_rel);
-      for (int j = 0; j < W; ++j) G[j + (int64_t)j * ldg] += sh;
-    }
-  }
+  __shared__ int bad_s;
+  for (int e = tid; e < W * W; e += NT) gs[e] = G[(e % W) + (int64_t)(e / W) * ldg];
+  if (tid == 0) bad_s = 0;
   __syncthreads();
+  if (shift_rel > 0.0) {
+    dfloat tr(0.0f, 0.0f);
+    for (int j = 0; j < W; ++j) tr += gs[j + j * W];
+    const dfloat sh = tr * dfloat(shift_rel);
+    __syncthreads();
+    for (int j = tid; j < W; j += NT) gs[j + j * W] += sh;
+    __syncthreads();
+  }
   for (int k = 0; k < W; ++k) {
+    dfloat d = gs[k + k * W];
+    const bool bad = !(d.hi > 0.0f);
+    if (bad) d = dfloat(1.0f, 0.0f);
+    const dfloat rkk = sqrt(d);
+    const dfloat inv = dfloat(1.0f, 0.0f) / rkk;
+    for (int j = k + 1 + tid; j < W; j += NT) gs[k + j * W] = gs[k + j * W] * inv;
+    __syncthreads();
     if (tid == 0) {
-      dfloat d = G[k + (int64_t)k * ldg];
-      if (!(d.hi > 0.0f)) {
-        bad = 1;
-        d = dfloat(1.0f, 0.0f);
-      }
-      G[k + (int64_t)k * ldg] = sqrt(d);
+      gs[k + k * W] = rkk;
+      if (bad) bad_s = 1;
     }
-    __syncthreads();
-    const dfloat inv = dfloat(1.0f, 0.0f) / G[k + (int64_t)k * ldg];
-    for (int j = k + 1 + tid; j < W; j += NT) G[k + (int64_t)j * ldg] = G[k + (int64_t)j * ldg] * inv;
-    __syncthreads();
     const int cnt = W - k - 1;
     for (int e = tid; e < cnt * cnt; e += NT) {
       const int i = k + 1 + e % cnt, j = k + 1 + e / cnt;
-      if (i <= j) G[i + (int64_t)j * ldg] = fma(-G[k + (int64_t)i * ldg], G[k + (int64_t)j * ldg], G[i + (int64_t)j * ldg]);
+      if (i <= j) gs[i + j * W] = fma(-gs[k + i * W], gs[k + j * W], gs[i + j * W]);
     }
     __syncthreads();
   }
-  const bool ok = (bad == 0);
+  for (int e = tid; e < W * W; e += NT) {
+    const int i = e % W, j = e / W;
+    if (i <= j) G[i + (int64_t)j * ldg] = gs[e];
+  }
+  const bool ok = (bad_s == 0);
   __syncthreads();
   return ok;
 }
 
 // K <- K R^{-1} row by row (forward substitution, backward stable), R upper
 // triangular W x W double-float (ld ldr); K is N x W (T, ld N).  Row tiles are
-// staged in shared memory with one row per thread.
+// staged in shared memory with one row per thread; the columns are solved in
+// blocks of four, so each staged x_i feeds four accumulators and R is read
+// as row segments of four (R kept row-major in shared memory).
 template <typename T>
 __device__ __noinline__ void trsm_rows(int N, int W, T* K, const dfloat* R, int ldr, T* stage, T* invd) {
   const int tid = threadIdx.x;
-  T* Rs = stage;  // W x W upper triangle
-  for (int e = tid; e < W * W; e += NT) {
-    const int i = e % W, j = e / W;
+  const int Wp = (W + 3) & ~3;
+  T* Rt = stage;  // Wp x Wp row-major: Rt[i * Wp + j] = R_ij for i <= j < W, else 0
+  for (int e = tid; e < Wp * Wp; e += NT) {
+    const int i = e / Wp, j = e - (e / Wp) * Wp;
     T v;
-    from_df((i <= j) ? R[i + (int64_t)j * ldr] : dfloat(0.0f, 0.0f), v);
-    Rs[e] = v;
+    from_df((i <= j && j < W) ? R[i + (int64_t)j * ldr] : dfloat(0.0f, 0.0f), v);
+    Rt[e] = v;
   }
-  for (int j = tid; j < W; j += NT) {
+  for (int j = tid; j < Wp; j += NT) {
     T v;
-    from_df(dfloat(1.0f, 0.0f) / R[j + (int64_t)j * ldr], v);
+    from_df(j < W ? dfloat(1.0f, 0.0f) / R[j + (int64_t)j * ldr] : dfloat(0.0f, 0.0f), v);
     invd[j] = v;
   }
-  int TR = (Stage<T>::ELEMS - W * W) / W;
+  int TR = (Stage<T>::ELEMS - Wp * Wp) / Wp;
   if (TR > NT) TR = NT;
   TR &= ~31;
-  T* ks = stage + W * W;  // [W][TR]
+  T* ks = stage + Wp * Wp;  // [Wp][TR]; the padding columns hold zeros
   __syncthreads();
   for (int i0 = 0; i0 < N; i0 += TR) {
     const int rows = min(TR, N - i0);
     for (int ii = tid; ii < rows; ii += NT) {
       const T* src = K + i0 + ii;
-      for (int kb = 0; kb < W; kb += 8) {
+      for (int kb = 0; kb < Wp; kb += 8) {
         T v[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) v[u] = (kb + u < W) ? src[(int64_t)(kb + u) * N] : T(0);
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-          if (kb + u < W) ks[(kb + u) * TR + ii] = v[u];
+          if (kb + u < Wp) ks[(kb + u) * TR + ii] = v[u];
       }
     }
     __syncthreads();
     if (tid < rows) {
-      for (int j = 0; j < W; ++j) {
-        // x_j = (k_j - sum_{i<j} x_i R_ij) / R_jj with four independent partial sums
-        T s4[4] = {T(0), T(0), T(0), T(0)};
-        int i = 0;
-        for (; i + 4 <= j; i += 4) {
+      for (int jb = 0; jb < Wp; jb += 4) {
+        // x_j = (k_j - sum_{i<j} x_i R_ij) / R_jj for j = jb .. jb+3
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        for (int i = 0; i < jb; ++i) {
+          const T x = ks[i * TR + tid];
+          T rr[4];
+          ld4(Rt + i * Wp + jb, rr);
 #pragma unroll
-          for (int u = 0; u < 4; ++u) s4[u] = fma_acc(ks[(i + u) * TR + tid], Rs[(i + u) + j * W], s4[u]);
+          for (int u = 0; u < 4; ++u) acc[u] = fma_acc(x, rr[u], acc[u]);
         }
-        for (; i < j; ++i) s4[0] = fma_acc(ks[i * TR + tid], Rs[i + j * W], s4[0]);
-        const T dot = renorm(renorm(s4[0]) + renorm(s4[1])) + renorm(renorm(s4[2]) + renorm(s4[3]));
-        ks[j * TR + tid] = (ks[j * TR + tid] - dot) * invd[j];
+        T xb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          T sum = renorm(acc[u]);
+#pragma unroll
+          for (int v = 0; v < u; ++v) sum = fma_acc(xb[v], Rt[(jb + v) * Wp + jb + u], sum);
+          xb[u] = (ks[(jb + u) * TR + tid] - renorm(sum)) * invd[jb + u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) ks[(jb + u) * TR + tid] = xb[u];
       }
     }
     __syncthreads();

@@ -117,7 +117,7 @@ __device__ __noinline__ bool cholqr_panel(const Inst<T>& I, T* K, int N, int W, 
       // breakdown) restart from the saved Gram with the shift, three passes.
       for (int e = threadIdx.x; e < W * W; e += NT) Rtmp[e] = G[e];
       __syncthreads();
-      ok = chol_df(W, G, W, 0.0);
+      ok = chol_df(W, G, W, 0.0, reinterpret_cast<dfloat*>(sm.stage));
       float dmax = 0.0f, dmin = 3.0e38f;
       for (int j = 0; j < W; ++j) {
         const float d = G[j + (int64_t)j * W].hi;
@@ -128,11 +128,11 @@ __device__ __noinline__ bool cholqr_panel(const Inst<T>& I, T* K, int N, int W, 
         __syncthreads();
         for (int e = threadIdx.x; e < W * W; e += NT) G[e] = Rtmp[e];
         __syncthreads();
-        ok = chol_df(W, G, W, shift);
+        ok = chol_df(W, G, W, shift, reinterpret_cast<dfloat*>(sm.stage));
         npass = 3;
       }
     } else {
-      ok = chol_df(W, G, W, 0.0);
+      ok = chol_df(W, G, W, 0.0, reinterpret_cast<dfloat*>(sm.stage));
     }
     if (!ok) {
       if (pass > 0 && R) copy_mat<T>(N, W, Qdst, N, K, N);
