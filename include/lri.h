@@ -193,9 +193,9 @@ LRI_API lri_status lri_batch_status(lri_batch* b, void* stream);
  *   dtype   LRI_F64 or LRI_F32 (LRI_DF: LRI_ERR_UNSUPPORTED)
  *   U (n x r), S (r x r), V (m x r)  caller's device buffers, column-major,
  *           updated in place; A (3n), B (3m) device coefficient vectors
- *   Sizes whose workspace exceeds the scratch, elem_size * (5r(n+m) + 15r^2)
+ *   Sizes whose workspace exceeds the scratch, elem_size * (5r(n+m) + 23r^2)
  *   + 256 bytes > 4 MiB (each term padded to 4 elements; for example
- *   n + m > 3200 at r = 32 in FP64), are rejected with LRI_ERR_ARG.
+ *   n + m > 3120 at r = 32 in FP64), are rejected with LRI_ERR_ARG.
  * The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture.  All calls share the one array and leave their

@@ -595,11 +595,18 @@ def core_condition(S: np.ndarray) -> float:
     return float(s[0] / s[-1]) if s[-1] > 0 else float("inf")
 
 
-# Fixed-rank BUG amplifies a relative perturbation of the factors by about
-# kappa(S) * dt per step: FP32 factors meet a 1e-5 relative error budget over
-# a few hundred steps only while kappa(S) stays below roughly 1e4.  Beyond
-# that the mixed form runs the instance in double-float.
-MIXED_KAPPA_MAX = 1.0e4
+# The FP32 form (FP32 panels; basis changes, projections and S-step in
+# double-float) keeps a rounding floor of a few 1e-6 relative error over a
+# hundred steps, independent of the core's conditioning, until the core's
+# smallest singular values approach the FP32 rounding level of the largest:
+# the K/L panels mix columns of size sigma_1 into columns of size sigma_r, so
+# each step perturbs the small directions by u_32 * kappa(S) relative to
+# their size.  Measured on the 4096-instance Lyapunov ensemble (103 steps,
+# graded cores kappa = 2^(r-1)): max error <= 5.7e-6 up to kappa = 2^22,
+# first failures at 2^23, total loss beyond 2^24 = 1/u_32.  The mixed form
+# runs an instance in FP32 while kappa(S0) <= 2^21 (u_32 * kappa <= 1/8),
+# else in double-float.
+MIXED_KAPPA_MAX = 2.0 ** 21
 
 
 class MixedEnsemble:

@@ -255,7 +255,7 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
     d.offWL = b->totWork;
     b->totWork += al(m * (2 * w + 3 * rc));
     d.offSmall = b->totSmall;
-    b->totSmall += 15 * al(w * w);  // 15 blocks, each padded to 4 elements (see Inst::blk)
+    b->totSmall += lri::kSmallBlocks * al(w * w);  // blocks padded to 4 elements (see Inst::blk)
     d.offY = b->totY;
     if (desc->op == LRI_OP_DATA) b->totY += n * m;
   }

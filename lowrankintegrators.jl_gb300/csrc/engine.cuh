@@ -60,6 +60,28 @@ __device__ __forceinline__ double fma_acc(double a, double b, double c) { return
 __device__ __forceinline__ float renorm(float a) { return a; }
 __device__ __forceinline__ double renorm(double a) { return a; }
 using lri_df::fma_acc;
+
+// acc + x*y accumulated in double-float: exact FP32 products (TwoProduct)
+// for float inputs, double-float FMA for double-float inputs.
+__device__ __forceinline__ dfloat acc_mul(dfloat acc, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);
+  const dfloat s = lri_df::two_sum(acc.hi, p);
+  return lri_df::fast_two_sum(s.hi, s.lo + (acc.lo + e));
+}
+__device__ __forceinline__ dfloat acc_mul(dfloat acc, dfloat x, dfloat y) { return fma(x, y, acc); }
+// the same without the final renormalisation (renorm() before reading)
+__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);
+  const dfloat s = lri_df::two_sum(acc.hi, p);
+  return dfloat(s.hi, acc.lo + (s.lo + e));
+}
+__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, dfloat x, dfloat y) { return lri_df::fma_acc(x, y, acc); }
+__device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.0f); }
+__device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
+__device__ __forceinline__ void from_df(dfloat x, float& y) { y = x.hi + x.lo; }
+__device__ __forceinline__ void from_df(dfloat x, dfloat& y) { y = x; }
 using lri_df::renorm;
 
 template <typename T>
@@ -913,6 +935,71 @@ __device__ void tile_gram(int N, int a, int c, T* stage, const LXr& lx, const LY
     tile_gram_impl<T, 2, LXr, LYr>(N, a, c, stage, lx, ly, out, ldo, alpha, beta, out2, csplit);
 }
 
+// tile_gram for FP32 panels with double-float accumulation (exact FP32
+// products, double-float sums; renormalised after every staged row chunk):
+// X^T Y (a x c, a4 * c4 <= NT) to the double-float matrices outd (columns
+// [0, csplit)) and out2d (columns [csplit, c)), ld ldo, and optionally their
+// FP32 roundings to outf / out2f (same ld).  Ends with __syncthreads().
+template <class LXr, class LYr>
+__device__ __noinline__ void tile_gram_acc(int N, int a, int c, float* stage, const LXr lx, const LYr ly,
+                                           dfloat* outd, dfloat* out2d, float* outf, float* out2f, int ldo,
+                                           int csplit) {
+  const int tid = threadIdx.x;
+  const int a4 = (a + 3) >> 2, c4 = (c + 3) >> 2;
+  const int MT = a4 * c4;  // <= NT
+  const int lxs = a4 * 4 + 4, lys = c4 * 4 + 4;
+  float* xs = stage;
+  float* ys = stage + TRG * lxs;
+  const int splits = NT / MT;
+  const int mt = tid % MT, split = tid / MT;
+  const bool active = split < splits;
+  const int ma = mt / c4, mc = mt - (mt / c4) * c4;
+  dfloat acc[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) acc[e] = dfloat(0.0f, 0.0f);
+  for (int i0 = 0; i0 < N; i0 += TRG) {
+    const int rows = min(TRG, N - i0);
+    lx(xs, i0, rows, lxs);
+    ly(ys, i0, rows, lys);
+    __syncthreads();
+    if (active) {
+      for (int ii = split; ii < rows; ii += splits) {
+        float xv[4], yv[4];
+        ld4(xs + ii * lxs + 4 * ma, xv);
+        ld4(ys + ii * lys + 4 * mc, yv);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p * 4 + q] = acc_mul_acc(acc[p * 4 + q], xv[p], yv[q]);
+      }
+#pragma unroll
+      for (int e = 0; e < 16; ++e) acc[e] = renorm(acc[e]);
+    }
+    __syncthreads();
+  }
+  dfloat* part = reinterpret_cast<dfloat*>(stage);  // splits * MT * 16 <= NT * 16 values
+  if (active) {
+#pragma unroll
+    for (int e = 0; e < 16; ++e) part[(split * MT + mt) * 16 + e] = acc[e];
+  }
+  __syncthreads();
+  for (int o = tid; o < MT * 16; o += NT) {
+    const int m2 = o >> 4, e = o & 15;
+    dfloat sum = part[m2 * 16 + e];
+    for (int sp = 1; sp < splits; ++sp) sum += part[(sp * MT + m2) * 16 + e];
+    const int a2 = m2 / c4, c2 = m2 - (m2 / c4) * c4;
+    const int ia = 4 * a2 + (e >> 2), jc = 4 * c2 + (e & 3);
+    if (ia < a && jc < c) {
+      const bool first = jc < csplit;
+      const int64_t off = ia + (int64_t)(first ? jc : jc - csplit) * ldo;
+      (first ? outd : out2d)[off] = sum;
+      float* of = first ? outf : out2f;
+      if (of) of[off] = sum.hi + sum.lo;
+    }
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Small dense products on column-major matrices in global scratch:
 //   C(p x s) = alpha * op(A)(p x q) * op(B)(q x s) + beta * C
@@ -1192,22 +1279,6 @@ __device__ __noinline__ void hh_form_q_inplace(T* A, int lda, int N, int W, Smem
 // Cholesky-based QR pieces for the fast forms (FP32 and double-float).
 // ---------------------------------------------------------------------------
 
-// acc + x*y accumulated in double-float: exact FP32 products (TwoProduct)
-// for float inputs, double-float FMA for double-float inputs.
-__device__ __forceinline__ dfloat acc_mul(dfloat acc, float x, float y) {
-  const float p = x * y;
-  const float e = fmaf(x, y, -p);
-  const dfloat s = lri_df::two_sum(acc.hi, p);
-  return lri_df::fast_two_sum(s.hi, s.lo + (acc.lo + e));
-}
-__device__ __forceinline__ dfloat acc_mul(dfloat acc, dfloat x, dfloat y) { return fma(x, y, acc); }
-// the same without the final renormalisation (renorm() before reading)
-__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, float x, float y) { return acc_mul(acc, x, y); }
-__device__ __forceinline__ dfloat acc_mul_acc(dfloat acc, dfloat x, dfloat y) { return lri_df::fma_acc(x, y, acc); }
-__device__ __forceinline__ dfloat to_df(float x) { return dfloat(x, 0.0f); }
-__device__ __forceinline__ dfloat to_df(dfloat x) { return x; }
-__device__ __forceinline__ void from_df(dfloat x, float& y) { y = x.hi + x.lo; }
-__device__ __forceinline__ void from_df(dfloat x, dfloat& y) { y = x; }
 
 // G = X^T X (W x W, W <= 64) accumulated in double-float; X is N x W
 // (column-major, ld ldx, type T), G column-major with ld ldg.  Only the 4x4

@@ -13,6 +13,11 @@ namespace lri {
 
 using lri_df::dfloat;
 
+// Blocks of W*W elements (each rounded up to 4 elements) in an instance's
+// small scratch: projections, basis changes, core-step work matrices, and
+// the double-float copies of M, N, P_U, P_V of the FP32 class.
+constexpr int kSmallBlocks = 23;
+
 enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2 };
 enum KslOrder : int32_t { KSL_PRIMAL = 0, KSL_DUAL = 1, KSL_STRANG = 2 };
 enum OpKind : int32_t { OP_ZERO = 0, OP_SYLVESTER = 1, OP_BURGERS = 2, OP_DATA = 3 };

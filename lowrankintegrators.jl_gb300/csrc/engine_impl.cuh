@@ -36,7 +36,7 @@ struct Inst {
   T* S;
   T* V;
   Side<T> k, l;
-  T* small;   // 15 blocks of W*W elements, each block 16-byte aligned
+  T* small;   // B_COUNT blocks of W*W elements, each block 16-byte aligned
   const T* Yp;
   const T* Yn;
   T* Ypw;     // writable previous snapshot
@@ -47,8 +47,11 @@ struct Inst {
 };
 
 // small-scratch block indices
+// (B_DM .. B_DPV: double-float matrices of the FP32 class, two blocks each)
 enum : int { B_GU = 0, B_GV = 2, B_M = 4, B_N = 5, B_ST = 6, B_SA = 7, B_SZ0 = 8, B_SZ1 = 9, B_SK = 10,
-             B_T1 = 11, B_T2 = 12, B_RK = 13, B_RL = 14, B_COUNT = 15 };
+             B_T1 = 11, B_T2 = 12, B_RK = 13, B_RL = 14, B_DM = 15, B_DN = 17, B_DPU = 19, B_DPV = 21,
+             B_COUNT = 23 };
+static_assert(B_COUNT == kSmallBlocks, "small-scratch layout and allocation disagree");
 
 // Projections of a basis X (N x w) needed by the Sylvester rhs:
 //   G = X^T X  (at dst, ld W),  P = X^T (T X)  (at dst + w*W, ld W).
@@ -360,6 +363,79 @@ __device__ void check_finite(const StepArgs<T>& g, const T* S, int r, int ld) {
   __syncthreads();
 }
 
+// S-step of the FP32 class in double-float (Sylvester flow, orthonormal
+// bases): S0 = M S N^T from the FP32 core and the double-float basis
+// changes, then the substeps of S' = P_U S + S P_V^T in Horner form (the
+// K/L substeps' form) on double-float P_U, P_V; the result is rounded into
+// the FP32 core.  Everything is staged in shared memory (5 r^2 double-float
+// values).  The FP32 step's rounding error is otherwise dominated by these
+// r x r reductions and the core update, not by the panel arithmetic.
+static __device__ __noinline__ void core_bug_acc(const Inst<float>& I, int r, const dfloat* Md, const dfloat* Nd,
+                                          const dfloat* PUd, const dfloat* PVd, const Scheme& sc, double dt,
+                                          Smem<float>& sm) {
+  const int W = I.W, rr = r * r;
+  dfloat* PUs = reinterpret_cast<dfloat*>(sm.stage);
+  dfloat* PVs = PUs + rr;
+  dfloat* Ss = PUs + 2 * rr;
+  dfloat* Wa = PUs + 3 * rr;
+  dfloat* Wb = PUs + 4 * rr;
+  for (int o = threadIdx.x; o < rr; o += NT) {
+    const int i = o % r, j = o / r;
+    PUs[o] = PUd[i + (int64_t)j * W];
+    PVs[o] = PVd[i + (int64_t)j * W];
+    Wb[o] = dfloat(I.S[i + (int64_t)j * I.rcap]);
+  }
+  __syncthreads();
+  // Wa = S N^T
+  for (int o = threadIdx.x; o < rr; o += NT) {
+    const int i = o % r, j = o / r;
+    dfloat acc(0.0f, 0.0f);
+    for (int k = 0; k < r; ++k) acc = fma_acc(Wb[i + k * r], Nd[j + (int64_t)k * W], acc);
+    Wa[o] = renorm(acc);
+  }
+  __syncthreads();
+  // Ss = M Wa
+  for (int o = threadIdx.x; o < rr; o += NT) {
+    const int i = o % r, j = o / r;
+    dfloat acc(0.0f, 0.0f);
+    for (int k = 0; k < r; ++k) acc = fma_acc(Md[i + (int64_t)k * W], Wa[k + j * r], acc);
+    Ss[o] = renorm(acc);
+  }
+  __syncthreads();
+  double gam[5];
+  horner_coeffs(sc, gam);
+  const int ns = sc.nstages;
+  const dfloat h(dt / sc.nsub);
+  for (int sub = 0; sub < sc.nsub; ++sub) {
+    // w = gam_ns S;  w <- gam_j S + h L(w) (j = ns-1 .. 0, gam_0 = 1)
+    const dfloat* win = Ss;
+    dfloat hw = h * dfloat(gam[ns]);
+    for (int j = ns - 1; j >= 0; --j) {
+      dfloat* wout = (win == Wa) ? Wb : Wa;
+      const dfloat gj = (j == 0) ? dfloat(1.0f, 0.0f) : dfloat(gam[j]);
+      for (int o = threadIdx.x; o < rr; o += NT) {
+        const int i = o % r, c = o / r;
+        dfloat l(0.0f, 0.0f);
+        for (int k = 0; k < r; ++k) {
+          l = fma_acc(PUs[i + k * r], win[k + c * r], l);
+          l = fma_acc(win[i + k * r], PVs[c + k * r], l);
+        }
+        wout[o] = fma(hw, renorm(l), gj * Ss[o]);
+      }
+      __syncthreads();
+      win = wout;
+      hw = h;
+    }
+    for (int o = threadIdx.x; o < rr; o += NT) Ss[o] = win[o];
+    __syncthreads();
+  }
+  for (int o = threadIdx.x; o < rr; o += NT) {
+    const int i = o % r, j = o / r;
+    I.S[i + (int64_t)j * I.rcap] = Ss[o].hi + Ss[o].lo;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // BUG (unconventional integrator) step
 // ---------------------------------------------------------------------------
@@ -378,6 +454,15 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   const bool fuse = sylv && AssumeOrthonormal<T>::value && 2 * r <= 128;
   T* PUn = I.blk(B_RK);
   T* PVn = I.blk(B_RL);
+  // FP32 class: the basis changes, the new projections and the S-step in
+  // double-float (their FP32 rounding errors dominate the FP32 step's)
+  bool acc = false;
+  if constexpr (sizeof(T) == 4) acc = fuse && ((r + 3) >> 2) * ((2 * r + 3) >> 2) <= NT &&
+                                      5 * r * r * 2 <= Stage<T>::ELEMS;
+  dfloat* DM = reinterpret_cast<dfloat*>(I.blk(B_DM));
+  dfloat* DN = reinterpret_cast<dfloat*>(I.blk(B_DN));
+  dfloat* DPU = reinterpret_cast<dfloat*>(I.blk(B_DPU));
+  dfloat* DPV = reinterpret_cast<dfloat*>(I.blk(B_DPV));
   if (sylv && g.proj_valid[I.inst] == 0) {
     projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
     projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
@@ -385,7 +470,16 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   // K step (unconventional.jl:136-142)
   k_step<T>(g, I, I.k, 0, I.U, I.S, I.rcap, false, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
   orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
-  if (fuse) {
+  bool done = false;
+  if constexpr (sizeof(T) == 4) {
+    if (acc) {
+      tile_gram_acc(n, r, 2 * r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r},
+                    RowLoadPanelStencil<T>{I.U, n, I.k.PQ, n, n, r, I.k.tri}, DM, DPU, nullptr, PUn, W, r);
+      done = true;
+    }
+  }
+  if (done) {
+  } else if (fuse) {
     // one pass over Q_K: [M | P_U(new)] = Q_K^T [U0 | A Q_K]
     tile_gram<T>(n, r, 2 * r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r},
                  RowLoadPanelStencil<T>{I.U, n, I.k.PQ, n, n, r, I.k.tri}, Mm, W, T(1), T(0), PUn, r);
@@ -395,7 +489,14 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   // L step (unconventional.jl:144-150), still with the old U
   k_step<T>(g, I, I.l, 1, I.V, I.S, I.rcap, true, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
   orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
-  if (fuse) {
+  if constexpr (sizeof(T) == 4) {
+    if (acc) {
+      tile_gram_acc(m, r, 2 * r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r},
+                    RowLoadPanelStencil<T>{I.V, m, I.l.PQ, m, m, r, I.l.tri}, DN, DPV, nullptr, PVn, W, r);
+    }
+  }
+  if (done) {
+  } else if (fuse) {
     tile_gram<T>(m, r, 2 * r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r},
                  RowLoadPanelStencil<T>{I.V, m, I.l.PQ, m, m, r, I.l.tri}, Nm, W, T(1), T(0), PVn, r);
   } else {
@@ -414,6 +515,13 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
     if (threadIdx.x == 0) g.proj_valid[I.inst] = 1;
   }
   // S step on the new bases (unconventional.jl:154-156): S0 = M S N^T
+  if constexpr (sizeof(T) == 4) {
+    if (acc) {
+      core_bug_acc(I, r, DM, DN, DPU, DPV, g.sS, g.dt, sm);
+      check_finite<T>(g, I.S, r, I.rcap);
+      return;
+    }
+  }
   small_gemm<T>(r, r, r, T(1), I.S, I.rcap, false, Nm, W, true, T(0), T1, W);
   small_gemm<T>(r, r, r, T(1), Mm, W, false, T1, W, false, T(0), St, W);
   substep_core<T>(g, I, St, r, r, T(1), GU, GV, I.U, I.V, g.sS, g.dt, sm);

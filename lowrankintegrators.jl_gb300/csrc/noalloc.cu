@@ -118,7 +118,7 @@ extern "C" lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, 
   d.offWL = al(n * (5 * r));
   d.offSmall = d.offWL + al(m * (5 * r));
   d.offY = 0;
-  const int64_t elems = d.offSmall + 15 * al(r * r);
+  const int64_t elems = d.offSmall + lri::kSmallBlocks * al(r * r);
   if (kHeaderBytes + es * (size_t)elems > kScratchBytes) return LRI_ERR_ARG;  // beyond the fixed scratch
   if (nsteps == 0) return LRI_OK;
 
