@@ -220,7 +220,7 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
     for (int j = ns - 1; j >= 0; --j) {
       T* wout = (j == 0) ? ((ns == 1) ? Zb[0] : Y) : Zb[(ns - 1 - j) & 1];
       const T gj = (j == 0) ? T(1) : T(gam[j]);
-      if (ortho) {
+      if constexpr (ortho) {
         tile_sylv<T>(N, r, win, sd.tri, P, I.W, wout, Y, gj, hw, sm.stage);
       } else {
         tile_gemm<T>(N, 2 * r, r, sm.stage, LoadStencilAug<T>{win, N, N, r, sd.tri}, LoadGP<T>{G, P, I.W, r},
