@@ -86,7 +86,10 @@ typedef enum { LRI_KSL_PRIMAL = 0, LRI_KSL_DUAL = 1, LRI_KSL_STRANG = 2 } lri_ks
  *               each stored as three vectors [sub | diag | sup] (sub[0] and
  *               sup[last] unused).  diag(theta) X terms fold into A's diagonal.
  *   BURGERS     F(X) = (Dxx X) diag(nu) + alpha (Dx X).*X + beta Dx(X.*X),
- *               periodic central differences of spacing h; nu per column.
+ *               periodic central differences of spacing h along the n rows
+ *               (h, alpha, beta in lri_batch_desc, shared by the batch);
+ *               nu per column (operator B, m values).  Evaluated tile by
+ *               tile on Y = K V^T without forming the n x m matrix.
  *   DATA        MatrixDataProblem: exact substep flows driven by the snapshot
  *               increment Δy = A(t+dt) - A(t) (data_integrator.jl:13-16). */
 typedef enum {

@@ -87,6 +87,34 @@ class SylvesterTridiagOperator:
         return np.concatenate(self.A), np.concatenate(self.B)
 
 
+class BurgersOperator:
+    """Periodic central-difference Burgers flow map, column j = sample j:
+
+        F(X, t) = (Dxx X) diag(nu) + alpha (Dx X) .* X + beta Dx(X .* X)
+
+    Dxx = tridiag(1, -2, 1) / h^2 and Dx = tridiag(-1, 0, 1) / (2h), both
+    periodic over the n grid points (rows).  The reference's smoke test
+    (test/data_agnostic_approximation.jl:16-33) is nu = 0.005 for every
+    column, alpha = -1, beta = 0; ``nu`` may also be one value per column.
+    """
+    kind = _native.LRI_OP_BURGERS_PERIODIC
+
+    def __init__(self, h: float, nu, alpha: float = -1.0, beta: float = 0.0):
+        self.h = float(h)
+        self.nu = np.asarray(nu, dtype=np.float64)
+        self.alpha = float(alpha)
+        self.beta = float(beta)
+
+    def params(self):
+        return (self.h, self.alpha, self.beta)
+
+    def packed_for(self, n: int, m: int):
+        nu = np.broadcast_to(self.nu, (m,)) if self.nu.ndim == 0 else self.nu
+        if nu.shape != (m,):
+            raise ValueError(f"nu has {nu.shape[0]} entries for {m} columns")
+        return np.zeros(0), np.array(nu, dtype=np.float64)
+
+
 @dataclass
 class MatrixDEProblem:
     """dX/dt = F(X, t) on tspan, X(t0) ~ u0 (src/primitives.jl:13-17)."""
@@ -263,7 +291,8 @@ class Batch:
     """
 
     def __init__(self, n: Sequence[int], m: Sequence[int], r: Sequence[int], alg, op_kind: int,
-                 precision: str = "fp64", r_cap: Optional[Sequence[int]] = None):
+                 precision: str = "fp64", r_cap: Optional[Sequence[int]] = None,
+                 op_params: Optional[Tuple[float, float, float]] = None):
         torch = _torch()
         self.torch = torch
         self.lib = _native.load()
@@ -291,6 +320,8 @@ class Batch:
         desc.m = self.m.ctypes.data_as(I64P)
         desc.r = self.r0.ctypes.data_as(I64P)
         desc.r_cap = self.rcap.ctypes.data_as(I64P)
+        if op_params is not None:  # Burgers (h, alpha, beta), shared by the batch
+            desc.burgers_h, desc.burgers_alpha, desc.burgers_beta = (float(x) for x in op_params)
         self._algd = _alg_desc(alg)
         self.handle = C.c_void_p()
         _native.check(self.lib.lri_batch_create(C.byref(self.handle), C.byref(desc), C.byref(self._algd)),
@@ -373,6 +404,12 @@ class Batch:
                 hA[self.offA[i]:self.offA[i] + len(a)] = a
                 hB[self.offB[i]:self.offB[i] + len(b)] = b
             self.opA.copy_(t.from_numpy(hA))
+            self.opB.copy_(t.from_numpy(hB))
+        if operators is not None and self.op_kind == _native.LRI_OP_BURGERS_PERIODIC:
+            hB = np.zeros(int(self.opB.numel()), self.np_dtype)
+            for i, op in enumerate(operators):
+                _, b = op.packed_for(int(self.n[i]), int(self.m[i]))
+                hB[self.offB[i]:self.offB[i] + len(b)] = b
             self.opB.copy_(t.from_numpy(hB))
         self.bind()
 
@@ -498,7 +535,20 @@ def _op_kind(prob) -> int:
         return _native.LRI_OP_ZERO
     if isinstance(f, SylvesterTridiagOperator):
         return _native.LRI_OP_SYLVESTER_TRIDIAG
+    if isinstance(f, BurgersOperator):
+        return _native.LRI_OP_BURGERS_PERIODIC
     raise LriError(2, "flow map is not one of the engine's operators (arbitrary closures are unsupported)")
+
+
+def _op_params(probs):
+    """Batch-wide Burgers parameters (h, alpha, beta), or None."""
+    fs = [p.f for p in probs if isinstance(p, MatrixDEProblem) and isinstance(p.f, BurgersOperator)]
+    if not fs:
+        return None
+    ps = {f.params() for f in fs}
+    if len(ps) != 1:
+        raise ValueError("Burgers instances of one batch must share h, alpha and beta")
+    return ps.pop()
 
 
 def _data_at(prob: MatrixDataProblem, t):
@@ -520,7 +570,7 @@ def init(prob, alg, dt, precision: str = "fp64") -> DLRIntegrator:
     rcap = r
     if isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
         rcap = max(r, min(alg.rmax, n // 2, m // 2))
-    b = Batch([n], [m], [r], alg, _op_kind(prob), precision, r_cap=[rcap])
+    b = Batch([n], [m], [r], alg, _op_kind(prob), precision, r_cap=[rcap], op_params=_op_params([prob]))
     b.upload([u0], [prob.f] if isinstance(prob, MatrixDEProblem) else None)
     if isinstance(prob, MatrixDataProblem):
         b.data_init([_data_at(prob, t0)])
@@ -615,6 +665,9 @@ class MixedEnsemble:
 
     def __init__(self, factors: Sequence[SVDLikeRepresentation], operators, alg, op_kind: int,
                  kappa_max: float = MIXED_KAPPA_MAX, r_cap=None):
+        op_params = None
+        if op_kind == _native.LRI_OP_BURGERS_PERIODIC:
+            op_params = _op_params([MatrixDEProblem(f, Y, (0.0, 1.0)) for f, Y in zip(operators, factors)])
         torch = _torch()
         self.torch = torch
         self.count = len(factors)
@@ -628,7 +681,7 @@ class MixedEnsemble:
             ops = None if operators is None else [operators[i] for i in sel]
             rc = None if r_cap is None else [r_cap[i] for i in sel]
             b = Batch([Y.U.shape[0] for Y in fs], [Y.V.shape[0] for Y in fs], [Y.S.shape[0] for Y in fs], alg,
-                      op_kind, prec, r_cap=rc)
+                      op_kind, prec, r_cap=rc, op_params=op_params)
             b.upload(fs, ops)
             self.parts.append((prec, sel, b, torch.cuda.Stream()))
 
@@ -692,7 +745,7 @@ def solve_ensemble(probs: Sequence[MatrixDEProblem], alg, dt, precision: str = "
     n = [p.u0.U.shape[0] for p in probs]
     m = [p.u0.V.shape[0] for p in probs]
     r = [p.u0.S.shape[0] for p in probs]
-    b = Batch(n, m, r, alg, kind, precision)
+    b = Batch(n, m, r, alg, kind, precision, op_params=_op_params(probs))
     b.upload([p.u0 for p in probs], [p.f for p in probs])
     b.step(tspan[0], dt, k)
     b.check_status()

@@ -193,7 +193,10 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   if (alg->kind == LRI_ALG_KSL && (alg->ksl_order < 0 || alg->ksl_order > 2)) return LRI_ERR_ARG;
   if (!scheme_ok(alg->K_alg) || !scheme_ok(alg->L_alg) || !scheme_ok(alg->S_alg)) return LRI_ERR_ARG;
   if (alg->kind == LRI_ALG_RA_BUG && (!(alg->tol >= 0.0) || alg->r_min < 1)) return LRI_ERR_ARG;
-  if (desc->op == LRI_OP_BURGERS_PERIODIC) return LRI_ERR_UNSUPPORTED;
+  if (desc->op == LRI_OP_BURGERS_PERIODIC &&
+      !(desc->burgers_h > 0.0 && std::isfinite(desc->burgers_h) && std::isfinite(desc->burgers_alpha) &&
+        std::isfinite(desc->burgers_beta)))
+    return LRI_ERR_ARG;
   // Strang needs the data at the half step: with one snapshot per step it is
   // not defined (the reference has no method for it either:
   // update_data! requires integer dt, data_integrator.jl:26).
@@ -247,6 +250,8 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
     if (desc->op == LRI_OP_SYLVESTER_TRIDIAG) {
       b->totA += 3 * n;
       b->totB += 3 * m;
+    } else if (desc->op == LRI_OP_BURGERS_PERIODIC) {
+      b->totB += m;  // per-column viscosity
     }
     // side workspaces: PY, PQ (N x W) + PA, PZ0, PZ1 (N x rcap); keep 16-byte alignment
     auto al = [](int64_t x) { return (x + 3) & ~int64_t(3); };

@@ -341,6 +341,185 @@ struct LoadDelta {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Periodic Burgers flow map contracted with low-rank factors (one CTA):
+//   Y = XL ZR^T (N x M: rows = grid points, columns = samples),
+//   F(Y) = (Dxx Y) diag(nu) + alpha (Dx Y).*Y + beta Dx(Y.*Y),
+//   Dxx = tridiag(1,-2,1)/h^2, Dx = tridiag(-1,0,1)/(2h), both periodic;
+//   BURG_K: out (N x k, ld ldo) = F ZR
+//   BURG_L: out (M x k, ld ldo) = F^T XL
+//   BURG_S: out (p x k, ld ldo) = sgn * CL^T F ZR      (CL: N x p, ld N)
+// XL: N x k (ld N), ZR: M x k (ld M), k, p <= 64.  Y and F exist only as
+// shared-memory tiles (row tiles with one periodic halo row on each side);
+// the reference evaluates F on the n x m matrix (unconventional.jl:51-79).
+// Ends with __syncthreads().
+// ---------------------------------------------------------------------------
+enum : int { BURG_K = 0, BURG_L = 1, BURG_S = 2 };
+
+template <typename T>
+__device__ __noinline__ void burgers_contract(int mode, int N, int M, int k, const T* XL, const T* ZR, const T* CL,
+                                              int p, const T* nu, double h, double alpha, double beta, T sgn, T* out,
+                                              int ldo, T* stage) {
+  const int tid = threadIdx.x;
+  const int ldk = k + 1, ldp = p + 1;
+  const int TCb = (mode == BURG_S) ? 16 : 32;
+  const int ldf = TCb + 1;
+  // rows per tile: 32 when the staging area holds it, else 16
+  auto need = [&](int tr) {
+    int e = (tr + 2) * ldk + TCb * ldk + (tr + 2) * TCb + tr * ldf + TCb;
+    if (mode == BURG_S) e += tr * ldp + tr * ldk;
+    return e;
+  };
+  const int TRb = (need(32) <= Stage<T>::ELEMS) ? 32 : 16;
+  T* xs = stage;                       // (TRb+2) x ldk: XL rows i0-1 .. i0+TRb (periodic)
+  T* zs = xs + (TRb + 2) * ldk;        // TCb x ldk: ZR rows j0 ..
+  T* ys = zs + TCb * ldk;              // (TRb+2) x TCb: Y tile
+  T* fs = ys + (TRb + 2) * TCb;        // TRb x ldf: F tile
+  T* nus = fs + TRb * ldf;             // TCb viscosities
+  T* cs = nus + TCb;                   // TRb x ldp: CL rows (BURG_S)
+  T* ts = cs + TRb * ldp;              // TRb x ldk: (F ZR) rows (BURG_S)
+  const T ih2 = T(1.0 / (h * h)), ihx = T(0.5 / h), al = T(alpha), be = T(beta);
+  constexpr int NACC = 8;  // accumulators per thread: TRb * k and TCb * k are <= 2048 = NACC * NT
+
+  auto stage_x = [&](int i0, int rows) {
+    for (int e = tid; e < (rows + 2) * k; e += NT) {
+      const int ii = e % (rows + 2), a = e / (rows + 2);
+      int g = i0 - 1 + ii;
+      g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
+      xs[ii * ldk + a] = XL[g + (int64_t)a * N];
+    }
+  };
+  auto stage_z = [&](int j0, int cols) {
+    for (int e = tid; e < TCb * k; e += NT) {
+      const int jj = e % TCb, a = e / TCb;
+      zs[jj * ldk + a] = (jj < cols) ? ZR[(j0 + jj) + (int64_t)a * M] : T(0);
+    }
+    for (int jj = tid; jj < TCb; jj += NT) nus[jj] = (jj < cols) ? nu[j0 + jj] : T(0);
+  };
+  // Y tile, then F tile (after the caller's barrier over the staged rows)
+  auto flow_tile = [&](int rows) {
+    for (int o = tid; o < (rows + 2) * TCb; o += NT) {
+      const int ii = o / TCb, jj = o - (o / TCb) * TCb;
+      T acc = T(0);
+      for (int a = 0; a < k; ++a) acc = fma_acc(xs[ii * ldk + a], zs[jj * ldk + a], acc);
+      ys[o] = renorm(acc);
+    }
+    __syncthreads();
+    for (int o = tid; o < rows * TCb; o += NT) {
+      const int ii = o / TCb, jj = o - (o / TCb) * TCb;
+      const T ym = ys[ii * TCb + jj], y0 = ys[(ii + 1) * TCb + jj], yp = ys[(ii + 2) * TCb + jj];
+      T f = nus[jj] * (((ym + yp) - (y0 + y0)) * ih2);
+      f = fma(al * ((yp - ym) * ihx), y0, f);
+      f = fma(be, (yp * yp - ym * ym) * ihx, f);
+      fs[ii * ldf + jj] = f;
+    }
+    __syncthreads();
+  };
+
+  if (mode == BURG_L) {
+    for (int j0 = 0; j0 < M; j0 += TCb) {
+      const int cols = min(TCb, M - j0);
+      T acc[NACC];
+#pragma unroll
+      for (int u = 0; u < NACC; ++u) acc[u] = T(0);
+      stage_z(j0, cols);
+      for (int i0 = 0; i0 < N; i0 += TRb) {
+        const int rows = min(TRb, N - i0);
+        stage_x(i0, rows);
+        __syncthreads();
+        flow_tile(rows);
+        // acc(jj, c) += sum_ii F(ii, jj) XL(i0+ii, c)
+#pragma unroll
+        for (int u = 0; u < NACC; ++u) {
+          const int o = tid + u * NT;
+          if (o < TCb * k) {
+            const int jj = o % TCb, c = o / TCb;
+            T sacc = acc[u];
+            for (int ii = 0; ii < rows; ++ii) sacc = fma_acc(fs[ii * ldf + jj], xs[(ii + 1) * ldk + c], sacc);
+            acc[u] = renorm(sacc);
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int u = 0; u < NACC; ++u) {
+        const int o = tid + u * NT;
+        if (o < TCb * k) {
+          const int jj = o % TCb, c = o / TCb;
+          if (jj < cols) out[(j0 + jj) + (int64_t)c * ldo] = acc[u];
+        }
+      }
+    }
+    __syncthreads();
+    return;
+  }
+
+  if (mode == BURG_S) {
+    for (int o = tid; o < p * k; o += NT) out[(o % p) + (int64_t)(o / p) * ldo] = T(0);
+  }
+  for (int i0 = 0; i0 < N; i0 += TRb) {
+    const int rows = min(TRb, N - i0);
+    T acc[NACC];
+#pragma unroll
+    for (int u = 0; u < NACC; ++u) acc[u] = T(0);
+    stage_x(i0, rows);
+    for (int j0 = 0; j0 < M; j0 += TCb) {
+      const int cols = min(TCb, M - j0);
+      stage_z(j0, cols);
+      __syncthreads();
+      flow_tile(rows);
+      // acc(i, c) += sum_jj F(i, jj) ZR(j0+jj, c)
+#pragma unroll
+      for (int u = 0; u < NACC; ++u) {
+        const int o = tid + u * NT;
+        if (o < TRb * k) {
+          const int i = o % TRb, c = o / TRb;
+          if (i < rows) {
+            T sacc = acc[u];
+            for (int jj = 0; jj < cols; ++jj) sacc = fma_acc(fs[i * ldf + jj], zs[jj * ldk + c], sacc);
+            acc[u] = renorm(sacc);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (mode == BURG_K) {
+#pragma unroll
+      for (int u = 0; u < NACC; ++u) {
+        const int o = tid + u * NT;
+        if (o < TRb * k) {
+          const int i = o % TRb, c = o / TRb;
+          if (i < rows) out[(i0 + i) + (int64_t)c * ldo] = acc[u];
+        }
+      }
+    } else {
+      // out += sgn * CL(rows)^T (F ZR)(rows)
+#pragma unroll
+      for (int u = 0; u < NACC; ++u) {
+        const int o = tid + u * NT;
+        if (o < TRb * k) {
+          const int i = o % TRb, c = o / TRb;
+          if (i < rows) ts[i * ldk + c] = acc[u];
+        }
+      }
+      for (int e = tid; e < rows * p; e += NT) {
+        const int ii = e % rows, a = e / rows;
+        cs[ii * ldp + a] = CL[(i0 + ii) + (int64_t)a * N];
+      }
+      __syncthreads();
+      for (int o = tid; o < p * k; o += NT) {
+        const int a = o % p, c = o / p;
+        T sacc = T(0);
+        for (int ii = 0; ii < rows; ++ii) sacc = fma_acc(cs[ii * ldp + a], ts[ii * ldk + c], sacc);
+        T* d = out + a + (int64_t)c * ldo;
+        *d = fma(sgn, renorm(sacc), *d);
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+}
+
 // One application of the orthonormal-basis Sylvester substep operator:
 //   out = g * y + h * (T z + z P^T)       (N x r, all column-major, ld N)
 // T tridiagonal [sub | dia | sup], P (r x r, ld ldp).  Each row tile of z is

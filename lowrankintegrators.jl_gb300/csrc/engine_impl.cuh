@@ -180,6 +180,52 @@ __device__ __noinline__ void orth_panel(const Inst<T>& I, T* Kp, int N, int W, T
   qr_panel<T>(Kp, N, W, Qdst, R, ldr, sm);
 }
 
+// Burgers K (side 0) or L (side 1) substep on the panel Y (N x r, ld N):
+// the scheme's stages one by one (the flow is nonlinear), each stage
+// derivative k_s = F(Z_s V^T) V (K) or F(U Z_s^T)^T U (L) formed by
+// burgers_contract into the free QR panel; Xo is the other side's basis.
+template <typename T>
+__device__ __noinline__ void burgers_panel_rk(const StepArgs<T>& g, const Inst<T>& I, const Side<T>& sd, int side,
+                                              T* Y, int r, const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
+  const int N = sd.N;
+  const T* nu = I.l.tri;  // operator B: per-column viscosities (m)
+  T* Kst = sd.PQ;
+  T* A = sd.PA;
+  T* Zb[2] = {sd.PZ0, sd.PZ1};
+  const int ns = sc.nstages;
+  const T h = T(dt / sc.nsub);
+  const int64_t NR = (int64_t)N * r;
+  for (int sub = 0; sub < sc.nsub; ++sub) {
+    for (int s = 0; s < ns; ++s) {
+      const T* Z = (s == 0) ? Y : Zb[(s - 1) & 1];
+      if (side == 0)
+        burgers_contract<T>(BURG_K, I.n, I.m, r, Z, Xo, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst, N,
+                            sm.stage);
+      else
+        burgers_contract<T>(BURG_L, I.n, I.m, r, Xo, Z, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst, N,
+                            sm.stage);
+      const T bs = T(sc.b[s]);
+      const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
+      T* Zout = Zb[s & 1];
+      for (int64_t o = threadIdx.x; o < NR; o += NT) {
+        const T kv = Kst[o];
+        if (ns == 1) {
+          Y[o] = fma(h * bs, kv, Y[o]);
+        } else if (s == 0) {
+          A[o] = bs * kv;
+          Zout[o] = fma(h * an, kv, Y[o]);
+        } else if (s + 1 < ns) {
+          A[o] = fma(bs, kv, A[o]);
+          Zout[o] = fma(h * an, kv, Y[o]);
+        } else {
+          Y[o] = fma(h, fma(bs, kv, A[o]), Y[o]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // One substep of side `sd` on the panel Y (N x r, ld N), in place.
 //   Sylvester: Y' = T Y G + Y P^T  with (G, P) the projections of the other
 //              side's basis (K: V^T V, V^T B V; L: U^T U, U^T A U).
@@ -190,6 +236,10 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
                              const T* Gp, const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
   const int N = sd.N;
   if (g.op == OP_ZERO) return;
+  if (g.op == OP_BURGERS) {
+    burgers_panel_rk<T>(g, I, sd, side, Y, r, Xo, sc, dt, sm);
+    return;
+  }
   if (g.op == OP_DATA) {
     const int a = (side == 0) ? I.m : I.n;
     const int ldo = (side == 0) ? I.m : I.n;
@@ -248,6 +298,44 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
     tile_gemm<T>(n, I.m, q, sm.stage, LoadDelta<T>{I.Yn, I.Yp, n, false}, LoadSmall<T>{Vb, I.m, false},
                  EpiStore<T>{Z, n});
     tile_gram<T>(n, p, q, sm.stage, RowLoadPanel<T>{Ub, n, p}, RowLoadPanel<T>{Z, n, q}, St, W, sign, T(1));
+    return;
+  }
+  if (g.op == OP_BURGERS) {
+    // k_s = sign * U^T F(U Z_s V^T) V with U Z_s formed in the free K-side
+    // QR panel (n x q), stages one by one
+    T* XLp = I.k.PY;
+    T* SAb = I.blk(B_SA);
+    T* SZb[2] = {I.blk(B_SZ0), I.blk(B_SZ1)};
+    T* SKb = I.blk(B_SK);
+    const int ns = sc.nstages;
+    const T h = T(dt / sc.nsub);
+    for (int sub = 0; sub < sc.nsub; ++sub) {
+      for (int s = 0; s < ns; ++s) {
+        const T* Z = (s == 0) ? St : SZb[(s - 1) & 1];
+        tile_gemm<T>(I.n, p, q, sm.stage, LoadPanel<T>{Ub, I.n}, LoadSmall<T>{Z, W, false}, EpiStore<T>{XLp, I.n});
+        burgers_contract<T>(BURG_S, I.n, I.m, q, XLp, Vb, Ub, p, I.l.tri, g.bh, g.balpha, g.bbeta, sign, SKb, W,
+                            sm.stage);
+        const T bs = T(sc.b[s]);
+        const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
+        T* Zout = SZb[s & 1];
+        for (int o = threadIdx.x; o < p * q; o += NT) {
+          const int64_t idx = (o % p) + (int64_t)(o / p) * W;
+          const T kv = SKb[idx];
+          if (ns == 1) {
+            St[idx] = fma(h * bs, kv, St[idx]);
+          } else if (s == 0) {
+            SAb[idx] = bs * kv;
+            Zout[idx] = fma(h * an, kv, St[idx]);
+          } else if (s + 1 < ns) {
+            SAb[idx] = fma(bs, kv, SAb[idx]);
+            Zout[idx] = fma(h * an, kv, St[idx]);
+          } else {
+            St[idx] = fma(h, fma(bs, kv, SAb[idx]), St[idx]);
+          }
+        }
+        __syncthreads();
+      }
+    }
     return;
   }
   const T* GU = GUp;
