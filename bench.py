@@ -42,6 +42,13 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
+# step of each class's step kernel, from one ncu capture of the 1024-instance
+# slice of this ensemble (655 FP32-class and 369 double-float-class
+# instances: 0.256 GB and 1.770 GB per launch); scaled by instance counts.
+TRAFFIC_PER_INSTANCE = {"fp32": 0.256e9 / 655, "df": 1.770e9 / 369}
+
+
 def algorithmic(shapes, nsub=NSUB, esize=4):
     """Per batched step: compulsory DRAM bytes (factors and operators read,
     factors written) and algorithmic flops of the implemented BUG step."""
@@ -429,7 +436,11 @@ def main():
         "plain_fp64": {"ms_per_step": fp64_ms, "steps_per_s": 1e3 / fp64_ms, "timed_steps": k64,
                        "speedup_mixed_over_fp64": (value / ws) / (1e3 / fp64_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": src,
+                     "traffic": TRAFFIC_PER_INSTANCE["fp32"] * n_fp32
+                                + TRAFFIC_PER_INSTANCE["df"] * (args.count - n_fp32),
+                     "traffic_source": "ncu dram bytes per instance-step of each class (1024-instance capture), "
+                                       "scaled by the instance counts",
+                     "peak_source": src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "compulsory bytes per batched step (factors and operators read, factors "
                              "written) / mixed step time; the kernels are CUDA-core bound: %.3g algorithmic "
