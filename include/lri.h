@@ -210,6 +210,25 @@ LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int
                                         const void* A, const void* B, double dt, int32_t nsteps,
                                         const lri_scheme* scheme, void* stream, int32_t* status_out);
 
+/* Discrete adjoint of one BUG step (no counterpart in the reference, which
+ * has no differentiation; the north-star's hand-written adjoint).  For an
+ * LRI_F64, LRI_ALG_BUG, LRI_OP_SYLVESTER_TRIDIAG batch at fixed rank
+ * (r = r_cap) whose operator A carries a diagonal shift theta
+ * (F = (A0 + diag theta) X + X B^T, A as bound):
+ *   U0, S0, V0      the step's input factors (device, packed like the bound
+ *                   U, S, V; e.g. saved before the step during a replay)
+ *   Ubar, Sbar, Vbar in: adjoints of the step's outputs; out: adjoints of
+ *                   its inputs (same packing)
+ *   theta_bar       device, sum_i n_i doubles (instance i at sum_{j<i} n_j):
+ *                   accumulates d loss / d theta
+ * Each instance recomputes its step in stage form (RK stage inputs, both
+ * QRs, basis changes, projections, S stages) and sweeps back through it;
+ * the thin-QR adjoint is (Q_bar + Q copyltu(-Q_bar^T Q)) R^{-T}.  Workspace
+ * is allocated on the first call.  Schemes with nstages * nsub > 16 and
+ * other batch kinds return LRI_ERR_UNSUPPORTED. */
+LRI_API lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const void* S0, const void* V0,
+                                          void* Ubar, void* Sbar, void* Vbar, void* theta_bar, void* stream);
+
 /* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
 

@@ -752,3 +752,87 @@ def solve_ensemble(probs: Sequence[MatrixDEProblem], alg, dt, precision: str = "
     out = b.download()
     b.close()
     return out
+
+
+# ---------------------------------------------------------------------------
+# Discrete adjoint of the BUG integrator (no counterpart in the reference)
+# ---------------------------------------------------------------------------
+
+def terminal_loss(Y: SVDLikeRepresentation, target):
+    """L = ||U S V^T - X_t||_F^2 and its gradient with respect to U, S, V;
+    ``target`` is an SVDLikeRepresentation (never formed as n x m) or a dense
+    array."""
+    U, S, V = Y.U, Y.S, Y.V
+    if isinstance(target, SVDLikeRepresentation):
+        Wt, Qt = target.U @ target.S, target.V       # X_t = Wt Qt^T
+    else:
+        Wt, Qt = np.asarray(target, dtype=np.float64), np.eye(V.shape[0])
+    VtV, UtU = V.T @ V, U.T @ U
+    QtV, WtU = Qt.T @ V, Wt.T @ U
+    loss = (np.trace(S.T @ UtU @ S @ VtV) - 2.0 * np.trace(S.T @ WtU.T @ QtV)
+            + np.sum((Wt.T @ Wt) * (Qt.T @ Qt)))
+    Ub = 2.0 * (U @ S @ VtV @ S.T - Wt @ QtV @ S.T)
+    Sb = 2.0 * (UtU @ S @ VtV - WtU.T @ QtV)
+    Vb = 2.0 * (V @ S.T @ UtU @ S - Qt @ WtU @ S)
+    return float(loss), Ub, Sb, Vb
+
+
+def bug_gradient(prob: MatrixDEProblem, alg: UnconventionalAlgorithm, dt: float, target,
+                 checkpoint_every: int = 20):
+    """Loss ||Y(T) - X_t||_F^2 of the BUG solution of ``prob`` (a
+    SylvesterTridiagOperator flow, FP64, fixed rank) and its gradient with
+    respect to the diagonal of the operator's A (i.e. theta of
+    A0 + diag(theta)) and the initial factors.
+
+    The forward run keeps the factors every ``checkpoint_every`` steps on the
+    device; the reverse sweep replays each segment once, keeping every
+    step's input factors, and runs lri_batch_adjoint_step back through it.
+    Returns (loss, theta_bar (n,), SVDLikeRepresentation(U0_bar, S0_bar, V0_bar)).
+    """
+    if not isinstance(alg, UnconventionalAlgorithm) or not isinstance(prob.f, SylvesterTridiagOperator):
+        raise LriError(2, "the adjoint covers BUG on the Sylvester tridiagonal flow")
+    torch = _torch()
+    u0 = prob.u0
+    n, m, r = u0.U.shape[0], u0.V.shape[0], u0.S.shape[0]
+    b = Batch([n], [m], [r], alg, _native.LRI_OP_SYLVESTER_TRIDIAG, "fp64")
+    try:
+        b.upload([u0], [prob.f])
+        t0 = prob.tspan[0]
+        k = n_steps(prob.tspan, dt)
+        c = max(1, int(checkpoint_every))
+        ckpts = []
+        done = 0
+        while done < k:
+            ckpts.append((b.U.clone(), b.S.clone(), b.V.clone()))
+            seg = min(c, k - done)
+            b.step(t0 + done * dt, dt, seg)
+            done += seg
+        b.check_status()
+        loss, Ub, Sb, Vb = terminal_loss(b.download()[0], target)
+        dev = b.device
+        col = lambda X: torch.from_numpy(np.asarray(X, dtype=np.float64).ravel(order="F")).to(dev)
+        Ubar, Sbar, Vbar = col(Ub), col(Sb), col(Vb)
+        thb = torch.zeros(n, dtype=torch.float64, device=dev)
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        stream = b._stream()
+        for ci in reversed(range(len(ckpts))):
+            k0 = ci * c
+            k1 = min(k, k0 + c)
+            for dst, src in zip((b.U, b.S, b.V), ckpts[ci]):
+                dst.copy_(src)
+            b.bind()  # the cached projections belong to the checkpoint's bases
+            inputs = []
+            for j in range(k0, k1):
+                inputs.append((b.U.clone(), b.S.clone(), b.V.clone()))
+                b.step(t0 + j * dt, dt, 1)
+            for (U0, S0, V0) in reversed(inputs):
+                _native.check(b.lib.lri_batch_adjoint_step(b.handle, float(dt), ptr(U0), ptr(S0), ptr(V0),
+                                                           ptr(Ubar), ptr(Sbar), ptr(Vbar), ptr(thb), stream),
+                              "lri_batch_adjoint_step")
+        b.check_status()
+        grads = SVDLikeRepresentation(Ubar.cpu().numpy().reshape((r, n)).T.copy(),
+                                      Sbar.cpu().numpy().reshape((r, r)).T.copy(),
+                                      Vbar.cpu().numpy().reshape((r, m)).T.copy())
+        return loss, thb.cpu().numpy(), grads
+    finally:
+        b.close()

@@ -78,4 +78,13 @@ cudaError_t convert_df_to_f64(const void* in, double* out, int64_t n, cudaStream
 template <typename T>
 size_t step_smem_bytes();
 
+// Discrete adjoint of the FP64 BUG step (adjoint.cu): workspace elements per
+// instance, the largest nstages * nsub it supports, and the launch.
+size_t adjoint_work_elems(int64_t n, int64_t m, int64_t r, int ns_k, int ns_l);
+int adjoint_max_stages();
+cudaError_t launch_adjoint_step(const InstDesc* inst, const int64_t* adj_off, const int64_t* th_off, int count,
+                                const double* U0, const double* S0, const double* V0, double* Ub, double* Sb,
+                                double* Vb, double* thb, const double* opA, const double* opB, double* work,
+                                const Scheme& sK, const Scheme& sL, const Scheme& sS, double dt, cudaStream_t st);
+
 }  // namespace lri
