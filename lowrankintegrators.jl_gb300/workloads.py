@@ -103,3 +103,21 @@ def data_rotation(seed: int = 0, N: int = 100):
         return expm(t * W1) @ (np.exp(t) * D) @ expm(t * W2)
 
     return Y
+
+
+def adjoint_2048(seed: int = 5, n: int = 2048, r: int = 32, rt: int = 40):
+    """The adjoint workload: F(X; theta) = A X + X A^T + diag(theta) X with A
+    the unscaled 1D Laplacian tridiag(1, -2, 1), n = m = 2048, theta with
+    variance 0.1, Y0 rank 32 (seeded orthonormal factors, spectrum
+    2^{-k/4}), target X_t seeded rank 40 with spectrum 2^{-k/4}.  Returns
+    (A0, theta, U, S, V, (P, d, Q)) with X_t = P diag(d) Q^T."""
+    g = np.random.default_rng(seed)
+    A0 = (np.ones(n), -2.0 * np.ones(n), np.ones(n))
+    theta = g.normal(0.0, np.sqrt(0.1), n)
+    U, _ = np.linalg.qr(g.standard_normal((n, r)))
+    V, _ = np.linalg.qr(g.standard_normal((n, r)))
+    S = np.diag(2.0 ** (-np.arange(1, r + 1) / 4.0))
+    P, _ = np.linalg.qr(g.standard_normal((n, rt)))
+    Q, _ = np.linalg.qr(g.standard_normal((n, rt)))
+    d = 2.0 ** (-np.arange(1, rt + 1) / 4.0)
+    return A0, theta, U, S, V, (P, d, Q)

@@ -10,10 +10,17 @@ checkpoints every 20 steps; 32 random directions, h = 1e-6, the directional
 derivatives must agree to 1e-4 relative.  The finite differences run as one
 batch of 64 perturbed problems.
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                "lowrankintegrators.jl_gb300"))
+import workloads  # noqa: E402
 
 
 def small_problem(seed=5, n=40, m=36, r=4, rt=6):
@@ -52,21 +59,8 @@ def test_adjoint_matches_cpu_adjoint(lri, oracle, scheme):
     assert rel(gr.V, Vb_c) <= 1e-9
 
 
-def cfg_adjoint(seed=5, n=2048, r=32, rt=40):
-    g = np.random.default_rng(seed)
-    A0 = (np.ones(n), -2.0 * np.ones(n), np.ones(n))
-    theta = g.normal(0.0, np.sqrt(0.1), n)
-    U, _ = np.linalg.qr(g.standard_normal((n, r)))
-    V, _ = np.linalg.qr(g.standard_normal((n, r)))
-    S = np.diag(2.0 ** (-np.arange(1, r + 1) / 4.0))
-    P, _ = np.linalg.qr(g.standard_normal((n, rt)))
-    Q, _ = np.linalg.qr(g.standard_normal((n, rt)))
-    d = 2.0 ** (-np.arange(1, rt + 1) / 4.0)
-    return A0, theta, U, S, V, (P, d, Q)
-
-
 def test_adjoint_workload_against_central_differences(lri):
-    A0, theta, U, S, V, (P, d, Q) = cfg_adjoint()
+    A0, theta, U, S, V, (P, d, Q) = workloads.adjoint_2048()
     n, r = U.shape
     dt, T = 1e-4, 0.02
     alg = lri.UnconventionalAlgorithm(lri.RK4(1))
