@@ -1680,6 +1680,13 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const T eps = T(Prec<T>::eps);
   for (int o = tid; o < P * P; o += NT) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
+  // Pairs whose columns are both below eps * ||B||_F are left alone: their
+  // directions are rounding noise, and rotating them could go on forever.
+  __shared__ __align__(16) unsigned char red_raw[NW * sizeof(T)];
+  T fro2 = T(0);
+  for (int o = tid; o < P * P; o += NT) fro2 = fma(a[o], a[o], fro2);
+  fro2 = block_sum(fro2, reinterpret_cast<T*>(red_raw));
+  const T tiny = eps * eps * fro2;
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
   bool converged = false;
   for (int sweep = 0; sweep < 40 && !converged; ++sweep) {
@@ -1700,7 +1707,8 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
           al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
         }
         al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
-        if (fabs(ga) > eps * sqrt(al * be) && ga != T(0)) {
+        // (sqrt(al) * sqrt(be): al * be can leave the FP32 exponent range)
+        if ((al > tiny || be > tiny) && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
           const T zeta = (be - al) / (T(2) * ga);
           // for large |zeta| use tan = 1/(2 zeta): zeta^2 would leave the FP32
           // exponent range of float and double-float values

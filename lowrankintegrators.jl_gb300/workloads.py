@@ -121,3 +121,47 @@ def adjoint_2048(seed: int = 5, n: int = 2048, r: int = 32, rt: int = 40):
     Q, _ = np.linalg.qr(g.standard_normal((n, rt)))
     d = 2.0 ** (-np.arange(1, rt + 1) / 4.0)
     return A0, theta, U, S, V, (P, d, Q)
+
+
+def data_stream(n: int, m: int, nsnap: int, seed: int = 2, K: int = 64, sub: int = 128, noise: float = 1e-4):
+    """Snapshots A(t_j), t_j = j / (nsnap - 1), of the compressed data stream
+    A(t) = sum_{k<=K} sigma_k(t) u_k(t) v_k(t)^T + noise * N(0, 1):
+    sigma_k(t) = e^{-k/8} (1 + 0.3 sin(2 pi f_k t)), f_k ~ U[0.5, 2];
+    u_k(t) = Q_u exp(t Omega_u) [I_K; 0] with Q_u an n x sub seeded orthonormal
+    basis and Omega_u a sub x sub skew matrix with N(0, 0.1) entries (the
+    same for v); the noise is one fixed realisation.  The full-size stream
+    is n = 8192, m = 4096, 500 snapshots."""
+    from scipy.linalg import expm
+
+    g = np.random.default_rng(seed)
+    f = g.uniform(0.5, 2.0, K)
+    Qu = random_orthonormal(g, n, sub)
+    Qv = random_orthonormal(g, m, sub)
+    Wu = g.normal(0.0, np.sqrt(0.1), (sub, sub))
+    Wv = g.normal(0.0, np.sqrt(0.1), (sub, sub))
+    Ou, Ov = np.triu(Wu, 1) - np.triu(Wu, 1).T, np.triu(Wv, 1) - np.triu(Wv, 1).T
+    E = noise * g.standard_normal((n, m))
+    k = np.arange(1, K + 1)
+    out = []
+    for j in range(nsnap):
+        t = j / max(1, nsnap - 1)
+        sig = np.exp(-k / 8.0) * (1.0 + 0.3 * np.sin(2 * np.pi * f * t))
+        Ut = Qu @ expm(t * Ou)[:, :K]
+        Vt = Qv @ expm(t * Ov)[:, :K]
+        out.append((Ut * sig) @ Vt.T + E)
+    return out
+
+
+def burgers_uq(n: int, m: int, seed: int = 3):
+    """The Burgers-UQ problem u_t + (u^2/2)_x = nu u_xx on the periodic grid
+    x_i = i/n (h = 1/n), one column per sample: nu_j ~ U[0.005, 0.02],
+    u0_j = sin(2 pi x) + a_j sin(4 pi x + phi_j), a_j ~ U[0, 0.5],
+    phi_j ~ U[0, 2 pi].  Returns (h, nu, X0) with X0 the n x m initial data
+    (exact rank 3).  The full-size problem is n = 4096, m = 16384."""
+    g = np.random.default_rng(seed)
+    x = np.arange(n) / n
+    nu = g.uniform(0.005, 0.02, m)
+    a = g.uniform(0.0, 0.5, m)
+    phi = g.uniform(0.0, 2 * np.pi, m)
+    X0 = np.sin(2 * np.pi * x)[:, None] + a[None, :] * np.sin(4 * np.pi * x[:, None] + phi[None, :])
+    return 1.0 / n, nu, X0
