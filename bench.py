@@ -183,6 +183,28 @@ def dist_setup():
     return ws, rank, local, pg
 
 
+def rank_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def rank_max(x: float, dist) -> float:
+    """Maximum of x over the ranks (the slowest rank's time)."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_value(ws: int, steps: int, seconds: float) -> float:
+    """Whole-job batched steps/s: every rank advances its own ensemble by
+    ``steps`` steps; the job takes the slowest rank's time."""
+    return ws * steps / seconds
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -301,15 +323,10 @@ def main():
     OPK = lri._native.LRI_OP_SYLVESTER_TRIDIAG
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        rank_barrier(dist)
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(x, dist)
 
     stream = torch.cuda.current_stream()
 
@@ -383,7 +400,7 @@ def main():
     # double-float batch for the rest, two streams)
     ms, ymix, launches, clocks = timed_run(lambda: lri.MixedEnsemble(factors, ops, alg, OPK), K, K, True)
     ms_max = max_over_ranks(ms)
-    value = ws * K / (ms_max * 1e-3)
+    value = weak_value(ws, K, ms_max * 1e-3)
     kap = np.array([lri.core_condition(Y.S) for Y in factors])
     n_fp32 = int((kap <= lri.MIXED_KAPPA_MAX).sum())
     # pure FP32 form and plain FP64 form, same steps
