@@ -229,6 +229,35 @@ LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int
 LRI_API lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const void* S0, const void* V0,
                                           void* Ubar, void* Sbar, void* Vbar, void* theta_bar, void* stream);
 
+/* ---- One large data stream on the whole GPU -------------------------------
+ * Rank-adaptive BUG for a MatrixDataProblem whose n x m snapshots are too
+ * large for the one-CTA-per-instance batch (the reference's
+ * rankadaptive_unconventional_step! with the data substeps,
+ * rank_adaptive_unconventional.jl:182-233, data_integrator.jl:13-16; the
+ * snapshot stream of primitives.jl:23-30).  Every kernel spreads over the
+ * whole GPU: three streaming passes over the snapshot pair per step (dY V,
+ * dY^T U, dY Vhat, with dY = A(t+dt) - A(t) formed in the loader), Gram
+ * reductions in FP64, single-CTA FP64 kernels for the r x r and 2r x 2r
+ * work.  Uhat = [U0 | orthonormal basis of (I - U0 U0^T) dY V0] spans the
+ * same space as the reference's orth([K1 | U0]).
+ *   dtype   LRI_F32 or LRI_F64 (snapshots and factors)
+ *   r0      initial rank, r_max <= 96 the buffers' width, tol the absolute
+ *           truncation tolerance, r_min >= 1 the lower bound
+ * The caller's U (n x r_max), S (r_max x r_max), V (m x r_max) hold Y0 with
+ * zeros beyond rank r0 and are updated in place; the rank stays on the
+ * device (lri_stream_rank reads it).  No counterpart handle in the reference
+ * (its DLRIntegrator, primitives.jl:54-63). */
+typedef struct lri_stream lri_stream;
+LRI_API lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0,
+                                     int64_t r_max, double tol, int32_t r_min);
+LRI_API lri_status lri_stream_destroy(lri_stream* s);
+LRI_API lri_status lri_stream_bind(lri_stream* s, void* U, void* S, void* V);
+/* One step from snapshot A_prev = A(t) to A_next = A(t+dt) (device, n x m,
+ * column-major, dtype of the stream). */
+LRI_API lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void* A_next, void* stream);
+LRI_API lri_status lri_stream_rank(lri_stream* s, int64_t* r_out, void* stream);
+LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
+
 /* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
 

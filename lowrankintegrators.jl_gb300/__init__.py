@@ -836,3 +836,114 @@ def bug_gradient(prob: MatrixDEProblem, alg: UnconventionalAlgorithm, dt: float,
         return loss, thb.cpu().numpy(), grads
     finally:
         b.close()
+
+
+# ---------------------------------------------------------------------------
+# One large data stream on the whole GPU (lri_stream_*)
+# ---------------------------------------------------------------------------
+
+class DataStreamEngine:
+    """Rank-adaptive BUG for one MatrixDataProblem too large for the
+    one-CTA-per-instance batch: multi-CTA streaming passes over each pair of
+    snapshots (see lri_stream_create).  Snapshots are device tensors holding
+    n x m column-major data (``to_device`` converts a host array)."""
+
+    def __init__(self, n: int, m: int, r0: int, rmax: int, tol: float, rmin: int = 1, precision: str = "fp32"):
+        torch = _torch()
+        self.torch = torch
+        self.lib = _native.load()
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.dtype = torch.float32 if precision == "fp32" else torch.float64
+        self.np_dtype = np.float32 if precision == "fp32" else np.float64
+        self.n, self.m, self.R = int(n), int(m), int(rmax)
+        self.handle = C.c_void_p()
+        code = _native.LRI_F32 if precision == "fp32" else _native.LRI_F64
+        _native.check(self.lib.lri_stream_create(C.byref(self.handle), code, self.n, self.m, int(r0), self.R,
+                                                 float(tol), int(rmin)), "lri_stream_create")
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        self.U = torch.zeros(self.n * self.R, dtype=self.dtype, device=dev)
+        self.S = torch.zeros(self.R * self.R, dtype=self.dtype, device=dev)
+        self.V = torch.zeros(self.m * self.R, dtype=self.dtype, device=dev)
+
+    def to_device(self, A: np.ndarray):
+        A = np.asarray(A)
+        if A.shape != (self.n, self.m):
+            raise ValueError(f"snapshot shape {A.shape} != {(self.n, self.m)}")
+        return self.torch.from_numpy(np.asarray(A, dtype=self.np_dtype).ravel(order="F")).to(self.device)
+
+    def bind(self, Y0: SVDLikeRepresentation):
+        r = Y0.S.shape[0]
+        u = np.zeros((self.n, self.R), self.np_dtype)
+        s = np.zeros((self.R, self.R), self.np_dtype)
+        v = np.zeros((self.m, self.R), self.np_dtype)
+        u[:, :r], s[:r, :r], v[:, :r] = Y0.U, Y0.S, Y0.V
+        for dst, x in ((self.U, u), (self.S, s), (self.V, v)):
+            dst.copy_(self.torch.from_numpy(x.ravel(order="F")))
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        _native.check(self.lib.lri_stream_bind(self.handle, ptr(self.U), ptr(self.S), ptr(self.V)), "lri_stream_bind")
+
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def step(self, A_prev, A_next):
+        _native.check(self.lib.lri_stream_step(self.handle, C.c_void_p(A_prev.data_ptr()),
+                                               C.c_void_p(A_next.data_ptr()), self._stream()), "lri_stream_step")
+
+    def rank(self) -> int:
+        r = C.c_int64(0)
+        _native.check(self.lib.lri_stream_rank(self.handle, C.byref(r), self._stream()), "lri_stream_rank")
+        return int(r.value)
+
+    def check_status(self):
+        _native.check(self.lib.lri_stream_status(self.handle, self._stream()), "stream status")
+
+    def download(self) -> SVDLikeRepresentation:
+        r = self.rank()
+        U = self.U.cpu().numpy().astype(np.float64).reshape((self.R, self.n)).T[:, :r].copy()
+        S = self.S.cpu().numpy().astype(np.float64).reshape((self.R, self.R)).T[:r, :r].copy()
+        V = self.V.cpu().numpy().astype(np.float64).reshape((self.R, self.m)).T[:, :r].copy()
+        return SVDLikeRepresentation(U, S, V)
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.lri_stream_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_stream(prob: MatrixDataProblem, alg: RankAdaptiveUnconventionalAlgorithm, precision: str = "fp32",
+                 save_everystep: bool = True) -> DLRSolution:
+    """solve(prob, alg) (src/primitives.jl:68-80) for a MatrixDataProblem given
+    as a list of snapshots, on the large-stream engine: rank-adaptive BUG,
+    one step per consecutive pair of snapshots."""
+    if callable(prob.y):
+        raise ValueError("the stream engine takes a list of snapshots")
+    u0 = prob.u0
+    n, m = u0.U.shape[0], u0.V.shape[0]
+    eng = DataStreamEngine(n, m, u0.S.shape[0], min(alg.rmax, 96), alg.tol, alg.rmin, precision)
+    try:
+        eng.bind(u0)
+        sol = DLRSolution([u0.copy()], [float(prob.tspan[0])])
+        prev = eng.to_device(prob.y[0])
+        for k in range(1, len(prob.y)):
+            nxt = eng.to_device(prob.y[k])
+            eng.step(prev, nxt)
+            prev = nxt
+            if save_everystep:
+                eng.check_status()
+                sol.Y.append(eng.download())
+                sol.t.append(float(prob.tspan[0] + k))
+        eng.check_status()
+        if not save_everystep:
+            sol.Y.append(eng.download())
+            sol.t.append(float(prob.tspan[0] + len(prob.y) - 1))
+        return sol
+    finally:
+        eng.close()

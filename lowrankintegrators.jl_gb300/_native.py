@@ -30,6 +30,8 @@ EXPORTED = [
     "lri_batch_layout", "lri_batch_bind", "lri_batch_data_layout", "lri_batch_data_init", "lri_batch_step",
     "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step", "lri_bug_step_noalloc",
     "lri_batch_prepare", "lri_batch_adjoint_step",
+    "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
+    "lri_stream_status",
 ]
 
 
@@ -88,6 +90,19 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_batch_status.argtypes = [P, P]
     lib.lri_batch_launches_per_step.restype = C.c_int32
     lib.lri_batch_launches_per_step.argtypes = [P]
+    lib.lri_stream_create.restype = C.c_int
+    lib.lri_stream_create.argtypes = [C.POINTER(P), C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                      C.c_double, C.c_int32]
+    lib.lri_stream_destroy.restype = C.c_int
+    lib.lri_stream_destroy.argtypes = [P]
+    lib.lri_stream_bind.restype = C.c_int
+    lib.lri_stream_bind.argtypes = [P, P, P, P]
+    lib.lri_stream_step.restype = C.c_int
+    lib.lri_stream_step.argtypes = [P, P, P, P]
+    lib.lri_stream_rank.restype = C.c_int
+    lib.lri_stream_rank.argtypes = [P, C.POINTER(C.c_int64), P]
+    lib.lri_stream_status.restype = C.c_int
+    lib.lri_stream_status.argtypes = [P, P]
     lib.lri_batch_adjoint_step.restype = C.c_int
     lib.lri_batch_adjoint_step.argtypes = [P, C.c_double, P, P, P, P, P, P, P, P]
     lib.lri_batch_prepare.restype = C.c_int

@@ -1,0 +1,646 @@
+// stream.cu - rank-adaptive BUG for one large data stream (MatrixDataProblem
+// whose snapshots are too large for the one-CTA instance engine), spread
+// over the whole GPU.
+//
+// One step A(t) -> A(t+1) (src/integrators/rank_adaptive_unconventional.jl:
+// 182-233 with the data substeps of data_integrator.jl:13-16):
+//   K1 = U0 S0 + dY V0,  L1 = V0 S0^T + dY^T U0          dY = A(t+1) - A(t)
+//   Uhat = orth[K1 | U0], Vhat = orth[L1 | V0]
+//   S~ = (Uhat^T U0) S0 (Vhat^T V0)^T + Uhat^T dY Vhat
+//   S~ = P Sigma Q^T, r1 = truncation, U1 = Uhat P1, V1 = Vhat Q1, S1 = Sigma1.
+// span[K1 | U0] = span[U0 | (I - U0 U0^T) dY V0], so Uhat is formed as
+// [U0 | Q] with Q an orthonormal basis of the part of dY V0 orthogonal to U0
+// (two classical Gram-Schmidt passes, then two eigenvalue-based
+// orthonormalisations X <- X D W Lambda^{-1/2}; directions with eigenvalues
+// below the rounding level become zero columns).  The step's result depends
+// only on span(Uhat), span(Vhat) as long as [K1 | U0] has full column rank.
+//
+// Kernels: three streaming passes over the snapshot pair (dY V0, dY^T U0,
+// dY Vhat; dY is formed in the loader and never stored), tall-skinny Gram
+// products X^T Y reduced in FP64 through per-block partials, row-parallel
+// panel products X B, and single-CTA FP64 kernels for the r x r / 2r x 2r
+// work.  Panel widths are fixed at r_max (Uhat, Vhat: 2 r_max) with zero
+// columns beyond the current rank, which stays on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/lri.h"
+#include "engine.cuh"
+
+namespace lri {
+namespace {
+
+constexpr int SMAX = 96;      // largest r_max
+constexpr int GROWS = 512;    // rows per Gram partial block
+
+// ---------------------------------------------------------------------------
+// Streaming pass A: out (n x c) = dY B,  dY = A1 - A0 (n x m, col-major),
+// B (m x c, ld ldb), c <= 2*SMAX.  CTA = 32 rows, loops over all columns.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pass_rows(int n, int m, int c, const T* __restrict__ A1,
+                                                 const T* __restrict__ A0, const T* __restrict__ B, int ldb,
+                                                 T* __restrict__ out) {
+  // 4 rows x CG columns per thread (c <= 192); BJ keeps the static shared
+  // memory under 48 KB for both types
+  constexpr int BI = 32, BJ = sizeof(T) == 8 ? 16 : 32, CG = 6;
+  __shared__ T ds[BJ][BI + 1];             // dY tile, column-major
+  __shared__ T bs[BJ][2 * SMAX + 1];       // B rows of the tile
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * BI;
+  const int rg = tid & 7, cg = tid >> 3;   // rows 4rg.., columns cg + 32u
+  T acc[4][CG];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int u = 0; u < CG; ++u) acc[p][u] = T(0);
+  for (int j0 = 0; j0 < m; j0 += BJ) {
+    for (int e = tid; e < BI * BJ; e += 256) {
+      const int ii = e % BI, jj = e / BI;
+      const int i = i0 + ii, j = j0 + jj;
+      T v = T(0);
+      if (i < n && j < m) {
+        const int64_t o = (int64_t)i + (int64_t)j * n;
+        v = A1[o] - A0[o];
+      }
+      ds[jj][ii] = v;
+    }
+    for (int e = tid; e < BJ * c; e += 256) {
+      const int jj = e % BJ, k = e / BJ;
+      const int j = j0 + jj;
+      bs[jj][k] = (j < m) ? B[j + (int64_t)k * ldb] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < BJ; ++jj) {
+      T x[4], w[CG];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) x[p] = ds[jj][4 * rg + p];
+#pragma unroll
+      for (int u = 0; u < CG; ++u) w[u] = (cg + 32 * u < c) ? bs[jj][cg + 32 * u] : T(0);
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int u = 0; u < CG; ++u) acc[p][u] = fma(x[p], w[u], acc[p][u]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int i = i0 + 4 * rg + p;
+    if (i >= n) continue;
+#pragma unroll
+    for (int u = 0; u < CG; ++u) {
+      const int k = cg + 32 * u;
+      if (k < c) out[i + (int64_t)k * n] = acc[p][u];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Streaming pass B: out (m x c) = dY^T X, X (n x c, ld ldx), c <= SMAX.
+// CTA = 16 columns of dY, loops over all rows.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pass_cols(int n, int m, int c, const T* __restrict__ A1,
+                                                 const T* __restrict__ A0, const T* __restrict__ X, int ldx,
+                                                 T* __restrict__ out) {
+  constexpr int BJ = 16, BI = sizeof(T) == 8 ? 32 : 64;
+  __shared__ T ds[BJ][BI + 1];
+  __shared__ T xs[BI][SMAX + 1];
+  const int tid = threadIdx.x;
+  const int j0 = blockIdx.x * BJ;
+  const int jg = tid & 3, cg = tid >> 2;   // columns 4jg.., outputs cg + 64u
+  T acc[4][2];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) acc[p][0] = acc[p][1] = T(0);
+  for (int i0 = 0; i0 < n; i0 += BI) {
+    for (int e = tid; e < BI * BJ; e += 256) {
+      const int ii = e % BI, jj = e / BI;
+      const int i = i0 + ii, j = j0 + jj;
+      T v = T(0);
+      if (i < n && j < m) {
+        const int64_t o = (int64_t)i + (int64_t)j * n;
+        v = A1[o] - A0[o];
+      }
+      ds[jj][ii] = v;
+    }
+    for (int e = tid; e < BI * c; e += 256) {
+      const int ii = e % BI, k = e / BI;
+      const int i = i0 + ii;
+      xs[ii][k] = (i < n) ? X[i + (int64_t)k * ldx] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < BI; ++ii) {
+      T x[4], w[2];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) x[p] = ds[4 * jg + p][ii];
+      w[0] = (cg < c) ? xs[ii][cg] : T(0);
+      w[1] = (cg + 64 < c) ? xs[ii][cg + 64] : T(0);
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        acc[p][0] = fma(x[p], w[0], acc[p][0]);
+        acc[p][1] = fma(x[p], w[1], acc[p][1]);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int j = j0 + 4 * jg + p;
+    if (j >= m) continue;
+    if (cg < c) out[j + (int64_t)cg * m] = acc[p][0];
+    if (cg + 64 < c) out[j + (int64_t)(cg + 64) * m] = acc[p][1];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gram partials: part[blk] (a x c, FP64, ld a) = X(rows of blk)^T Y(rows),
+// X (N x a, ld ldx), Y (N x c, ld ldy); a, c <= 2*SMAX.  Grid
+// (row blocks of GROWS) x (64 x 64 output tiles).  Then gram_reduce.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* __restrict__ X, int ldx,
+                                                 const T* __restrict__ Y, int ldy, double* __restrict__ part) {
+  constexpr int TI = 32;
+  __shared__ double xs[TI][65];
+  __shared__ double ys[TI][65];
+  const int tid = threadIdx.x;
+  const int blk = blockIdx.x;
+  const int ta = blockIdx.y % ((a + 63) / 64), tc = blockIdx.y / ((a + 63) / 64);
+  const int a0 = ta * 64, c0 = tc * 64;
+  const int r0 = blk * GROWS, r1 = min(N, r0 + GROWS);
+  const int pa = tid & 15, pc = tid >> 4;  // 4 x 4 outputs: a0 + 4pa.., c0 + 4pc..
+  double acc[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = 0.0;
+  for (int i0 = r0; i0 < r1; i0 += TI) {
+    for (int e = tid; e < TI * 64; e += 256) {
+      const int ii = e % TI, k = e / TI;
+      const int i = i0 + ii;
+      const bool ok = i < r1;
+      xs[ii][k] = (ok && a0 + k < a) ? (double)X[i + (int64_t)(a0 + k) * ldx] : 0.0;
+      ys[ii][k] = (ok && c0 + k < c) ? (double)Y[i + (int64_t)(c0 + k) * ldy] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < TI; ++ii) {
+      double xv[4], yv[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) xv[p] = xs[ii][4 * pa + p];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) yv[q] = ys[ii][4 * pc + q];
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], yv[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+  double* dst = part + (int64_t)blk * a * c;
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int ia = a0 + 4 * pa + p, jc = c0 + 4 * pc + q;
+      if (ia < a && jc < c) dst[ia + (int64_t)jc * a] = acc[p][q];
+    }
+}
+
+// out (a x c, ld ldo) = alpha * sum_blk part[blk] + beta * out
+__global__ void gram_reduce(int nblk, int a, int c, const double* __restrict__ part, double alpha, double beta,
+                            double* __restrict__ out, int ldo) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= a * c) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * a * c + o];
+  const int i = o % a, j = o / a;
+  double* d = out + i + (int64_t)j * ldo;
+  *d = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *d);
+}
+
+// ---------------------------------------------------------------------------
+// Panel product: out (N x c, ld ldo) = X (N x a, ld ldx) B (a x c, FP64,
+// ld ldb) + beta * out.  Grid (row blocks of 32) x (column tiles of 64);
+// a <= 2*SMAX.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) panel_mul(int N, int a, int c, const T* __restrict__ X, int ldx,
+                                                 const double* __restrict__ B, int ldb, T beta, T* __restrict__ out,
+                                                 int ldo) {
+  constexpr int KC2 = 32;
+  __shared__ T xs[32][KC2 + 1];
+  __shared__ T bs[KC2][65];
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+  const int ri = tid & 15, cj = tid >> 4;  // rows ri, ri+16; columns cj + 16q
+  T acc[2][4];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+  for (int k0 = 0; k0 < a; k0 += KC2) {
+    const int kc = min(KC2, a - k0);
+    for (int e = tid; e < 32 * KC2; e += 256) {
+      const int ii = e % 32, k = e / 32;
+      const int i = i0 + ii;
+      xs[ii][k] = (i < N && k < kc) ? X[i + (int64_t)(k0 + k) * ldx] : T(0);
+    }
+    for (int e = tid; e < KC2 * 64; e += 256) {
+      const int k = e % KC2, cc = e / KC2;
+      bs[k][cc] = (k < kc && c0 + cc < c) ? T(B[(k0 + k) + (int64_t)(c0 + cc) * ldb]) : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < KC2; ++k) {
+      const T x0 = xs[ri][k], x1 = xs[ri + 16][k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const T w = bs[k][cj + 16 * q];
+        acc[0][q] = fma(x0, w, acc[0][q]);
+        acc[1][q] = fma(x1, w, acc[1][q]);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int i = i0 + ri + 16 * p;
+    if (i >= N) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = c0 + cj + 16 * q;
+      if (j >= c) continue;
+      T* d = out + i + (int64_t)j * ldo;
+      *d = (beta == T(0)) ? acc[p][q] : fma(beta, *d, acc[p][q]);
+    }
+  }
+}
+
+__global__ void negate(int k, double* x) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < k) x[o] = -x[o];
+}
+
+template <typename T>
+__global__ void copy_cols(int N, int c, const T* __restrict__ X, int ldx, T* __restrict__ Y, int ldy) {
+  const int64_t total = (int64_t)N * c;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = o % N, j = o / N;
+    Y[i + j * ldy] = X[i + j * ldx];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Single-CTA FP64 kernels (dynamic shared memory).
+// ---------------------------------------------------------------------------
+
+// Eigenvalue-based orthonormalisation factor of a Gram matrix G (a x a, ld a):
+// Bout (a x a, ld a) = D W Lambda^{-1/2} with D = diag(G)^{-1/2} and
+// D G D = W Lambda W^T, so X Bout has orthonormal columns; eigenvalues below
+// tol_rel * max eigenvalue (and zero diagonal entries) give zero columns.
+__global__ void svqb_factor(int a, const double* __restrict__ G, double tol_rel, double* __restrict__ Bout) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* M = reinterpret_cast<double*>(smraw);  // a x a
+  double* W = M + a * a;                          // a x a
+  double* lam = W + a * a;                        // a
+  double* d = lam + a;                            // a
+  int* perm = reinterpret_cast<int*>(d + a);
+  int* flag = perm + a + 1;
+  const int tid = threadIdx.x;
+  for (int j = tid; j < a; j += NT) {
+    const double g = G[j + (int64_t)j * a];
+    d[j] = (g > 0.0) ? 1.0 / sqrt(g) : 0.0;
+  }
+  __syncthreads();
+  for (int o = tid; o < a * a; o += NT) {
+    const int i = o % a, j = o / a;
+    M[o] = d[i] * G[o] * d[j];
+  }
+  __syncthreads();
+  // symmetric PSD: the one-sided Jacobi SVD gives eigenvectors (v) and eigenvalues (sigma)
+  jacobi_svd<double>(a, M, W, lam, perm, flag);
+  double lmax = 0.0;
+  for (int j = 0; j < a; ++j) lmax = fmax(lmax, lam[j]);
+  for (int o = tid; o < a * a; o += NT) {
+    const int i = o % a, j = o / a;
+    const double l = lam[j];
+    Bout[o] = (l > tol_rel * lmax && l > 0.0) ? d[i] * W[i + j * a] / sqrt(l) : 0.0;
+  }
+}
+
+// S-step core and truncation.  In: Mh = Uhat^T U0 (w x R), Nh = Vhat^T V0
+// (w x R), D = Uhat^T dY Vhat (w x w), S0 (R x R, T), rank r (device).
+// Out: P1, Q1 (w x R FP64: the kept left / right singular vectors, zero
+// beyond the new rank), S (R x R, diag), rank.  Scratch (w*w*2 doubles) in
+// global memory (the 2R x 2R SVD does not fit in shared memory).
+template <typename T>
+__global__ void core_step(int R, const double* __restrict__ Mh, const double* __restrict__ Nh,
+                          const double* __restrict__ D, T* S0, int32_t* rank, double tol, int rmin,
+                          double* __restrict__ scr, double* __restrict__ P1, double* __restrict__ Q1,
+                          uint32_t* status) {
+  __shared__ double sig[2 * SMAX];
+  __shared__ int perm[2 * SMAX + 1];
+  __shared__ int flag;
+  __shared__ int r_new;
+  const int tid = threadIdx.x;
+  const int w = 2 * R;
+  double* a = scr;          // w x w
+  double* v = scr + w * w;  // w x w
+  // T1 = S0 N^T (R x w) into v; a = M T1 + D
+  for (int o = tid; o < R * w; o += NT) {
+    const int i = o % R, j = o / R;
+    double s = 0.0;
+    for (int k = 0; k < R; ++k) s = fma((double)S0[i + (int64_t)k * R], Nh[j + (int64_t)k * w], s);
+    v[i + (int64_t)j * R] = s;
+  }
+  __syncthreads();
+  for (int o = tid; o < w * w; o += NT) {
+    const int i = o % w, j = o / w;
+    double s = D[o];
+    for (int k = 0; k < R; ++k) s = fma(Mh[i + (int64_t)k * w], v[k + (int64_t)j * R], s);
+    a[o] = s;
+  }
+  __syncthreads();
+  const bool ok = jacobi_svd<double>(w, a, v, sig, perm, &flag);
+  if (tid == 0) {
+    if (!ok) atomicOr(status, ST_SVD_NOCONV);
+    // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R]
+    const double tol2 = tol * tol;
+    double acc = 0.0;
+    int rr = w;
+    while (acc < tol2 && rr > 0) {
+      const double s = sig[perm[rr - 1]];
+      acc += s * s;
+      --rr;
+    }
+    int r1 = rr + 1;
+    if (r1 > R) r1 = R;
+    if (r1 < rmin) r1 = rmin;
+    if (r1 > w) r1 = w;
+    r_new = r1;
+    *rank = r1;
+  }
+  __syncthreads();
+  const int r1 = r_new;
+  for (int o = tid; o < w * R; o += NT) {
+    const int i = o % w, j = o / w;
+    double pv = 0.0, qv = 0.0;
+    if (j < r1) {
+      const int pj = perm[j];
+      const double sg = sig[pj];
+      pv = (sg > 0.0) ? a[i + (int64_t)pj * w] / sg : 0.0;
+      qv = v[i + (int64_t)pj * w];
+    }
+    P1[o] = pv;
+    Q1[o] = qv;
+  }
+  for (int o = tid; o < R * R; o += NT) {
+    const int i = o % R, j = o / R;
+    S0[o] = (i == j && i < r1) ? T(sig[perm[i]]) : T(0);
+  }
+  __syncthreads();
+  bool bad = false;
+  for (int o = tid; o < R * R; o += NT) bad |= !isfinite((double)S0[o]);
+  if (__syncthreads_or(bad) && tid == 0) atomicOr(status, ST_NONFINITE);
+}
+
+}  // namespace
+}  // namespace lri
+
+using namespace lri;
+
+struct lri_stream {
+  int32_t dtype;
+  int64_t n, m, R;
+  double tol;
+  int32_t rmin;
+  size_t es;
+  void* U = nullptr;
+  void* S = nullptr;
+  void* V = nullptr;
+  bool bound = false;
+  // device workspace
+  int32_t* d_rank = nullptr;
+  uint32_t* d_status = nullptr;
+  void* Uh = nullptr;   // n x 2R: [U0 | Q]
+  void* Vh = nullptr;   // m x 2R
+  void* Xk = nullptr;   // n x R (dY V0, then its orthonormalised part)
+  void* Xl = nullptr;   // m x R
+  void* Zp = nullptr;   // max(n, m) x 2R (dY Vhat; scratch of the orthonormalisation)
+  double* part = nullptr;
+  double* small = nullptr;
+};
+
+namespace {
+
+constexpr int kBlocksSmall = 16;  // FP64 scratch of (2R)^2 each
+
+template <typename T>
+struct StreamOps {
+  lri_stream* s;
+  cudaStream_t st;
+  double* blk(int i) const { return s->small + (int64_t)i * 4 * s->R * s->R; }
+  T* tp(void* p) const { return static_cast<T*>(p); }
+
+  cudaError_t gram(int N, int a, int c, const T* X, int ldx, const T* Y, int ldy, double alpha, double beta,
+                   double* out, int ldo) const {
+    const int nblk = (N + GROWS - 1) / GROWS;
+    dim3 grid(nblk, ((a + 63) / 64) * ((c + 63) / 64));
+    gram_part<T><<<grid, 256, 0, st>>>(N, a, c, X, ldx, Y, ldy, s->part);
+    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(nblk, a, c, s->part, alpha, beta, out, ldo);
+    return cudaGetLastError();
+  }
+  cudaError_t mul(int N, int a, int c, const T* X, int ldx, const double* B, int ldb, T beta, T* out,
+                  int ldo) const {
+    dim3 grid((N + 31) / 32, (c + 63) / 64);
+    panel_mul<T><<<grid, 256, 0, st>>>(N, a, c, X, ldx, B, ldb, beta, out, ldo);
+    return cudaGetLastError();
+  }
+  cudaError_t svqb(int a, const double* G, double* B) const {
+    const size_t smem = (size_t)(2 * a * a + 2 * a) * sizeof(double) + (size_t)(a + 2) * sizeof(int);
+    static bool attr_set = false;
+    if (!attr_set) {
+      const size_t mx = (size_t)(2 * SMAX * SMAX + 2 * SMAX) * sizeof(double) + (SMAX + 2) * sizeof(int);
+      cudaError_t e = cudaFuncSetAttribute(svqb_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    // eigenvalues below (64 u^2) of the largest are rounding noise of the panel
+    const double tol_rel = sizeof(T) == 4 ? 1e-12 : 1e-28;
+    svqb_factor<<<1, NT, smem, st>>>(a, G, tol_rel, B);
+    return cudaGetLastError();
+  }
+  // X (N x R) <- orthonormal basis of the part of X orthogonal to the
+  // orthonormal columns of Y0 (N x R); B blocks i0..i0+2 are scratch.
+  cudaError_t orth_against(int N, T* X, const T* Y0) const {
+    const int R = (int)s->R;
+    cudaError_t e = cudaSuccess;
+    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+      e = gram(N, R, R, Y0, N, X, N, 1.0, 0.0, blk(0), R);                                // C = Y0^T X
+      if (e == cudaSuccess) {
+        // X <- X - Y0 C   (panel_mul computes Y0 (-C) + X)
+        negate<<<(R * R + 255) / 256, 256, 0, st>>>(R * R, blk(0));
+        e = mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
+      }
+    }
+    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+      e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);                                 // G = X^T X
+      if (e == cudaSuccess) e = svqb(R, blk(1), blk(2));
+      if (e == cudaSuccess) e = mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);        // Z = X B
+      if (e == cudaSuccess) {
+        copy_cols<T><<<304, 256, 0, st>>>(N, R, tp(s->Zp), N, X, N);
+        e = cudaGetLastError();
+      }
+    }
+    return e;
+  }
+
+  cudaError_t step(const T* A0, const T* A1) const {
+    const int n = (int)s->n, m = (int)s->m, R = (int)s->R, w = 2 * R;
+    T* U = tp(s->U);
+    T* V = tp(s->V);
+    T* S = tp(s->S);
+    T* Uh = tp(s->Uh);
+    T* Vh = tp(s->Vh);
+    T* Xk = tp(s->Xk);
+    T* Xl = tp(s->Xl);
+    cudaError_t e = cudaSuccess;
+    // data passes 1 and 2: dY V0, dY^T U0
+    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, A1, A0, V, m, Xk);
+    pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, A1, A0, U, n, Xl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // Uhat = [U0 | orth((I - U0 U0^T) dY V0)], Vhat likewise
+    if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
+    if ((e = orth_against(m, Xl, V)) != cudaSuccess) return e;
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, U, n, Uh, n);
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, Xk, n, Uh + (int64_t)R * n, n);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, V, m, Vh, m);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, Vh + (int64_t)R * m, m);
+    // Mh = Uhat^T U0, Nh = Vhat^T V0 (w x R)
+    if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
+    if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
+    // data pass 3: Z = dY Vhat; D = Uhat^T Z
+    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, w, A1, A0, Vh, m, tp(s->Zp));
+    if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
+    core_step<T><<<1, NT, 0, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, blk(6), blk(8),
+                                   blk(9), s->d_status);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // U1 = Uhat P1, V1 = Vhat Q1
+    if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
+    return mul(m, w, R, Vh, m, blk(9), w, T(0), V, m);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0, int64_t r_max,
+                             double tol, int32_t r_min) {
+  if (!out) return LRI_ERR_ARG;
+  *out = nullptr;
+  if (dtype != LRI_F32 && dtype != LRI_F64) return LRI_ERR_UNSUPPORTED;
+  if (r_max < 1 || r_max > SMAX || r0 < 1 || r0 > r_max || r_min < 1 || r_min > r_max) return LRI_ERR_ARG;
+  if (n < 2 * r_max || m < 2 * r_max || n >= (1LL << 31) / 4 || m >= (1LL << 31) / 4) return LRI_ERR_ARG;
+  if (!(tol >= 0.0)) return LRI_ERR_ARG;
+  lri_stream* s = new lri_stream();
+  s->dtype = dtype;
+  s->n = n;
+  s->m = m;
+  s->R = r_max;
+  s->tol = tol;
+  s->rmin = r_min;
+  s->es = dtype == LRI_F32 ? 4 : 8;
+  const int64_t R = r_max;
+  const int64_t nblk = (std::max(n, m) + GROWS - 1) / GROWS;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes < 16 ? 16 : bytes);
+  };
+  alloc((void**)&s->d_rank, sizeof(int32_t));
+  alloc((void**)&s->d_status, sizeof(uint32_t));
+  alloc(&s->Uh, s->es * n * 2 * R);
+  alloc(&s->Vh, s->es * m * 2 * R);
+  alloc(&s->Xk, s->es * n * R);
+  alloc(&s->Xl, s->es * m * R);
+  alloc(&s->Zp, s->es * std::max(n, m) * 2 * R);
+  alloc((void**)&s->part, sizeof(double) * nblk * 4 * R * R);
+  alloc((void**)&s->small, sizeof(double) * kBlocksSmall * 4 * R * R);
+  const int32_t r32 = (int32_t)r0;
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_rank, &r32, sizeof(r32), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    lri_stream_destroy(s);
+    return LRI_ERR_CUDA;
+  }
+  *out = s;
+  return LRI_OK;
+}
+
+lri_status lri_stream_destroy(lri_stream* s) {
+  if (!s) return LRI_ERR_ARG;
+  cudaFree(s->d_rank);
+  cudaFree(s->d_status);
+  cudaFree(s->Uh);
+  cudaFree(s->Vh);
+  cudaFree(s->Xk);
+  cudaFree(s->Xl);
+  cudaFree(s->Zp);
+  cudaFree(s->part);
+  cudaFree(s->small);
+  delete s;
+  return LRI_OK;
+}
+
+lri_status lri_stream_bind(lri_stream* s, void* U, void* S, void* V) {
+  if (!s || !U || !S || !V) return LRI_ERR_ARG;
+  s->U = U;
+  s->S = S;
+  s->V = V;
+  s->bound = true;
+  return LRI_OK;
+}
+
+lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void* A_next, void* stream) {
+  if (!s || !A_prev || !A_next) return LRI_ERR_ARG;
+  if (!s->bound) return LRI_ERR_STATE;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (s->dtype == LRI_F32)
+    e = StreamOps<float>{s, st}.step(static_cast<const float*>(A_prev), static_cast<const float*>(A_next));
+  else
+    e = StreamOps<double>{s, st}.step(static_cast<const double*>(A_prev), static_cast<const double*>(A_next));
+  return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
+}
+
+lri_status lri_stream_rank(lri_stream* s, int64_t* r_out, void* stream) {
+  if (!s || !r_out) return LRI_ERR_ARG;
+  int32_t r = 0;
+  if (cudaMemcpyAsync(&r, s->d_rank, sizeof(r), cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess ||
+      cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    return LRI_ERR_CUDA;
+  *r_out = r;
+  return LRI_OK;
+}
+
+lri_status lri_stream_status(lri_stream* s, void* stream) {
+  if (!s) return LRI_ERR_ARG;
+  uint32_t w = 0;
+  if (cudaMemcpyAsync(&w, s->d_status, sizeof(w), cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess ||
+      cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    return LRI_ERR_CUDA;
+  if (w) cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), (cudaStream_t)stream);
+  if (w & ST_NONFINITE) return LRI_ERR_NONFINITE;
+  if (w & ST_SVD_NOCONV) return LRI_ERR_BREAKDOWN;
+  return w ? LRI_ERR_ARG : LRI_OK;
+}
+
+}  // extern "C"

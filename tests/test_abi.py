@@ -91,6 +91,12 @@ def test_create_rejects_bad_scheme_and_unsupported(lri):
     assert lib.lri_batch_create(None, C.byref(d), C.byref(a)) == 1
     assert lib.lri_batch_step(None, 0.0, 0.1, 1, None, None) == 1
     assert lib.lri_batch_prepare(None, 0.1, 5) == 1
+    # the large-stream engine: r_max above 96, double-float, too few rows
+    hs = C.c_void_p()
+    assert lib.lri_stream_create(C.byref(hs), native.LRI_F32, 8192, 4096, 16, 97, 1e-6, 1) == 1
+    assert lib.lri_stream_create(C.byref(hs), native.LRI_DF, 8192, 4096, 16, 96, 1e-6, 1) == 2
+    assert lib.lri_stream_create(C.byref(hs), native.LRI_F32, 100, 4096, 16, 64, 1e-6, 1) == 1
+    assert lib.lri_stream_step(None, None, None, None) == 1
     assert lib.lri_batch_destroy(None) == 1
 
 
