@@ -1675,25 +1675,37 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 // v's columns = right singular vectors, both permuted to the sorted order
 // through perm[].  Returns false if it did not converge.
 // ---------------------------------------------------------------------------
-template <typename T>
+// NTH: threads of the calling block (a multiple of 32); the instance engine
+// calls it with its NT threads, the single-CTA kernels of the large-stream
+// engine with 1024.
+template <typename T, int NTH = NT>
 __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag) {
+  constexpr int NWJ = NTH / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const T eps = T(Prec<T>::eps);
-  for (int o = tid; o < P * P; o += NT) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
+  // rotation threshold: P ulps (the rounding level of a length-P dot
+  // product), so a sweep whose remaining products are rounding noise ends
+  const T eps = T(Prec<T>::eps * P);
+  for (int o = tid; o < P * P; o += NTH) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
   // Pairs whose columns are both below eps * ||B||_F are left alone: their
   // directions are rounding noise, and rotating them could go on forever.
-  __shared__ __align__(16) unsigned char red_raw[NW * sizeof(T)];
+  __shared__ __align__(16) unsigned char red_raw[NWJ * sizeof(T)];
+  T* red = reinterpret_cast<T*>(red_raw);
   T fro2 = T(0);
-  for (int o = tid; o < P * P; o += NT) fro2 = fma(a[o], a[o], fro2);
-  fro2 = block_sum(fro2, reinterpret_cast<T*>(red_raw));
-  const T tiny = eps * eps * fro2;
+  for (int o = tid; o < P * P; o += NTH) fro2 = fma(a[o], a[o], fro2);
+  fro2 = warp_sum(fro2);
+  if (lane == 0) red[warp] = fro2;
+  __syncthreads();
+  fro2 = T(0);
+  for (int wv = 0; wv < NWJ; ++wv) fro2 += red[wv];
+  __syncthreads();
+  const T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
   bool converged = false;
   for (int sweep = 0; sweep < 40 && !converged; ++sweep) {
     if (tid == 0) *flag = 0;
     __syncthreads();
     for (int rnd = 0; rnd < Pe - 1; ++rnd) {
-      for (int pr = warp; pr < Pe / 2; pr += NW) {
+      for (int pr = warp; pr < Pe / 2; pr += NWJ) {
         int p, q;
         if (pr == 0) { p = rnd % (Pe - 1); q = Pe - 1; }
         else { p = (rnd + pr) % (Pe - 1); q = (rnd - pr + (Pe - 1)) % (Pe - 1); }
@@ -1737,7 +1749,7 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
     __syncthreads();
   }
   // singular values = column norms
-  for (int j = warp; j < P; j += NW) {
+  for (int j = warp; j < P; j += NWJ) {
     T s = T(0);
     for (int i = lane; i < P; i += 32) s = fma(a[j * P + i], a[j * P + i], s);
     s = warp_sum(s);

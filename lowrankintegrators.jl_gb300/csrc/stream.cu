@@ -164,35 +164,45 @@ __global__ void __launch_bounds__(256) pass_cols(int n, int m, int c, const T* _
 // X (N x a, ld ldx), Y (N x c, ld ldy); a, c <= 2*SMAX.  Grid
 // (row blocks of GROWS) x (64 x 64 output tiles).  Then gram_reduce.
 // ---------------------------------------------------------------------------
+// FP32 panels: exact products, double-float sums (the FP64 pipe of GB300
+// runs at 1/64 of the FP32 rate); FP64 panels: FP64.
+template <typename T> struct GramAcc { using type = double; };
+template <> struct GramAcc<float> { using type = dfloat; };
+__device__ __forceinline__ double gacc_mul(double acc, double x, double y) { return fma(x, y, acc); }
+__device__ __forceinline__ dfloat gacc_mul(dfloat acc, float x, float y) { return acc_mul_acc(acc, x, y); }
+__device__ __forceinline__ double gacc_val(double a) { return a; }
+__device__ __forceinline__ double gacc_val(dfloat a) { return (double)a.hi + (double)a.lo; }
+
 template <typename T>
 __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* __restrict__ X, int ldx,
                                                  const T* __restrict__ Y, int ldy, double* __restrict__ part) {
+  using A = typename GramAcc<T>::type;
   constexpr int TI = 32;
-  __shared__ double xs[TI][65];
-  __shared__ double ys[TI][65];
+  __shared__ T xs[TI][65];
+  __shared__ T ys[TI][65];
   const int tid = threadIdx.x;
   const int blk = blockIdx.x;
   const int ta = blockIdx.y % ((a + 63) / 64), tc = blockIdx.y / ((a + 63) / 64);
   const int a0 = ta * 64, c0 = tc * 64;
   const int r0 = blk * GROWS, r1 = min(N, r0 + GROWS);
   const int pa = tid & 15, pc = tid >> 4;  // 4 x 4 outputs: a0 + 4pa.., c0 + 4pc..
-  double acc[4][4];
+  A acc[4][4];
 #pragma unroll
   for (int p = 0; p < 4; ++p)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) acc[p][q] = 0.0;
+    for (int q = 0; q < 4; ++q) acc[p][q] = A(0.0);
   for (int i0 = r0; i0 < r1; i0 += TI) {
     for (int e = tid; e < TI * 64; e += 256) {
       const int ii = e % TI, k = e / TI;
       const int i = i0 + ii;
       const bool ok = i < r1;
-      xs[ii][k] = (ok && a0 + k < a) ? (double)X[i + (int64_t)(a0 + k) * ldx] : 0.0;
-      ys[ii][k] = (ok && c0 + k < c) ? (double)Y[i + (int64_t)(c0 + k) * ldy] : 0.0;
+      xs[ii][k] = (ok && a0 + k < a) ? X[i + (int64_t)(a0 + k) * ldx] : T(0);
+      ys[ii][k] = (ok && c0 + k < c) ? Y[i + (int64_t)(c0 + k) * ldy] : T(0);
     }
     __syncthreads();
 #pragma unroll 4
     for (int ii = 0; ii < TI; ++ii) {
-      double xv[4], yv[4];
+      T xv[4], yv[4];
 #pragma unroll
       for (int p = 0; p < 4; ++p) xv[p] = xs[ii][4 * pa + p];
 #pragma unroll
@@ -200,8 +210,12 @@ __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* _
 #pragma unroll
       for (int p = 0; p < 4; ++p)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[p][q] = fma(xv[p], yv[q], acc[p][q]);
+        for (int q = 0; q < 4; ++q) acc[p][q] = gacc_mul(acc[p][q], xv[p], yv[q]);
     }
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = renorm(acc[p][q]);
     __syncthreads();
   }
   double* dst = part + (int64_t)blk * a * c;
@@ -210,7 +224,7 @@ __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* _
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int ia = a0 + 4 * pa + p, jc = c0 + 4 * pc + q;
-      if (ia < a && jc < c) dst[ia + (int64_t)jc * a] = acc[p][q];
+      if (ia < a && jc < c) dst[ia + (int64_t)jc * a] = gacc_val(acc[p][q]);
     }
 }
 
@@ -302,113 +316,189 @@ __global__ void copy_cols(int N, int c, const T* __restrict__ X, int ldx, T* __r
 // Single-CTA FP64 kernels (dynamic shared memory).
 // ---------------------------------------------------------------------------
 
-// Eigenvalue-based orthonormalisation factor of a Gram matrix G (a x a, ld a):
-// Bout (a x a, ld a) = D W Lambda^{-1/2} with D = diag(G)^{-1/2} and
-// D G D = W Lambda W^T, so X Bout has orthonormal columns; eigenvalues below
-// tol_rel * max eigenvalue (and zero diagonal entries) give zero columns.
-__global__ void svqb_factor(int a, const double* __restrict__ G, double tol_rel, double* __restrict__ Bout) {
+// Small-matrix arithmetic of the single-CTA kernels: double-float for FP32
+// panels (the FP64 pipe of GB300 runs at 1/64 of the FP32 rate), FP64 for
+// FP64 panels.
+template <typename T> struct SmallT { using type = double; };
+template <> struct SmallT<float> { using type = dfloat; };
+__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ double to_d(dfloat x) { return (double)x; }
+
+constexpr int NTS = 1024;  // threads of the single-CTA kernels
+
+// Eigenvalue-based orthonormalisation factor of a Gram matrix G (a x a, ld a)
+// restricted to its leading r x r block (r = *rank: the panel's columns
+// beyond the rank are zero): Bout (a x a, ld a, zero outside that block) =
+// D W Lambda^{-1/2} with D = diag(G)^{-1/2} and D G D = W Lambda W^T, so
+// X Bout has orthonormal columns; eigenvalues below tol_rel * max
+// eigenvalue (and zero diagonal entries) give zero columns.
+template <typename ST>
+__global__ void __launch_bounds__(NTS) svqb_factor(int a, const double* __restrict__ G, const int32_t* rank,
+                                                   double tol_rel, double* __restrict__ Bout) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* M = reinterpret_cast<double*>(smraw);  // a x a
-  double* W = M + a * a;                          // a x a
-  double* lam = W + a * a;                        // a
-  double* d = lam + a;                            // a
-  int* perm = reinterpret_cast<int*>(d + a);
-  int* flag = perm + a + 1;
+  const int r = min(a, (int)*rank);
+  ST* M = reinterpret_cast<ST*>(smraw);  // r x r
+  ST* W = M + r * r;                      // r x r
+  ST* lam = W + r * r;                    // r
+  double* d = reinterpret_cast<double*>(lam + r);
+  int* perm = reinterpret_cast<int*>(d + r);
+  int* flag = perm + r + 1;
   const int tid = threadIdx.x;
-  for (int j = tid; j < a; j += NT) {
+  for (int j = tid; j < r; j += NTS) {
     const double g = G[j + (int64_t)j * a];
     d[j] = (g > 0.0) ? 1.0 / sqrt(g) : 0.0;
   }
   __syncthreads();
-  for (int o = tid; o < a * a; o += NT) {
-    const int i = o % a, j = o / a;
-    M[o] = d[i] * G[o] * d[j];
+  for (int o = tid; o < r * r; o += NTS) {
+    const int i = o % r, j = o / r;
+    M[o] = ST(d[i] * G[i + (int64_t)j * a] * d[j]);
   }
   __syncthreads();
   // symmetric PSD: the one-sided Jacobi SVD gives eigenvectors (v) and eigenvalues (sigma)
-  jacobi_svd<double>(a, M, W, lam, perm, flag);
+  jacobi_svd<ST, NTS>(r, M, W, lam, perm, flag);
   double lmax = 0.0;
-  for (int j = 0; j < a; ++j) lmax = fmax(lmax, lam[j]);
-  for (int o = tid; o < a * a; o += NT) {
+  for (int j = 0; j < r; ++j) lmax = fmax(lmax, to_d(lam[j]));
+  for (int o = tid; o < a * a; o += NTS) {
     const int i = o % a, j = o / a;
-    const double l = lam[j];
-    Bout[o] = (l > tol_rel * lmax && l > 0.0) ? d[i] * W[i + j * a] / sqrt(l) : 0.0;
+    double bv = 0.0;
+    if (i < r && j < r) {
+      const double l = to_d(lam[j]);
+      bv = (l > tol_rel * lmax && l > 0.0) ? d[i] * to_d(W[i + j * r]) / sqrt(l) : 0.0;
+    }
+    Bout[o] = bv;
   }
 }
 
+// One CholeskyQR factor: G = R^T R (a x a, ld a), Bout = R^{-1}; columns with
+// G_jj <= tol_rel * max G_jj are decoupled (R_jj = 1, zero off-diagonal), so
+// zero columns of the panel stay zero.  R and R^{-1} in shared memory.
+template <typename ST>
+__global__ void __launch_bounds__(NTS) chol_inv_factor(int a, const double* __restrict__ G, double tol_rel,
+                                                       double* __restrict__ Bout) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  ST* R = reinterpret_cast<ST*>(smraw);  // a x a
+  ST* Ri = R + a * a;                     // a x a
+  __shared__ int keep[2 * SMAX];
+  const int tid = threadIdx.x;
+  double gmax = 0.0;
+  for (int j = 0; j < a; ++j) gmax = fmax(gmax, G[j + (int64_t)j * a]);
+  for (int j = tid; j < a; j += NTS) keep[j] = G[j + (int64_t)j * a] > tol_rel * gmax;
+  __syncthreads();
+  for (int o = tid; o < a * a; o += NTS) {
+    const int i = o % a, j = o / a;
+    const bool kk = keep[i] && keep[j];
+    R[o] = kk ? ST(G[o]) : ST((i == j) ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  // right-looking Cholesky, upper factor in R (two barriers per column)
+  for (int k = 0; k < a; ++k) {
+    ST dk = R[k + k * a];
+    if (!(to_d(dk) > 0.0)) dk = ST(1.0);
+    const ST rkk = sqrt(dk);
+    const ST inv = ST(1.0) / rkk;
+    for (int j = k + 1 + tid; j < a; j += NTS) R[k + j * a] = R[k + j * a] * inv;
+    __syncthreads();
+    if (tid == 0) R[k + k * a] = rkk;
+    const int cnt = a - k - 1;
+    for (int e = tid; e < cnt * cnt; e += NTS) {
+      const int i = k + 1 + e % cnt, j = k + 1 + e / cnt;
+      if (i <= j) R[i + j * a] = R[i + j * a] - R[k + i * a] * R[k + j * a];
+    }
+    __syncthreads();
+  }
+  // R^{-1} row by row from the bottom: row i needs rows i+1.. (one barrier per row)
+  for (int o = tid; o < a * a; o += NTS) Ri[o] = ST(0.0);
+  __syncthreads();
+  for (int i = a - 1; i >= 0; --i) {
+    const ST rii = ST(1.0) / R[i + i * a];
+    for (int j = i + tid; j < a; j += NTS) {
+      ST sacc = (i == j) ? ST(1.0) : ST(0.0);
+      for (int k = i + 1; k <= j; ++k) sacc = sacc - R[i + k * a] * Ri[k + j * a];
+      Ri[i + j * a] = sacc * rii;
+    }
+    __syncthreads();
+  }
+  for (int o = tid; o < a * a; o += NTS) Bout[o] = to_d(Ri[o]);
+}
+
 // S-step core and truncation.  In: Mh = Uhat^T U0 (w x R), Nh = Vhat^T V0
-// (w x R), D = Uhat^T dY Vhat (w x w), S0 (R x R, T), rank r (device).
-// Out: P1, Q1 (w x R FP64: the kept left / right singular vectors, zero
-// beyond the new rank), S (R x R, diag), rank.  Scratch (w*w*2 doubles) in
-// global memory (the 2R x 2R SVD does not fit in shared memory).
-template <typename T>
-__global__ void core_step(int R, const double* __restrict__ Mh, const double* __restrict__ Nh,
-                          const double* __restrict__ D, T* S0, int32_t* rank, double tol, int rmin,
-                          double* __restrict__ scr, double* __restrict__ P1, double* __restrict__ Q1,
-                          uint32_t* status) {
-  __shared__ double sig[2 * SMAX];
+// (w x R), D = Uhat^T dY Vhat (w x w), S0 (R x R, T), rank (device).  Out:
+// P1, Q1 (w x R FP64: the kept left / right singular vectors, zero beyond
+// the new rank), S (R x R, diag), rank.  The SVD runs in ST (double-float
+// for FP32 panels: an FP32 Jacobi SVD of a w x w matrix accumulates
+// O(w u) rotation error per sweep) with the w x w matrix in shared memory
+// when it fits, else in the global scratch ag; the right vectors in vg.
+template <typename T, typename ST>
+__global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict__ Mh, const double* __restrict__ Nh,
+                                                 const double* __restrict__ D, T* S0, int32_t* rank, double tol,
+                                                 int rmin, ST* __restrict__ ag, ST* __restrict__ vg,
+                                                 double* __restrict__ P1, double* __restrict__ Q1, uint32_t* status,
+                                                 int a_in_smem) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(16) unsigned char sig_raw[2 * SMAX * sizeof(ST)];
+  ST* sig = reinterpret_cast<ST*>(sig_raw);
   __shared__ int perm[2 * SMAX + 1];
   __shared__ int flag;
   __shared__ int r_new;
   const int tid = threadIdx.x;
   const int w = 2 * R;
-  double* a = scr;          // w x w
-  double* v = scr + w * w;  // w x w
-  // T1 = S0 N^T (R x w) into v; a = M T1 + D
-  for (int o = tid; o < R * w; o += NT) {
-    const int i = o % R, j = o / R;
-    double s = 0.0;
-    for (int k = 0; k < R; ++k) s = fma((double)S0[i + (int64_t)k * R], Nh[j + (int64_t)k * w], s);
-    v[i + (int64_t)j * R] = s;
+  // active rows / columns: the first r of each half of [U0 | Q] ([V0 | Q])
+  const int r = min(R, (int)*rank), wa = 2 * r;
+  auto idx = [&](int i) { return (i < r) ? i : R + (i - r); };
+  ST* a = a_in_smem ? reinterpret_cast<ST*>(smraw) : ag;  // wa x wa
+  ST* v = vg;                                              // wa x wa
+  // T1 = S0 N^T (r x wa) into v; a = M T1 + D on the active block (FP64 products)
+  for (int o = tid; o < r * wa; o += NTS) {
+    const int i = o % r, j = o / r;
+    double sacc = 0.0;
+    for (int k = 0; k < r; ++k) sacc = fma((double)S0[i + (int64_t)k * R], Nh[idx(j) + (int64_t)k * w], sacc);
+    v[i + (int64_t)j * r] = ST(sacc);
   }
   __syncthreads();
-  for (int o = tid; o < w * w; o += NT) {
-    const int i = o % w, j = o / w;
-    double s = D[o];
-    for (int k = 0; k < R; ++k) s = fma(Mh[i + (int64_t)k * w], v[k + (int64_t)j * R], s);
-    a[o] = s;
+  for (int o = tid; o < wa * wa; o += NTS) {
+    const int i = o % wa, j = o / wa;
+    double sacc = D[idx(i) + (int64_t)idx(j) * w];
+    for (int k = 0; k < r; ++k) sacc = fma(Mh[idx(i) + (int64_t)k * w], to_d(v[k + (int64_t)j * r]), sacc);
+    a[o] = ST(sacc);
   }
   __syncthreads();
-  const bool ok = jacobi_svd<double>(w, a, v, sig, perm, &flag);
+  const bool ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag);
   if (tid == 0) {
     if (!ok) atomicOr(status, ST_SVD_NOCONV);
     // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R]
     const double tol2 = tol * tol;
     double acc = 0.0;
-    int rr = w;
+    int rr = wa;
     while (acc < tol2 && rr > 0) {
-      const double s = sig[perm[rr - 1]];
-      acc += s * s;
+      const double sv = to_d(sig[perm[rr - 1]]);
+      acc += sv * sv;
       --rr;
     }
     int r1 = rr + 1;
     if (r1 > R) r1 = R;
     if (r1 < rmin) r1 = rmin;
-    if (r1 > w) r1 = w;
+    if (r1 > wa) r1 = wa;
     r_new = r1;
     *rank = r1;
   }
   __syncthreads();
   const int r1 = r_new;
-  for (int o = tid; o < w * R; o += NT) {
-    const int i = o % w, j = o / w;
-    double pv = 0.0, qv = 0.0;
-    if (j < r1) {
-      const int pj = perm[j];
-      const double sg = sig[pj];
-      pv = (sg > 0.0) ? a[i + (int64_t)pj * w] / sg : 0.0;
-      qv = v[i + (int64_t)pj * w];
-    }
-    P1[o] = pv;
-    Q1[o] = qv;
+  for (int o = tid; o < w * R; o += NTS) P1[o] = Q1[o] = 0.0;
+  __syncthreads();
+  for (int o = tid; o < wa * r1; o += NTS) {
+    const int i = o % wa, j = o / wa;
+    const int pj = perm[j];
+    const double sg = to_d(sig[pj]);
+    P1[idx(i) + (int64_t)j * w] = (sg > 0.0) ? to_d(a[i + (int64_t)pj * wa]) / sg : 0.0;
+    Q1[idx(i) + (int64_t)j * w] = to_d(v[i + (int64_t)pj * wa]);
   }
-  for (int o = tid; o < R * R; o += NT) {
+  for (int o = tid; o < R * R; o += NTS) {
     const int i = o % R, j = o / R;
-    S0[o] = (i == j && i < r1) ? T(sig[perm[i]]) : T(0);
+    S0[o] = (i == j && i < r1) ? T(to_d(sig[perm[i]])) : T(0);
   }
   __syncthreads();
   bool bad = false;
-  for (int o = tid; o < R * R; o += NT) bad |= !isfinite((double)S0[o]);
+  for (int o = tid; o < R * R; o += NTS) bad |= !isfinite((double)S0[o]);
   if (__syncthreads_or(bad) && tid == 0) atomicOr(status, ST_NONFINITE);
 }
 
@@ -439,6 +529,8 @@ struct lri_stream {
   double* small = nullptr;
 };
 
+
+namespace lri {
 namespace {
 
 constexpr int kBlocksSmall = 16;  // FP64 scratch of (2R)^2 each
@@ -464,18 +556,33 @@ struct StreamOps {
     panel_mul<T><<<grid, 256, 0, st>>>(N, a, c, X, ldx, B, ldb, beta, out, ldo);
     return cudaGetLastError();
   }
+  using ST = typename SmallT<T>::type;
+  static size_t svqb_smem(int a) {
+    return (size_t)(2 * a * a + a) * sizeof(ST) + (size_t)a * sizeof(double) + (size_t)(a + 2) * sizeof(int);
+  }
   cudaError_t svqb(int a, const double* G, double* B) const {
-    const size_t smem = (size_t)(2 * a * a + 2 * a) * sizeof(double) + (size_t)(a + 2) * sizeof(int);
     static bool attr_set = false;
     if (!attr_set) {
-      const size_t mx = (size_t)(2 * SMAX * SMAX + 2 * SMAX) * sizeof(double) + (SMAX + 2) * sizeof(int);
-      cudaError_t e = cudaFuncSetAttribute(svqb_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+      cudaError_t e = cudaFuncSetAttribute(svqb_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)svqb_smem(SMAX));
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    // eigenvalues below (64 u^2) of the largest are rounding noise of the panel
-    const double tol_rel = sizeof(T) == 4 ? 1e-12 : 1e-28;
-    svqb_factor<<<1, NT, smem, st>>>(a, G, tol_rel, B);
+    // eigenvalues below 1e-26 of the largest are rounding noise of the Gram
+    // (double-float or FP64 sums of exact products)
+    svqb_factor<ST><<<1, NTS, svqb_smem(a), st>>>(a, G, s->d_rank, 1e-26, B);
+    return cudaGetLastError();
+  }
+  cudaError_t cholinv(int a, const double* G, double* B) const {
+    static bool attr_set = false;
+    const size_t smem = 2 * (size_t)a * a * sizeof(ST);
+    if (!attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(chol_inv_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(2 * SMAX * SMAX * sizeof(ST)));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    chol_inv_factor<ST><<<1, NTS, smem, st>>>(a, G, 1e-20, B);
     return cudaGetLastError();
   }
   // X (N x R) <- orthonormal basis of the part of X orthogonal to the
@@ -491,9 +598,10 @@ struct StreamOps {
         e = mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
       }
     }
+    // one eigenvalue-based pass (rank-revealing), one CholeskyQR pass (orthogonality)
     for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
       e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);                                 // G = X^T X
-      if (e == cudaSuccess) e = svqb(R, blk(1), blk(2));
+      if (e == cudaSuccess) e = (pass == 0) ? svqb(R, blk(1), blk(2)) : cholinv(R, blk(1), blk(2));
       if (e == cudaSuccess) e = mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);        // Z = X B
       if (e == cudaSuccess) {
         copy_cols<T><<<304, 256, 0, st>>>(N, R, tp(s->Zp), N, X, N);
@@ -530,8 +638,22 @@ struct StreamOps {
     // data pass 3: Z = dY Vhat; D = Uhat^T Z
     pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, w, A1, A0, Vh, m, tp(s->Zp));
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
-    core_step<T><<<1, NT, 0, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, blk(6), blk(8),
-                                   blk(9), s->d_status);
+    {
+      // the 2R x 2R matrix in shared memory when it fits (up to 200 KB)
+      const size_t abytes = (size_t)w * w * sizeof(ST);
+      const int in_smem = abytes <= 200 * 1024;
+      static bool attr_set = false;
+      if (!attr_set) {
+        if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+            cudaSuccess)
+          return e;
+        attr_set = true;
+      }
+      ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
+      core_step<T, ST><<<1, NTS, in_smem ? abytes : 0, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol,
+                                                            s->rmin, scr, scr + (int64_t)w * w, blk(8), blk(9),
+                                                            s->d_status, in_smem);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
     if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
@@ -540,6 +662,7 @@ struct StreamOps {
 };
 
 }  // namespace
+}  // namespace lri
 
 extern "C" {
 

@@ -165,3 +165,38 @@ def burgers_uq(n: int, m: int, seed: int = 3):
     phi = g.uniform(0.0, 2 * np.pi, m)
     X0 = np.sin(2 * np.pi * x)[:, None] + a[None, :] * np.sin(4 * np.pi * x[:, None] + phi[None, :])
     return 1.0 / n, nu, X0
+
+
+def data_stream_device(n: int, m: int, nsnap: int, seed: int = 2, K: int = 64, sub: int = 128,
+                       noise: float = 1e-4, dtype=None, device="cuda"):
+    """The data-compression stream of ``data_stream`` generated on the device
+    (mode bases and amplitudes from the seeded host generator, the fixed
+    noise realisation from the device generator).  Returns snap(j) -> a
+    device tensor with the n x m snapshot A(t_j), t_j = j / (nsnap - 1),
+    stored column-major (shape (m, n) row-major)."""
+    import torch
+    from scipy.linalg import expm
+
+    dtype = dtype or torch.float32
+    g = np.random.default_rng(seed)
+    f = g.uniform(0.5, 2.0, K)
+    Qu = random_orthonormal(g, n, sub)
+    Qv = random_orthonormal(g, m, sub)
+    Wu = g.normal(0.0, np.sqrt(0.1), (sub, sub))
+    Wv = g.normal(0.0, np.sqrt(0.1), (sub, sub))
+    Ou, Ov = np.triu(Wu, 1) - np.triu(Wu, 1).T, np.triu(Wv, 1) - np.triu(Wv, 1).T
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    E = noise * torch.randn((m, n), generator=gen, device=device, dtype=dtype)
+    k = np.arange(1, K + 1)
+
+    def snap(j: int):
+        t = j / max(1, nsnap - 1)
+        sig = np.exp(-k / 8.0) * (1.0 + 0.3 * np.sin(2 * np.pi * f * t))
+        Ut = torch.from_numpy(Qu @ expm(t * Ou)[:, :K] * sig).to(device, dtype)
+        Vt = torch.from_numpy(Qv @ expm(t * Ov)[:, :K]).to(device, dtype)
+        return torch.addmm(E, Vt, Ut.T)  # (m, n) row-major = n x m column-major
+
+    # the noise-free rank-K part of A(0): orthonormal factors and amplitudes
+    snap.signal0 = (Qu[:, :K].copy(), np.exp(-k / 8.0), Qv[:, :K].copy())
+    return snap
