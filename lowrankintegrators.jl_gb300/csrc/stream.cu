@@ -369,12 +369,13 @@ __global__ void __launch_bounds__(NTS) svqb_factor(int a, const double* __restri
   }
 }
 
-// One CholeskyQR factor: G = R^T R (a x a, ld a), Bout = R^{-1}; columns with
-// G_jj <= tol_rel * max G_jj are decoupled (R_jj = 1, zero off-diagonal), so
-// zero columns of the panel stay zero.  R and R^{-1} in shared memory.
+// One CholeskyQR factor: G + shift_rel * trace(G) I = R^T R (a x a, ld a),
+// Bout = R^{-1}; columns with G_jj <= tol_rel * max G_jj are decoupled
+// (R_jj = 1, zero off-diagonal), so zero columns of the panel stay zero.
+// R and R^{-1} in shared memory.
 template <typename ST>
 __global__ void __launch_bounds__(NTS) chol_inv_factor(int a, const double* __restrict__ G, double tol_rel,
-                                                       double* __restrict__ Bout) {
+                                                       double shift_rel, double* __restrict__ Bout) {
   extern __shared__ __align__(16) unsigned char smraw[];
   ST* R = reinterpret_cast<ST*>(smraw);  // a x a
   ST* Ri = R + a * a;                     // a x a
@@ -384,10 +385,12 @@ __global__ void __launch_bounds__(NTS) chol_inv_factor(int a, const double* __re
   for (int j = 0; j < a; ++j) gmax = fmax(gmax, G[j + (int64_t)j * a]);
   for (int j = tid; j < a; j += NTS) keep[j] = G[j + (int64_t)j * a] > tol_rel * gmax;
   __syncthreads();
+  double tr = 0.0;
+  for (int j = 0; j < a; ++j) tr += keep[j] ? G[j + (int64_t)j * a] : 0.0;
   for (int o = tid; o < a * a; o += NTS) {
     const int i = o % a, j = o / a;
     const bool kk = keep[i] && keep[j];
-    R[o] = kk ? ST(G[o]) : ST((i == j) ? 1.0 : 0.0);
+    R[o] = kk ? ST(G[o] + ((i == j) ? shift_rel * tr : 0.0)) : ST((i == j) ? 1.0 : 0.0);
   }
   __syncthreads();
   // right-looking Cholesky, upper factor in R (two barriers per column)
@@ -433,7 +436,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
                                                  const double* __restrict__ D, T* S0, int32_t* rank, double tol,
                                                  int rmin, ST* __restrict__ ag, ST* __restrict__ vg,
                                                  double* __restrict__ P1, double* __restrict__ Q1, uint32_t* status,
-                                                 int a_in_smem) {
+                                                 int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ __align__(16) unsigned char sig_raw[2 * SMAX * sizeof(ST)];
   ST* sig = reinterpret_cast<ST*>(sig_raw);
@@ -445,6 +448,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   // active rows / columns: the first r of each half of [U0 | Q] ([V0 | Q])
   const int r = min(R, (int)*rank), wa = 2 * r;
   auto idx = [&](int i) { return (i < r) ? i : R + (i - r); };
+  const bool a_in_smem = (size_t)wa * wa * sizeof(ST) <= (size_t)smem_bytes;
   ST* a = a_in_smem ? reinterpret_cast<ST*>(smraw) : ag;  // wa x wa
   ST* v = vg;                                              // wa x wa
   // T1 = S0 N^T (r x wa) into v; a = M T1 + D on the active block (FP64 products)
@@ -573,7 +577,7 @@ struct StreamOps {
     svqb_factor<ST><<<1, NTS, svqb_smem(a), st>>>(a, G, s->d_rank, 1e-26, B);
     return cudaGetLastError();
   }
-  cudaError_t cholinv(int a, const double* G, double* B) const {
+  cudaError_t cholinv(int a, const double* G, double* B, double shift_rel) const {
     static bool attr_set = false;
     const size_t smem = 2 * (size_t)a * a * sizeof(ST);
     if (!attr_set) {
@@ -582,7 +586,7 @@ struct StreamOps {
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    chol_inv_factor<ST><<<1, NTS, smem, st>>>(a, G, 1e-20, B);
+    chol_inv_factor<ST><<<1, NTS, smem, st>>>(a, G, 1e-20, shift_rel, B);
     return cudaGetLastError();
   }
   // X (N x R) <- orthonormal basis of the part of X orthogonal to the
@@ -598,10 +602,15 @@ struct StreamOps {
         e = mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
       }
     }
-    // one eigenvalue-based pass (rank-revealing), one CholeskyQR pass (orthogonality)
-    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+    // shifted CholeskyQR3 (Fukaya et al., SIAM J. Sci. Comput. 2020): the
+    // first pass shifted by 11 (N a + a (a+1)) u tr(G) with u the Gram's
+    // rounding unit (double-float sums of exact FP32 products: 2^-44; FP64:
+    // 2^-53), then two plain passes
+    const double ug = sizeof(T) == 4 ? 5.7e-14 : 1.1e-16;
+    const double shift = 11.0 * ((double)N * R + (double)R * (R + 1)) * ug;
+    for (int pass = 0; pass < 3 && e == cudaSuccess; ++pass) {
       e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);                                 // G = X^T X
-      if (e == cudaSuccess) e = (pass == 0) ? svqb(R, blk(1), blk(2)) : cholinv(R, blk(1), blk(2));
+      if (e == cudaSuccess) e = cholinv(R, blk(1), blk(2), pass == 0 ? shift : 0.0);
       if (e == cudaSuccess) e = mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);        // Z = X B
       if (e == cudaSuccess) {
         copy_cols<T><<<304, 256, 0, st>>>(N, R, tp(s->Zp), N, X, N);
@@ -639,9 +648,8 @@ struct StreamOps {
     pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, w, A1, A0, Vh, m, tp(s->Zp));
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
     {
-      // the 2R x 2R matrix in shared memory when it fits (up to 200 KB)
-      const size_t abytes = (size_t)w * w * sizeof(ST);
-      const int in_smem = abytes <= 200 * 1024;
+      // the active 2r x 2r matrix in shared memory when it fits (200 KB)
+      const int abytes = 200 * 1024;
       static bool attr_set = false;
       if (!attr_set) {
         if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
@@ -650,9 +658,8 @@ struct StreamOps {
         attr_set = true;
       }
       ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
-      core_step<T, ST><<<1, NTS, in_smem ? abytes : 0, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol,
-                                                            s->rmin, scr, scr + (int64_t)w * w, blk(8), blk(9),
-                                                            s->d_status, in_smem);
+      core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, scr,
+                                               scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
