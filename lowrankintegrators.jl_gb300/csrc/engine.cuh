@@ -1678,8 +1678,10 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 // NTH: threads of the calling block (a multiple of 32); the instance engine
 // calls it with its NT threads, the single-CTA kernels of the large-stream
 // engine with 1024.
+// max_sweeps < 40 runs that many sweeps at most (a polishing pass after a
+// lower-precision solve).
 template <typename T, int NTH = NT>
-__device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag) {
+__device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag, int max_sweeps = 40) {
   constexpr int NWJ = NTH / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // rotation threshold: P ulps (the rounding level of a length-P dot
@@ -1701,7 +1703,7 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   const T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
   bool converged = false;
-  for (int sweep = 0; sweep < 40 && !converged; ++sweep) {
+  for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
     if (tid == 0) *flag = 0;
     __syncthreads();
     for (int rnd = 0; rnd < Pe - 1; ++rnd) {

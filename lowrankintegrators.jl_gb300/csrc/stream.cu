@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/lri.h"
@@ -424,6 +425,52 @@ __global__ void __launch_bounds__(NTS) chol_inv_factor(int a, const double* __re
   for (int o = tid; o < a * a; o += NTS) Bout[o] = to_d(Ri[o]);
 }
 
+// C (P x P, ld P) = op(A) B with op(A) = A or A^T, all in ST, NTS threads.
+template <typename ST>
+__device__ void sq_mul(int P, const ST* A, bool ta, const ST* B, ST* C) {
+  for (int o = threadIdx.x; o < P * P; o += NTS) {
+    const int i = o % P, j = o / P;
+    ST acc(0.0);
+    for (int k = 0; k < P; ++k) acc = fma_acc(ta ? A[k + i * P] : A[i + k * P], B[k + j * P], acc);
+    C[o] = renorm(acc);
+  }
+  __syncthreads();
+}
+
+// SVD of the P x P double-float matrix a (in place; right vectors to v): the
+// Jacobi sweeps run in FP32 (a32, v32: P*P floats each), the FP32 right
+// vectors are made orthonormal to double-float precision by two Newton-Schulz
+// steps X <- X (3I - X^T X) / 2, a <- a X, and one double-float sweep
+// polishes the rotated matrix (its columns are then orthogonal to FP32
+// precision, so one sweep squares that).  t1, t2: P*P double-float scratch.
+__device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* perm, int* flag, float* a32,
+                                 float* v32, float* sig32, dfloat* t1, dfloat* t2) {
+  for (int o = threadIdx.x; o < P * P; o += NTS) a32[o] = a[o].hi + a[o].lo;
+  __syncthreads();
+  const bool ok = jacobi_svd<float, NTS>(P, a32, v32, sig32, perm, flag);
+  for (int o = threadIdx.x; o < P * P; o += NTS) t1[o] = dfloat(v32[o], 0.0f);  // X0 = V32
+  __syncthreads();
+  for (int it = 0; it < 2; ++it) {
+    sq_mul<dfloat>(P, t1, true, t1, t2);                                             // X^T X
+    for (int o = threadIdx.x; o < P * P; o += NTS) {
+      const int i = o % P, j = o / P;
+      t2[o] = ((i == j) ? dfloat(1.5f, 0.0f) : dfloat(0.0f, 0.0f)) - dfloat(0.5f, 0.0f) * t2[o];
+    }
+    __syncthreads();
+    sq_mul<dfloat>(P, t1, false, t2, v);                                             // X (3I - X^T X)/2
+    for (int o = threadIdx.x; o < P * P; o += NTS) t1[o] = v[o];
+    __syncthreads();
+  }
+  sq_mul<dfloat>(P, a, false, t1, t2);                                               // a X
+  for (int o = threadIdx.x; o < P * P; o += NTS) a[o] = t2[o];
+  __syncthreads();
+  jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, 1);                              // polish: a = U S, V_p
+  sq_mul<dfloat>(P, t1, false, v, t2);                                               // V = X V_p
+  for (int o = threadIdx.x; o < P * P; o += NTS) v[o] = t2[o];
+  __syncthreads();
+  return ok;
+}
+
 // S-step core and truncation.  In: Mh = Uhat^T U0 (w x R), Nh = Vhat^T V0
 // (w x R), D = Uhat^T dY Vhat (w x w), S0 (R x R, T), rank (device).  Out:
 // P1, Q1 (w x R FP64: the kept left / right singular vectors, zero beyond
@@ -436,7 +483,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
                                                  const double* __restrict__ D, T* S0, int32_t* rank, double tol,
                                                  int rmin, ST* __restrict__ ag, ST* __restrict__ vg,
                                                  double* __restrict__ P1, double* __restrict__ Q1, uint32_t* status,
-                                                 int smem_bytes) {
+                                                 int smem_bytes, double* __restrict__ mx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ __align__(16) unsigned char sig_raw[2 * SMAX * sizeof(ST)];
   ST* sig = reinterpret_cast<ST*>(sig_raw);
@@ -466,7 +513,18 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     a[o] = ST(sacc);
   }
   __syncthreads();
-  const bool ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag);
+  bool ok;
+  if constexpr (sizeof(ST) == 8 && !std::is_same<ST, double>::value) {
+    // double-float: FP32 sweeps, double-float polish (scratch after a in
+    // shared memory when it fits, else in the global scratch mx)
+    float* a32 = reinterpret_cast<float*>(mx);
+    float* v32 = a32 + wa * wa;
+    __shared__ float sig32[2 * SMAX];
+    ok = jacobi_svd_mixed(wa, a, v, sig, perm, &flag, a32, v32, sig32,
+                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa);
+  } else {
+    ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag);
+  }
   if (tid == 0) {
     if (!ok) atomicOr(status, ST_SVD_NOCONV);
     // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R]
@@ -658,8 +716,9 @@ struct StreamOps {
         attr_set = true;
       }
       ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
+      // blocks 10..13: FP32 copies and double-float products of the mixed-precision SVD
       core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, scr,
-                                               scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes);
+                                               scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes, blk(10));
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
