@@ -307,6 +307,124 @@ def run_stream(args):
     print(json.dumps(line), flush=True)
 
 
+FP32_FFMA_TFLOPS = 74.6  # FP32 FMA-loop probe on this machine's GB300 (152 SMs at 2070 MHz)
+
+
+def run_burgers(args):
+    """The Burgers-UQ workload on one GPU: u_t + (u^2/2)_x = nu u_xx,
+    periodic, n = 4096 grid points, m = 16384 samples (nu_j ~ U[0.005, 0.02],
+    u0_j = sin 2 pi x + a_j sin(4 pi x + phi_j)), rank-adaptive BUG with
+    rmin = 16, rmax = 64, tol = 1e-4, dt = 1e-4, FP32 panels, on the large
+    Burgers engine from the exact rank-3 initial data (padded to 16).  The
+    diffusion term is stiff (4 nu / h^2 = 1.34e6, dt * lambda = 134), so the
+    substeps are RK4 with 64 substeps (dt * lambda / 64 = 2.1, inside RK4's
+    stability interval of 2.78; the reference's adaptive Tsit5 takes steps of
+    that size too).  W warm-up steps, then K timed steps; the same at a fixed
+    rank 64 (rmin = rmax) for the upper end of the rank range; accuracy of 3
+    steps against the FP64 engine at full size (whose oracle parity the tests
+    check at smaller sizes); the oracle's step timed on a bounded sample."""
+    import torch
+    import __graft_entry__ as ge
+    import workloads
+    from oracle import lri_oracle as O
+    lri = ge.load_package()
+    n, m, r0, R, tol, dt, nsub = 4096, 16384, 16, 64, 1e-4, 1e-4, 64
+    K, W = args.steps, args.warmup
+    h, nu, U0, s0, V0 = workloads.burgers_uq_factors(n, m, r0)
+    Y0 = lri.SVDLikeRepresentation(U0, np.diag(s0), V0)
+    op = lri.BurgersOperator(h, nu, alpha=0.0, beta=-0.5)
+    stream = torch.cuda.current_stream()
+
+    def timed(rmin, k, w, precision="fp32", sample=False):
+        eng = lri.BurgersLargeEngine(op, n, m, r0 if rmin < R else R, R, tol, lri.RK4(nsub), rmin, precision)
+        if rmin < R:
+            eng.bind(Y0)
+        else:  # rank 64 from the start: Y0 padded with zero directions
+            _, _, U64, s64, V64 = workloads.burgers_uq_factors(n, m, R)
+            eng.bind(lri.SVDLikeRepresentation(U64, np.diag(s64), V64))
+        eng.advance(dt, w)
+        eng.check_status()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(torch.cuda.current_device()) if sample else None
+        if sampler:
+            sampler.__enter__()
+        e0.record(stream)
+        eng.advance(dt, k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+        eng.check_status()
+        rank = eng.rank()
+        y = eng.download()
+        eng.close()
+        return e0.elapsed_time(e1) / k, rank, (sampler.summary() if sampler else None), y
+
+    ms, rank_end, clocks, _ = timed(16, K, W, sample=True)
+    ms64, _, _, _ = timed(R, 3, 1)
+    # accuracy: 3 steps in FP32 against the same 3 steps in FP64 (full size)
+    _, _, _, y32 = timed(16, 1, 2)
+    ms_f64, _, _, y64 = timed(16, 1, 2, precision="fp64")
+
+    def gram_fro(a, b):
+        return np.trace((a.U.T @ b.U) @ b.S @ (b.V.T @ a.V) @ a.S.T)
+    d2 = gram_fro(y32, y32) - 2 * gram_fro(y32, y64) + gram_fro(y64, y64)
+    err = float(np.sqrt(max(d2, 0.0) / gram_fro(y64, y64)))
+    # e2e through the public solve: factors from host memory, result back to host
+    prob = lri.MatrixDEProblem(op, Y0, (0.0, 3 * dt))
+    alg = lri.RankAdaptiveUnconventionalAlgorithm(tol, rmax=R, K_alg=lri.RK4(nsub), rmin=16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lri.solve_burgers_large(prob, alg, dt)
+    e2e_s = (time.perf_counter() - t0) / 3
+    # CPU: the oracle's first step on the first m_s = 2048 samples with 1 and
+    # 2 RK4 substeps; the step's cost is linear in m and in the substeps, so
+    # t(m, 64) = (m / m_s) (t1 + 63 (t2 - t1))
+    ms_cols = 2048
+    Ys = O.SVDLikeRepresentation(U0, np.diag(s0), V0[:ms_cols])
+    Ys.V = np.linalg.qr(V0[:ms_cols])[0]
+    tcpu = []
+    for ns in (1, 2):
+        po = O.MatrixDEProblem(O.BurgersOp(n, h, nu[:ms_cols], alpha=0.0, beta=-0.5), Ys.copy(), (0.0, dt))
+        t0 = time.perf_counter()
+        O.solve(po, O.RankAdaptiveUnconventionalAlgorithm(tol, rmax=R, K_alg=O.RK4(ns), rmin=16), dt,
+                save_everystep=False)
+        tcpu.append(time.perf_counter() - t0)
+    cpu_step = (m / ms_cols) * (tcpu[0] + (nsub - 1) * max(tcpu[1] - tcpu[0], 0.0))
+
+    # flow contractions of one step at rank r: every RK stage of the K and L
+    # substeps forms the r-column tiles of K V^T and contracts F with V
+    # (2 n m r FMA each), of the S substep the same with 2r columns
+    def step_flops(r):
+        return nsub * 4 * (2 * n * m * r * 2 + 2 * n * m * (2 * r)) * 2.0
+    achieved = step_flops(rank_end) / (ms * 1e-3) / 1e12
+    line = {"metric": "rank-adaptive BUG steps/s (Burgers UQ, n=4096, m=16384, r 16..64)", "value": 1e3 / ms,
+            "unit": "steps/s", "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Burgers-UQ samples)",
+            "config": {"workload": "burgers_uq_4096x16384", "dt": dt, "tol": tol, "r_min": 16, "r_max": R,
+                       "rank_after": rank_end, "scheme": f"RK4, {nsub} substeps",
+                       "ms_per_step_at_rank_64": ms64, "ms_per_step_fp64_engine": ms_f64,
+                       "l2": "no n x m matrix exists; factors (4096 + 16384) x 128 FP32 stay in L2"},
+            "accuracy": {"steps": 3, "rel_fro_fp32_vs_fp64_engine": err, "rank_fp32": y32.S.shape[0],
+                         "rank_fp64": y64.S.shape[0]},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_FFMA_TFLOPS, "unit": "TFLOP/s",
+                         "frac": achieved / FP32_FFMA_TFLOPS, "traffic": None,
+                         "peak_source": "measured FP32 FMA probe (not tensor cores: the flow tiles run on the "
+                                        "FP32 pipe)",
+                         "algorithmic_flops_per_step": step_flops(rank_end)},
+            "gpu_launches": None,
+            "clocks": clocks,
+            "cpu_baseline": {"value": 1.0 / cpu_step, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"oracle step on {ms_cols} of {m} samples with 1 and 2 RK4 substeps "
+                                       f"({tcpu[0]:.1f} s, {tcpu[1]:.1f} s), scaled linearly to {m} samples "
+                                       f"and {nsub} substeps"},
+            "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s",
+                    "h2d_bytes_per_step": ((n + m) * r0 + r0 * r0 + m) * 4 // 3,
+                    "d2h_bytes_per_step": ((n + m) * R + R * R) * 4 // 3}}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """The adjoint workload on one GPU: one loss + gradient sweep (forward
     with checkpoints every 20 steps, segment replays, 200 adjoint-step
@@ -378,6 +496,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--adjoint", action="store_true",
                     help="instead of the ensemble: the adjoint workload (loss + gradient, FD check)")
+    ap.add_argument("--burgers", action="store_true",
+                    help="instead of the ensemble: the Burgers-UQ workload (n=4096, m=16384, rank 16..64)")
     ap.add_argument("--stream", action="store_true",
                     help="instead of the ensemble: the 8192 x 4096 data-compression stream (rank-adaptive)")
     args = ap.parse_args()
@@ -393,6 +513,10 @@ def main():
     if args.stream:
         if rank == 0:
             run_stream(args)
+        return
+    if args.burgers:
+        if rank == 0:
+            run_burgers(args)
         return
 
     # CPU baseline first: its spawn pool starts before any GPU work

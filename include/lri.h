@@ -258,6 +258,20 @@ LRI_API lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void
 LRI_API lri_status lri_stream_rank(lri_stream* s, int64_t* r_out, void* stream);
 LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
 
+/* One large Burgers instance (the Burgers-UQ workload: n grid points x m
+ * samples too large for the batch) on the same engine: rank-adaptive BUG
+ * (rank_adaptive_unconventional.jl:194-233) for LRI_OP_BURGERS_PERIODIC with
+ * the given substep scheme; every flow evaluation F(K V^T) V, F(U L^T)^T U,
+ * Uhat^T F(Uhat S Vhat^T) Vhat is a grid of 32 x 32 tiles of Y formed in
+ * shared memory, never the n x m matrix.  r_max <= 64.  bind: the caller's
+ * U, S, V (as lri_stream_bind) and nu (m viscosities, device).  Destroy with
+ * lri_stream_destroy; rank and status as for the stream. */
+LRI_API lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0,
+                                      int64_t r_max, double tol, int32_t r_min, double h, double alpha,
+                                      double beta, const lri_scheme* scheme);
+LRI_API lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void* nu);
+LRI_API lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stream);
+
 /* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);
 

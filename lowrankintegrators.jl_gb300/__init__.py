@@ -947,3 +947,74 @@ def solve_stream(prob: MatrixDataProblem, alg: RankAdaptiveUnconventionalAlgorit
         return sol
     finally:
         eng.close()
+
+
+class BurgersLargeEngine(DataStreamEngine):
+    """Rank-adaptive BUG for one large BurgersOperator instance (the
+    Burgers-UQ workload) on the whole GPU (lri_burgers_*): every flow
+    evaluation is a grid of shared-memory tiles of K V^T, never the n x m
+    matrix."""
+
+    def __init__(self, op: "BurgersOperator", n: int, m: int, r0: int, rmax: int, tol: float, scheme,
+                 rmin: int = 1, precision: str = "fp32"):
+        torch = _torch()
+        self.torch = torch
+        self.lib = _native.load()
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.dtype = torch.float32 if precision == "fp32" else torch.float64
+        self.np_dtype = np.float32 if precision == "fp32" else np.float64
+        self.n, self.m, self.R = int(n), int(m), int(rmax)
+        self.handle = C.c_void_p()
+        code = _native.LRI_F32 if precision == "fp32" else _native.LRI_F64
+        self._sch = scheme.to_c()
+        _native.check(self.lib.lri_burgers_create(C.byref(self.handle), code, self.n, self.m, int(r0), self.R,
+                                                  float(tol), int(rmin), op.h, op.alpha, op.beta,
+                                                  C.byref(self._sch)), "lri_burgers_create")
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        self.U = torch.zeros(self.n * self.R, dtype=self.dtype, device=dev)
+        self.S = torch.zeros(self.R * self.R, dtype=self.dtype, device=dev)
+        self.V = torch.zeros(self.m * self.R, dtype=self.dtype, device=dev)
+        _, nu = op.packed_for(self.n, self.m)
+        self.nu = torch.from_numpy(np.asarray(nu, dtype=self.np_dtype)).to(dev)
+
+    def bind(self, Y0: SVDLikeRepresentation):
+        super().bind(Y0)
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        _native.check(self.lib.lri_burgers_bind(self.handle, ptr(self.U), ptr(self.S), ptr(self.V), ptr(self.nu)),
+                      "lri_burgers_bind")
+
+    def advance(self, dt: float, nsteps: int = 1):
+        _native.check(self.lib.lri_burgers_step(self.handle, float(dt), int(nsteps), self._stream()),
+                      "lri_burgers_step")
+
+
+def solve_burgers_large(prob: MatrixDEProblem, alg: RankAdaptiveUnconventionalAlgorithm, dt: float,
+                        precision: str = "fp32", save_everystep: bool = False) -> DLRSolution:
+    """solve(prob, alg, dt) (src/primitives.jl:68-80) for one BurgersOperator
+    instance too large for the batch, on the whole GPU (rank-adaptive BUG)."""
+    if not isinstance(prob.f, BurgersOperator):
+        raise LriError(2, "the large Burgers engine takes a BurgersOperator problem")
+    u0 = prob.u0
+    n, m = u0.U.shape[0], u0.V.shape[0]
+    eng = BurgersLargeEngine(prob.f, n, m, u0.S.shape[0], min(alg.rmax, 64), alg.tol, alg.K_alg, alg.rmin, precision)
+    try:
+        eng.bind(u0)
+        t0 = prob.tspan[0]
+        sol = DLRSolution([u0.copy()], [float(t0)])
+        k = n_steps(prob.tspan, dt)
+        if save_everystep:
+            for j in range(k):
+                eng.advance(dt, 1)
+                eng.check_status()
+                sol.Y.append(eng.download())
+                sol.t.append(float(t0 + (j + 1) * dt))
+        else:
+            eng.advance(dt, k)
+            eng.check_status()
+            sol.Y.append(eng.download())
+            sol.t.append(float(t0 + k * dt))
+        return sol
+    finally:
+        eng.close()

@@ -31,7 +31,7 @@ EXPORTED = [
     "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step", "lri_bug_step_noalloc",
     "lri_batch_prepare", "lri_batch_adjoint_step",
     "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
-    "lri_stream_status",
+    "lri_stream_status", "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
 ]
 
 
@@ -103,6 +103,13 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_stream_rank.argtypes = [P, C.POINTER(C.c_int64), P]
     lib.lri_stream_status.restype = C.c_int
     lib.lri_stream_status.argtypes = [P, P]
+    lib.lri_burgers_create.restype = C.c_int
+    lib.lri_burgers_create.argtypes = [C.POINTER(P), C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                       C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double, P]
+    lib.lri_burgers_bind.restype = C.c_int
+    lib.lri_burgers_bind.argtypes = [P, P, P, P, P]
+    lib.lri_burgers_step.restype = C.c_int
+    lib.lri_burgers_step.argtypes = [P, C.c_double, C.c_int32, P]
     lib.lri_batch_adjoint_step.restype = C.c_int
     lib.lri_batch_adjoint_step.argtypes = [P, C.c_double, P, P, P, P, P, P, P, P]
     lib.lri_batch_prepare.restype = C.c_int

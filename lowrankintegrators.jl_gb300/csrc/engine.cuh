@@ -1679,17 +1679,24 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 // calls it with its NT threads, the single-CTA kernels of the large-stream
 // engine with 1024.
 // max_sweeps < 40 runs that many sweeps at most (a polishing pass after a
-// lower-precision solve).
+// lower-precision solve).  skip_noise = false also rotates a noise-level
+// column against a larger one (the FP32 preconditioning sweeps of the mixed
+// SVD, which stop after a few sweeps anyway and leave the larger columns'
+// orthogonality to the polish).
 template <typename T, int NTH = NT>
-__device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag, int max_sweeps = 40) {
+__device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag, int max_sweeps = 40,
+                                        bool skip_noise = true) {
   constexpr int NWJ = NTH / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // rotation threshold: P ulps (the rounding level of a length-P dot
   // product), so a sweep whose remaining products are rounding noise ends
   const T eps = T(Prec<T>::eps * P);
   for (int o = tid; o < P * P; o += NTH) v[o] = ((o % P) == (o / P)) ? T(1) : T(0);
-  // Pairs whose columns are both below eps * ||B||_F are left alone: their
-  // directions are rounding noise, and rotating them could go on forever.
+  // Pairs with a column below eps * ||B||_F are left alone: such a column is
+  // rounding noise, and rotating it against several such columns that are
+  // not orthogonal among themselves converges only linearly (projection one
+  // column at a time).  Their left vectors a_j / sigma_j are therefore not
+  // orthogonal to the rest; complete_left below repairs the kept ones.
   __shared__ __align__(16) unsigned char red_raw[NWJ * sizeof(T)];
   T* red = reinterpret_cast<T*>(red_raw);
   T fro2 = T(0);
@@ -1722,7 +1729,8 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
         }
         al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
         // (sqrt(al) * sqrt(be): al * be can leave the FP32 exponent range)
-        if ((al > tiny || be > tiny) && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
+        const bool live = skip_noise ? (al > tiny && be > tiny) : (al > tiny || be > tiny);
+        if (live && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
           const T zeta = (be - al) / (T(2) * ga);
           // for large |zeta| use tan = 1/(2 zeta): zeta^2 would leave the FP32
           // exponent range of float and double-float values
@@ -1769,6 +1777,97 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   }
   __syncthreads();
   return converged;
+}
+
+// Left singular vectors of jacobi_svd's output, in place: the kept columns
+// a[:, perm[j]], j < r1 (descending sigma), become a_j / sigma_j.  Those
+// whose sigma_j is at the rounding level of the matrix (sigma_j^2 <= 16 eps^2
+// ||A||_F^2, where the sweeps leave pairs alone) are not orthogonal to the
+// others; the minimum rank can keep them.  Each is re-orthogonalised against
+// the kept columns before it (classical Gram-Schmidt, two passes) and
+// normalised; when that leaves less than 1 / (2P) of its squared norm (or it
+// is zero) a unit vector e_k takes its place (of the P unit vectors, the
+// squared residuals sum to P - j >= 1, so one of them passes).  Any unit
+// direction orthogonal to the others serves: sigma_j is below rounding.
+// scr: P + r1 values of scratch (global or shared).
+template <typename T, int NTH = NT>
+__device__ __noinline__ void complete_left(int P, int r1, T* a, const T* sigma, const int* perm, T* scr) {
+  constexpr int NWJ = NTH / 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ int j0s;
+  __shared__ double nrm_s;
+  for (int o = tid; o < P * r1; o += NTH) {
+    const int i = o % P, j = o / P;
+    const int pj = perm[j];
+    const T sg = sigma[pj];
+    a[i + pj * P] = (sg > T(0)) ? a[i + pj * P] / sg : T(0);
+  }
+  if (tid == 0) {
+    double fro2 = 0.0;
+    for (int j = 0; j < P; ++j) {
+      const double sv = (double)sigma[j];
+      fro2 += sv * sv;
+    }
+    const double thr2 = 16.0 * Prec<T>::eps * Prec<T>::eps * fro2;
+    int j0 = r1;
+    while (j0 > 0) {
+      const double sv = (double)sigma[perm[j0 - 1]];
+      if (sv * sv > thr2) break;
+      --j0;
+    }
+    j0s = j0;
+  }
+  __syncthreads();
+  T* cand = scr;
+  T* coef = scr + P;
+  int next_unit = 0;
+  for (int jj = j0s; jj < r1; ++jj) {
+    T* col = a + perm[jj] * P;
+    bool use_unit = false;
+    for (int attempt = 0; attempt <= P; ++attempt) {
+      for (int i = tid; i < P; i += NTH) cand[i] = use_unit ? T((i == next_unit) ? 1.0 : 0.0) : col[i];
+      __syncthreads();
+      double n0 = 0.0;
+      if (tid == 0)
+        for (int i = 0; i < P; ++i) n0 += (double)cand[i] * (double)cand[i];
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int c = warp; c < jj; c += NWJ) {
+          const T* pc = a + perm[c] * P;
+          T d = T(0);
+          for (int i = lane; i < P; i += 32) d = fma(pc[i], cand[i], d);
+          d = warp_sum(d);
+          if (lane == 0) coef[c] = d;
+        }
+        __syncthreads();
+        for (int i = tid; i < P; i += NTH) {
+          T x = cand[i];
+          for (int c = 0; c < jj; ++c) x = fma(-coef[c], a[i + perm[c] * P], x);
+          cand[i] = x;
+        }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        T q = T(0);
+        for (int i = 0; i < P; ++i) q = fma(cand[i], cand[i], q);
+        nrm_s = (n0 > 0.0 && (double)q > n0 / (2.0 * P)) ? (double)q : 0.0;
+      }
+      __syncthreads();
+      if (nrm_s > 0.0) break;
+      if (use_unit) next_unit = (next_unit + 1) % P;
+      use_unit = true;
+      __syncthreads();
+    }
+    if (nrm_s > 0.0) {
+      T q = T(0);
+      for (int i = 0; i < P; ++i) q = fma(cand[i], cand[i], q);  // every thread: the same sum
+      const T inv = T(1) / sqrt(q);
+      for (int i = tid; i < P; i += NTH) col[i] = cand[i] * inv;
+    } else {
+      for (int i = tid; i < P; i += NTH) col[i] = T(0);
+    }
+    if (use_unit) next_unit = (next_unit + 1) % P;
+    __syncthreads();
+  }
 }
 
 }  // namespace lri

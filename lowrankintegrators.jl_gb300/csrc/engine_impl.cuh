@@ -683,14 +683,15 @@ __device__ __noinline__ void ra_bug_step(const StepArgs<T>& g, Inst<T>& I, int r
   }
   __syncthreads();
   const int r1 = r_new_s;
+  // left vectors a_j / sigma_j in place (T1 as scratch)
+  complete_left<T>(w2, r1, a, sigma, perm, T1);
   // P1 = left vectors (2r x r1) into T1, Q1 = right vectors into T2; sorted
   // singular values into sm.vec[WMAX..] (the staging area is reused below)
   T* sig_sorted = sm.vec + WMAX;
   for (int o = threadIdx.x; o < w2 * r1; o += NT) {
     const int i = o % w2, j = o / w2;
     const int pj = perm[j];
-    const T sg = sigma[pj];
-    T1[i + (int64_t)j * W] = (sg > T(0)) ? a[i + pj * w2] / sg : T(0);
+    T1[i + (int64_t)j * W] = a[i + pj * w2];
     T2[i + (int64_t)j * W] = v[i + pj * w2];
   }
   for (int j = threadIdx.x; j < r1; j += NT) sig_sorted[j] = sigma[perm[j]];

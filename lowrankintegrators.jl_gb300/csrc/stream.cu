@@ -299,6 +299,66 @@ __global__ void __launch_bounds__(256) panel_mul(int N, int a, int c, const T* _
   }
 }
 
+// out = X B for FP32 panels with double-float sums: B = Bh + Bl split into
+// floats, X Bh accumulated from exact products (TwoProduct), X Bl added to
+// the low part.  For orthonormalisation factors B whose entries are far
+// larger than the entries of X B (1 / sqrt of small eigenvalues of a nearly
+// dependent panel): FP32 sums would lose u32 * |X| |B| to cancellation.
+__global__ void __launch_bounds__(256) panel_mul_df(int N, int a, int c, const float* __restrict__ X, int ldx,
+                                                    const double* __restrict__ B, int ldb, float* __restrict__ out,
+                                                    int ldo) {
+  constexpr int KC2 = 32;
+  __shared__ float xs[32][KC2 + 1];
+  __shared__ float bh[KC2][65];
+  __shared__ float bl[KC2][65];
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+  const int ri = tid & 15, cj = tid >> 4;
+  dfloat acc[2][4];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = dfloat(0.0f, 0.0f);
+  for (int k0 = 0; k0 < a; k0 += KC2) {
+    const int kc = min(KC2, a - k0);
+    for (int e = tid; e < 32 * KC2; e += 256) {
+      const int ii = e % 32, k = e / 32;
+      const int i = i0 + ii;
+      xs[ii][k] = (i < N && k < kc) ? X[i + (int64_t)(k0 + k) * ldx] : 0.0f;
+    }
+    for (int e = tid; e < KC2 * 64; e += 256) {
+      const int k = e % KC2, cc = e / KC2;
+      const double b = (k < kc && c0 + cc < c) ? B[(k0 + k) + (int64_t)(c0 + cc) * ldb] : 0.0;
+      const float h = (float)b;
+      bh[k][cc] = h;
+      bl[k][cc] = (float)(b - (double)h);
+    }
+    __syncthreads();
+    for (int k = 0; k < KC2; ++k) {
+      const float x0 = xs[ri][k], x1 = xs[ri + 16][k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float wh = bh[k][cj + 16 * q], wl = bl[k][cj + 16 * q];
+        acc[0][q] = acc_mul_acc(acc[0][q], x0, wh);
+        acc[0][q].lo = fmaf(x0, wl, acc[0][q].lo);
+        acc[1][q] = acc_mul_acc(acc[1][q], x1, wh);
+        acc[1][q].lo = fmaf(x1, wl, acc[1][q].lo);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int i = i0 + ri + 16 * p;
+    if (i >= N) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = c0 + cj + 16 * q;
+      if (j < c) out[i + (int64_t)j * ldo] = renorm(acc[p][q]).hi;
+    }
+  }
+}
+
 __global__ void negate(int k, double* x) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o < k) x[o] = -x[o];
@@ -326,49 +386,6 @@ __device__ __forceinline__ double to_d(double x) { return x; }
 __device__ __forceinline__ double to_d(dfloat x) { return (double)x; }
 
 constexpr int NTS = 1024;  // threads of the single-CTA kernels
-
-// Eigenvalue-based orthonormalisation factor of a Gram matrix G (a x a, ld a)
-// restricted to its leading r x r block (r = *rank: the panel's columns
-// beyond the rank are zero): Bout (a x a, ld a, zero outside that block) =
-// D W Lambda^{-1/2} with D = diag(G)^{-1/2} and D G D = W Lambda W^T, so
-// X Bout has orthonormal columns; eigenvalues below tol_rel * max
-// eigenvalue (and zero diagonal entries) give zero columns.
-template <typename ST>
-__global__ void __launch_bounds__(NTS) svqb_factor(int a, const double* __restrict__ G, const int32_t* rank,
-                                                   double tol_rel, double* __restrict__ Bout) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int r = min(a, (int)*rank);
-  ST* M = reinterpret_cast<ST*>(smraw);  // r x r
-  ST* W = M + r * r;                      // r x r
-  ST* lam = W + r * r;                    // r
-  double* d = reinterpret_cast<double*>(lam + r);
-  int* perm = reinterpret_cast<int*>(d + r);
-  int* flag = perm + r + 1;
-  const int tid = threadIdx.x;
-  for (int j = tid; j < r; j += NTS) {
-    const double g = G[j + (int64_t)j * a];
-    d[j] = (g > 0.0) ? 1.0 / sqrt(g) : 0.0;
-  }
-  __syncthreads();
-  for (int o = tid; o < r * r; o += NTS) {
-    const int i = o % r, j = o / r;
-    M[o] = ST(d[i] * G[i + (int64_t)j * a] * d[j]);
-  }
-  __syncthreads();
-  // symmetric PSD: the one-sided Jacobi SVD gives eigenvectors (v) and eigenvalues (sigma)
-  jacobi_svd<ST, NTS>(r, M, W, lam, perm, flag);
-  double lmax = 0.0;
-  for (int j = 0; j < r; ++j) lmax = fmax(lmax, to_d(lam[j]));
-  for (int o = tid; o < a * a; o += NTS) {
-    const int i = o % a, j = o / a;
-    double bv = 0.0;
-    if (i < r && j < r) {
-      const double l = to_d(lam[j]);
-      bv = (l > tol_rel * lmax && l > 0.0) ? d[i] * to_d(W[i + j * r]) / sqrt(l) : 0.0;
-    }
-    Bout[o] = bv;
-  }
-}
 
 // One CholeskyQR factor: G + shift_rel * trace(G) I = R^T R (a x a, ld a),
 // Bout = R^{-1}; columns with G_jj <= tol_rel * max G_jj are decoupled
@@ -440,14 +457,19 @@ __device__ void sq_mul(int P, const ST* A, bool ta, const ST* B, ST* C) {
 // SVD of the P x P double-float matrix a (in place; right vectors to v): the
 // Jacobi sweeps run in FP32 (a32, v32: P*P floats each), the FP32 right
 // vectors are made orthonormal to double-float precision by two Newton-Schulz
-// steps X <- X (3I - X^T X) / 2, a <- a X, and one double-float sweep
-// polishes the rotated matrix (its columns are then orthogonal to FP32
-// precision, so one sweep squares that).  t1, t2: P*P double-float scratch.
+// steps X <- X (3I - X^T X) / 2, a <- a X, and double-float sweeps polish the
+// rotated matrix (its columns are then orthogonal to FP32 precision, so one
+// sweep squares that for well-separated singular values; directions whose
+// singular values FP32 cannot resolve need sweeps to convergence).
+// t1, t2: P*P double-float scratch.
 __device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* perm, int* flag, float* a32,
-                                 float* v32, float* sig32, dfloat* t1, dfloat* t2) {
+                                 float* v32, float* sig32, dfloat* t1, dfloat* t2, int polish_sweeps) {
   for (int o = threadIdx.x; o < P * P; o += NTS) a32[o] = a[o].hi + a[o].lo;
   __syncthreads();
-  const bool ok = jacobi_svd<float, NTS>(P, a32, v32, sig32, perm, flag);
+  // FP32 sweeps as a preconditioner: near FP32's resolution limit they need
+  // not converge (rotations between columns of very different size keep
+  // re-creating rounding-level products), so at most 12
+  jacobi_svd<float, NTS>(P, a32, v32, sig32, perm, flag, 12, false);
   for (int o = threadIdx.x; o < P * P; o += NTS) t1[o] = dfloat(v32[o], 0.0f);  // X0 = V32
   __syncthreads();
   for (int it = 0; it < 2; ++it) {
@@ -464,11 +486,122 @@ __device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* 
   sq_mul<dfloat>(P, a, false, t1, t2);                                               // a X
   for (int o = threadIdx.x; o < P * P; o += NTS) a[o] = t2[o];
   __syncthreads();
-  jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, 1);                              // polish: a = U S, V_p
+  const bool ok = jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, polish_sweeps);  // polish: a = U S, V_p
   sq_mul<dfloat>(P, t1, false, v, t2);                                               // V = X V_p
   for (int o = threadIdx.x; o < P * P; o += NTS) v[o] = t2[o];
   __syncthreads();
   return ok;
+}
+
+// Rank-revealing orthonormalisation factor of a Gram matrix G (a x a, ld a)
+// restricted to its leading r x r block (r = *rank: the panel's columns
+// beyond the rank are zero): Cholesky with diagonal pivoting of the scaled
+// Gram D G D (D = diag(G)^{-1/2}), D G D = Pi R^T R Pi^T, stopped when the
+// largest remaining diagonal entry (the squared distance of a unit column
+// from the span of those chosen) is <= tol_rel.  Bout (a x a, zero outside
+// the leading k x k block, k the revealed rank) = D Pi R^{-1}, so X Bout has
+// k orthonormal columns up to about (error of G) / tol_rel and zero columns
+// after them.  Columns whose squared norm is <= tol_rel of the largest are
+// rounding noise of the panel and are dropped before the scaling (which
+// would hide that).  Factor and inverse in shared memory (2 r^2 ST).
+template <typename ST>
+__global__ void __launch_bounds__(NTS) pchol_factor(int a, const double* __restrict__ G, const int32_t* rank,
+                                                    double tol_rel, double* __restrict__ Bout) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int r = min(a, (int)*rank);
+  ST* A = reinterpret_cast<ST*>(smraw);  // r x r, column-major
+  ST* Ri = A + r * r;                     // r x r
+  __shared__ double d[SMAX];
+  __shared__ int piv[SMAX];
+  __shared__ int pk_s, kk_s;
+  const int tid = threadIdx.x;
+  double gmax = 0.0;
+  for (int j = 0; j < r; ++j) gmax = fmax(gmax, G[j + (int64_t)j * a]);
+  for (int j = tid; j < r; j += NTS) {
+    const double g = G[j + (int64_t)j * a];
+    d[j] = (g > tol_rel * gmax && g > 0.0) ? 1.0 / sqrt(g) : 0.0;
+    piv[j] = j;
+  }
+  __syncthreads();
+  for (int o = tid; o < r * r; o += NTS) {
+    const int i = o % r, j = o / r;
+    A[o] = ST(d[i] * G[i + (int64_t)j * a] * d[j]);
+  }
+  if (tid == 0) kk_s = r;
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (tid < 32) {  // pivot: the largest remaining diagonal entry (first on ties)
+      double best = -1.0;
+      int bi = k;
+      for (int j = k + tid; j < r; j += 32) {
+        const double v = to_d(A[j + j * r]);
+        if (v > best) { best = v; bi = j; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        pk_s = bi;
+        if (!(best > tol_rel)) kk_s = k;
+      }
+    }
+    __syncthreads();
+    if (kk_s == k) break;
+    const int p = pk_s;
+    if (p != k) {  // symmetric swap of rows and columns k and p (R's rows above k: columns only)
+      for (int i = tid; i < r; i += NTS) {
+        const ST t = A[i + k * r];
+        A[i + k * r] = A[i + p * r];
+        A[i + p * r] = t;
+      }
+      __syncthreads();
+      for (int j = tid; j < r; j += NTS) {
+        const ST t = A[k + j * r];
+        A[k + j * r] = A[p + j * r];
+        A[p + j * r] = t;
+      }
+      if (tid == 0) {
+        const int t = piv[k];
+        piv[k] = piv[p];
+        piv[p] = t;
+      }
+      __syncthreads();
+    }
+    const ST rkk = sqrt(A[k + k * r]);
+    const ST inv = ST(1.0) / rkk;
+    for (int j = k + 1 + tid; j < r; j += NTS) A[k + j * r] = A[k + j * r] * inv;
+    __syncthreads();
+    if (tid == 0) A[k + k * r] = rkk;
+    // trailing update of the full symmetric block (rows and columns > k)
+    const int cnt = r - k - 1;
+    for (int e = tid; e < cnt * cnt; e += NTS) {
+      const int i = k + 1 + e % cnt, j = k + 1 + e / cnt;
+      A[i + j * r] = A[i + j * r] - A[k + i * r] * A[k + j * r];
+    }
+    __syncthreads();
+  }
+  const int kk = kk_s;
+  // R^{-1} (kk x kk) row by row from the bottom (one barrier per row)
+  for (int o = tid; o < r * r; o += NTS) Ri[o] = ST(0.0);
+  __syncthreads();
+  for (int i = kk - 1; i >= 0; --i) {
+    const ST rii = ST(1.0) / A[i + i * r];
+    for (int j = i + tid; j < kk; j += NTS) {
+      ST sacc = (i == j) ? ST(1.0) : ST(0.0);
+      for (int q = i + 1; q <= j; ++q) sacc = sacc - A[i + q * r] * Ri[q + j * r];
+      Ri[i + j * r] = sacc * rii;
+    }
+    __syncthreads();
+  }
+  for (int o = tid; o < a * a; o += NTS) Bout[o] = 0.0;
+  __syncthreads();
+  for (int o = tid; o < kk * kk; o += NTS) {
+    const int i = o % kk, j = o / kk;
+    const int pi = piv[i];
+    Bout[pi + (int64_t)j * a] = d[pi] * to_d(Ri[i + j * r]);
+  }
 }
 
 // S-step core and truncation.  In: Mh = Uhat^T U0 (w x R), Nh = Vhat^T V0
@@ -520,8 +653,11 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     float* a32 = reinterpret_cast<float*>(mx);
     float* v32 = a32 + wa * wa;
     __shared__ float sig32[2 * SMAX];
+    // (double-float sweeps to convergence: kept singular values far below the
+    // largest are beyond what the FP32 sweeps resolve, and their left vectors
+    // a_j / sigma_j need the double-float accuracy)
     ok = jacobi_svd_mixed(wa, a, v, sig, perm, &flag, a32, v32, sig32,
-                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa);
+                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa, 40);
   } else {
     ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag);
   }
@@ -545,13 +681,14 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   }
   __syncthreads();
   const int r1 = r_new;
+  // left vectors a_j / sigma_j in place (P1 as scratch before it is written)
+  complete_left<ST, NTS>(wa, r1, a, sig, perm, reinterpret_cast<ST*>(P1));
   for (int o = tid; o < w * R; o += NTS) P1[o] = Q1[o] = 0.0;
   __syncthreads();
   for (int o = tid; o < wa * r1; o += NTS) {
     const int i = o % wa, j = o / wa;
     const int pj = perm[j];
-    const double sg = to_d(sig[pj]);
-    P1[idx(i) + (int64_t)j * w] = (sg > 0.0) ? to_d(a[i + (int64_t)pj * wa]) / sg : 0.0;
+    P1[idx(i) + (int64_t)j * w] = to_d(a[i + (int64_t)pj * wa]);
     Q1[idx(i) + (int64_t)j * w] = to_d(v[i + (int64_t)pj * wa]);
   }
   for (int o = tid; o < R * R; o += NTS) {
@@ -562,6 +699,282 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   bool bad = false;
   for (int o = tid; o < R * R; o += NTS) bad |= !isfinite((double)S0[o]);
   if (__syncthreads_or(bad) && tid == 0) atomicOr(status, ST_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// Periodic Burgers flow on one large instance, spread over the GPU (the
+// multi-CTA form of the batch engine's burgers_contract):
+//   Y = XL ZR^T (N x M, rows = grid points), F(Y) = (Dxx Y) diag(nu)
+//   + alpha (Dx Y).*Y + beta Dx(Y.*Y), periodic central differences.
+// burg_rows: part[cs] (N x k) = F(rows of tile) ZR(columns of split cs), or,
+//   with CL, part[cta] (p x k, FP64) = CL(rows)^T F ZR(columns of split cs);
+// burg_cols: out (M x k) = F^T XL, complete per column tile.
+// Y and F exist only as 32 x 32 shared-memory tiles (with a periodic halo
+// row on each side).  k, p <= 128.
+// ---------------------------------------------------------------------------
+constexpr int BNACC = 16;  // accumulators per thread: 32 x 128 / 256
+
+template <typename T>
+__device__ __forceinline__ void burg_stage_x(int N, int k, const T* XL, int i0, int rows, T* xs, int ldk) {
+  for (int e = threadIdx.x; e < (rows + 2) * k; e += 256) {
+    const int ii = e % (rows + 2), a = e / (rows + 2);
+    int g = i0 - 1 + ii;
+    g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
+    xs[ii * ldk + a] = XL[g + (int64_t)a * N];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void burg_stage_z(int M, int k, const T* ZR, const T* nu, int j0, int cols, T* zs,
+                                             T* nus, int ldk) {
+  for (int e = threadIdx.x; e < 32 * k; e += 256) {
+    const int jj = e % 32, a = e / 32;
+    zs[jj * ldk + a] = (jj < cols) ? ZR[(j0 + jj) + (int64_t)a * M] : T(0);
+  }
+  for (int jj = threadIdx.x; jj < 32; jj += 256) nus[jj] = (jj < cols) ? nu[j0 + jj] : T(0);
+}
+
+// Y tile (rows+2 x 32) then F tile (rows x 32, ld 33)
+template <typename T>
+__device__ __forceinline__ void burg_flow_tile(int k, int rows, const T* xs, const T* zs, const T* nus, T* ys,
+                                               T* fs, int ldk, T ih2, T ihx, T al, T be) {
+  for (int o = threadIdx.x; o < (rows + 2) * 32; o += 256) {
+    const int ii = o >> 5, jj = o & 31;
+    T acc = T(0);
+    for (int a = 0; a < k; ++a) acc = fma(xs[ii * ldk + a], zs[jj * ldk + a], acc);
+    ys[o] = acc;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < rows * 32; o += 256) {
+    const int ii = o >> 5, jj = o & 31;
+    const T ym = ys[ii * 32 + jj], y0 = ys[(ii + 1) * 32 + jj], yp = ys[(ii + 2) * 32 + jj];
+    T f = nus[jj] * (((ym + yp) - (y0 + y0)) * ih2);
+    f = fma(al * ((yp - ym) * ihx), y0, f);
+    f = fma(be, (yp * yp - ym * ym) * ihx, f);
+    fs[ii * 33 + jj] = f;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) burg_rows(int N, int M, int k, int csplit, const T* __restrict__ XL,
+                                                 const T* __restrict__ ZR, const T* __restrict__ nu, double h,
+                                                 double alpha, double beta, const T* __restrict__ CL, int p,
+                                                 T* __restrict__ part, double* __restrict__ spart) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ldk = k + 1, ldp = p + 1;
+  T* xs = reinterpret_cast<T*>(smraw);  // 34 x ldk
+  T* zs = xs + 34 * ldk;                // 32 x ldk
+  T* ys = zs + 32 * ldk;                // 34 x 32
+  T* fs = ys + 34 * 32;                 // 32 x 33
+  T* nus = fs + 32 * 33;                // 32
+  T* cs = nus + 32;                     // 32 x ldp (CL rows)
+  T* ts = cs + 32 * ldp;                // 32 x ldk ((F ZR) rows)
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * 32, rows = min(32, N - i0);
+  const int cs_id = blockIdx.y;
+  const int per = (M + csplit - 1) / csplit;
+  const int c0 = cs_id * per, c1 = min(M, c0 + per);
+  const T ih2 = T(1.0 / (h * h)), ihx = T(0.5 / h), al = T(alpha), be = T(beta);
+  T acc[BNACC];
+#pragma unroll
+  for (int u = 0; u < BNACC; ++u) acc[u] = T(0);
+  burg_stage_x(N, k, XL, i0, rows, xs, ldk);
+  for (int j0 = c0; j0 < c1; j0 += 32) {
+    const int cols = min(32, c1 - j0);
+    burg_stage_z(M, k, ZR, nu, j0, cols, zs, nus, ldk);
+    __syncthreads();
+    burg_flow_tile(k, rows, xs, zs, nus, ys, fs, ldk, ih2, ihx, al, be);
+#pragma unroll
+    for (int u = 0; u < BNACC; ++u) {
+      const int o = tid + u * 256;
+      if (o < 32 * k) {
+        const int i = o & 31, c = o >> 5;
+        if (i < rows) {
+          T sacc = acc[u];
+          for (int jj = 0; jj < cols; ++jj) sacc = fma(fs[i * 33 + jj], zs[jj * ldk + c], sacc);
+          acc[u] = sacc;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!CL) {
+    T* dst = part + (int64_t)cs_id * N * k;
+#pragma unroll
+    for (int u = 0; u < BNACC; ++u) {
+      const int o = tid + u * 256;
+      if (o < 32 * k) {
+        const int i = o & 31, c = o >> 5;
+        if (i < rows) dst[(i0 + i) + (int64_t)c * N] = acc[u];
+      }
+    }
+    return;
+  }
+  // part (p x k, FP64) = CL(rows)^T (F ZR)(rows)
+#pragma unroll
+  for (int u = 0; u < BNACC; ++u) {
+    const int o = tid + u * 256;
+    if (o < 32 * k) {
+      const int i = o & 31, c = o >> 5;
+      ts[i * ldk + c] = (i < rows) ? acc[u] : T(0);
+    }
+  }
+  for (int e = tid; e < 32 * p; e += 256) {
+    const int ii = e & 31, a = e >> 5;
+    cs[ii * ldp + a] = (ii < rows) ? CL[(i0 + ii) + (int64_t)a * N] : T(0);
+  }
+  __syncthreads();
+  double* dst = spart + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * p * k;
+  for (int o = tid; o < p * k; o += 256) {
+    const int a = o % p, c = o / p;
+    double sacc = 0.0;
+    for (int ii = 0; ii < rows; ++ii) sacc = fma((double)cs[ii * ldp + a], (double)ts[ii * ldk + c], sacc);
+    dst[o] = sacc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) burg_cols(int N, int M, int k, const T* __restrict__ XL,
+                                                 const T* __restrict__ ZR, const T* __restrict__ nu, double h,
+                                                 double alpha, double beta, T* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ldk = k + 1;
+  T* xs = reinterpret_cast<T*>(smraw);
+  T* zs = xs + 34 * ldk;
+  T* ys = zs + 32 * ldk;
+  T* fs = ys + 34 * 32;
+  T* nus = fs + 32 * 33;
+  const int tid = threadIdx.x;
+  const int j0 = blockIdx.x * 32, cols = min(32, M - j0);
+  const T ih2 = T(1.0 / (h * h)), ihx = T(0.5 / h), al = T(alpha), be = T(beta);
+  T acc[BNACC];
+#pragma unroll
+  for (int u = 0; u < BNACC; ++u) acc[u] = T(0);
+  burg_stage_z(M, k, ZR, nu, j0, cols, zs, nus, ldk);
+  for (int i0 = 0; i0 < N; i0 += 32) {
+    const int rows = min(32, N - i0);
+    burg_stage_x(N, k, XL, i0, rows, xs, ldk);
+    __syncthreads();
+    burg_flow_tile(k, rows, xs, zs, nus, ys, fs, ldk, ih2, ihx, al, be);
+    // acc(jj, c) += sum_ii F(ii, jj) XL(i0+ii, c)
+#pragma unroll
+    for (int u = 0; u < BNACC; ++u) {
+      const int o = tid + u * 256;
+      if (o < 32 * k) {
+        const int jj = o & 31, c = o >> 5;
+        T sacc = acc[u];
+        for (int ii = 0; ii < rows; ++ii) sacc = fma(fs[ii * 33 + jj], xs[(ii + 1) * ldk + c], sacc);
+        acc[u] = sacc;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < BNACC; ++u) {
+    const int o = tid + u * 256;
+    if (o < 32 * k) {
+      const int jj = o & 31, c = o >> 5;
+      if (jj < cols) out[(j0 + jj) + (int64_t)c * M] = acc[u];
+    }
+  }
+}
+
+// out (len) = sum_{c < cs} part[c * len + .]
+template <typename T>
+__global__ void sum_parts(int64_t len, int cs, const T* __restrict__ part, T* __restrict__ out) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    T s = part[o];
+    for (int c = 1; c < cs; ++c) s += part[(int64_t)c * len + o];
+    out[o] = s;
+  }
+}
+
+// y = a x + b z (z may be null), element-wise over len
+template <typename T>
+__global__ void axpbz(int64_t len, T a, const T* __restrict__ x, T b, const T* __restrict__ z, T* __restrict__ y) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x)
+    y[o] = z ? fma(b, z[o], a * x[o]) : a * x[o];
+}
+
+// small FP64 helpers of the S step: X (R x R, T, ld R) -> Y (FP64, ld R), optionally transposed
+template <typename T>
+__global__ void small_to_f64(int R, const T* __restrict__ X, int trans, double* __restrict__ Y) {
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < R * R; o += gridDim.x * blockDim.x) {
+    const int i = o % R, j = o / R;
+    Y[o] = (double)(trans ? X[j + (int64_t)i * R] : X[o]);
+  }
+}
+
+// S~0 (w x w) = Mh S0 Nh^T with Mh, Nh (w x R), S0 (R x R, FP64)
+__global__ void small_msn(int w, int R, const double* __restrict__ Mh, const double* __restrict__ S0,
+                          const double* __restrict__ Nh, double* __restrict__ tmp, double* __restrict__ out) {
+  for (int o = threadIdx.x; o < R * w; o += blockDim.x) {
+    const int i = o % R, j = o / R;
+    double s = 0.0;
+    for (int kk = 0; kk < R; ++kk) s = fma(S0[i + (int64_t)kk * R], Nh[j + (int64_t)kk * w], s);
+    tmp[i + (int64_t)j * R] = s;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < w * w; o += blockDim.x) {
+    const int i = o % w, j = o / w;
+    double s = 0.0;
+    for (int kk = 0; kk < R; ++kk) s = fma(Mh[i + (int64_t)kk * w], tmp[kk + (int64_t)j * R], s);
+    out[o] = s;
+  }
+}
+
+// One Newton-Schulz step towards orthonormal factors without changing
+// Y = U S V^T: with Gu = U^T U = I + Eu (and Gv likewise) on the active
+// r x r block, Xu = (3I - Gu) / 2 (U <- U Xu has U^T U = I + O(Eu^2)) and
+// S <- (I + Eu/2) S (I + Ev/2)^T, the inverse of Xu to first order.
+// Identity outside the active block.  Eu and Ev are at the rounding level
+// of FP32 panels, so the corrections Eu S and S Ev^T are accumulated in
+// FP32 (relative error u32 of a u32-sized term) from shared-memory copies;
+// S is updated in FP64 before its final rounding.  One CTA; dynamic shared
+// memory 3 r^2 floats.
+__global__ void ns_refresh(int R, const int32_t* __restrict__ rank, const double* __restrict__ Gu,
+                           const double* __restrict__ Gv, double* __restrict__ Xu, double* __restrict__ Xv,
+                           float* __restrict__ S, double* __restrict__ tmp) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int r = min(R, (int)*rank);
+  float* E = reinterpret_cast<float*>(smraw);  // r x r: Eu / 2, then Ev / 2
+  float* Sf = E + r * r;                        // r x r: S, then tmp
+  float* Cf = Sf + r * r;                       // r x r: correction
+  for (int o = threadIdx.x; o < R * R; o += blockDim.x) {
+    const int i = o % R, j = o / R;
+    const bool act = i < r && j < r;
+    const double id = (i == j) ? 1.0 : 0.0;
+    Xu[o] = act ? 0.5 * (3.0 * id - Gu[o]) : id;
+    Xv[o] = act ? 0.5 * (3.0 * id - Gv[o]) : id;
+  }
+  for (int o = threadIdx.x; o < r * r; o += blockDim.x) {
+    const int i = o % r, j = o / r;
+    E[o] = (float)(0.5 * (Gu[i + (int64_t)j * R] - ((i == j) ? 1.0 : 0.0)));
+    Sf[o] = S[i + (int64_t)j * R];
+  }
+  __syncthreads();
+  // tmp = S + (Eu/2) S
+  for (int o = threadIdx.x; o < r * r; o += blockDim.x) {
+    const int i = o % r, j = o / r;
+    float c = 0.0f;
+    for (int k = 0; k < r; ++k) c = fmaf(E[i + k * r], Sf[k + j * r], c);
+    tmp[i + (int64_t)j * R] = (double)Sf[o] + (double)c;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < r * r; o += blockDim.x) {
+    const int i = o % r, j = o / r;
+    E[o] = (float)(0.5 * (Gv[i + (int64_t)j * R] - ((i == j) ? 1.0 : 0.0)));
+    Sf[o] = (float)tmp[i + (int64_t)j * R];
+  }
+  __syncthreads();
+  // S = tmp + tmp (Ev/2)^T
+  for (int o = threadIdx.x; o < r * r; o += blockDim.x) {
+    const int i = o % r, j = o / r;
+    float c = 0.0f;
+    for (int k = 0; k < r; ++k) c = fmaf(Sf[i + k * r], E[j + k * r], c);
+    S[i + (int64_t)j * R] = (float)(tmp[i + (int64_t)j * R] + (double)c);
+  }
 }
 
 }  // namespace
@@ -589,13 +1002,23 @@ struct lri_stream {
   void* Zp = nullptr;   // max(n, m) x 2R (dY Vhat; scratch of the orthonormalisation)
   double* part = nullptr;
   double* small = nullptr;
+  // Burgers flow (lri_burgers_create): parameters and RK work panels
+  bool burgers = false;
+  double bh = 0.0, balpha = 0.0, bbeta = 0.0, bh_dt = 0.0;
+  lri::Scheme sc{};
+  const void* nu = nullptr;
+  void* Kp = nullptr;      // n x R x 4: y, stage input, stage derivative, accumulator
+  void* Lp = nullptr;      // m x R x 4
+  void* kpart = nullptr;   // kCS x n x R partial K-stage derivatives
+  double* spart = nullptr; // (n/32 * kCS) x (2R)^2 partial S-stage derivatives
 };
 
 
 namespace lri {
 namespace {
 
-constexpr int kBlocksSmall = 16;  // FP64 scratch of (2R)^2 each
+constexpr int kBlocksSmall = 24;  // FP64 scratch of (2R)^2 each (14, 15, 23: refresh; 16..22: the Burgers S step)
+constexpr int kCS = 4;            // column splits of the K-side Burgers contraction
 
 template <typename T>
 struct StreamOps {
@@ -618,21 +1041,34 @@ struct StreamOps {
     panel_mul<T><<<grid, 256, 0, st>>>(N, a, c, X, ldx, B, ldb, beta, out, ldo);
     return cudaGetLastError();
   }
-  using ST = typename SmallT<T>::type;
-  static size_t svqb_smem(int a) {
-    return (size_t)(2 * a * a + a) * sizeof(ST) + (size_t)a * sizeof(double) + (size_t)(a + 2) * sizeof(int);
+  // X B for factors with large entries: double-float sums for FP32 panels
+  cudaError_t mul_precise(int N, int a, int c, const T* X, int ldx, const double* B, int ldb, T* out,
+                          int ldo) const {
+    if constexpr (std::is_same<T, float>::value) {
+      dim3 grid((N + 31) / 32, (c + 63) / 64);
+      panel_mul_df<<<grid, 256, 0, st>>>(N, a, c, X, ldx, B, ldb, out, ldo);
+      return cudaGetLastError();
+    } else {
+      return mul(N, a, c, X, ldx, B, ldb, T(0), out, ldo);
+    }
   }
-  cudaError_t svqb(int a, const double* G, double* B) const {
+  using ST = typename SmallT<T>::type;
+  cudaError_t pchol(int a, const double* G, double* B) const {
     static bool attr_set = false;
     if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(svqb_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)svqb_smem(SMAX));
+      cudaError_t e = cudaFuncSetAttribute(pchol_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(2 * SMAX * SMAX * sizeof(ST)));
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    // eigenvalues below 1e-26 of the largest are rounding noise of the Gram
-    // (double-float or FP64 sums of exact products)
-    svqb_factor<ST><<<1, NTS, svqb_smem(a), st>>>(a, G, s->d_rank, 1e-26, B);
+    // directions whose squared distance from the span of the others (unit
+    // columns) is below tol_rel are treated as dependent.  The columns of
+    // X B are orthonormal up to about (error of G) / tol_rel: about 1e-3 for
+    // FP32 panels (Gram and factor in double-float, ~1e-14; X B with
+    // double-float sums) and for FP64 panels (~1e-16), so that one
+    // CholeskyQR pass afterwards is well conditioned.
+    const double tol_rel = sizeof(T) == 4 ? 1e-11 : 1e-13;
+    pchol_factor<ST><<<1, NTS, 2 * (size_t)a * a * sizeof(ST), st>>>(a, G, s->d_rank, tol_rel, B);
     return cudaGetLastError();
   }
   cudaError_t cholinv(int a, const double* G, double* B, double shift_rel) const {
@@ -647,35 +1083,218 @@ struct StreamOps {
     chol_inv_factor<ST><<<1, NTS, smem, st>>>(a, G, 1e-20, shift_rel, B);
     return cudaGetLastError();
   }
+  // X <- X - Y0 (Y0^T X) for the orthonormal columns of Y0 (N x R)
+  cudaError_t project_out(int N, T* X, const T* Y0) const {
+    const int R = (int)s->R;
+    cudaError_t e = gram(N, R, R, Y0, N, X, N, 1.0, 0.0, blk(0), R);  // C = Y0^T X
+    if (e != cudaSuccess) return e;
+    // panel_mul computes Y0 (-C) + X
+    negate<<<(R * R + 255) / 256, 256, 0, st>>>(R * R, blk(0));
+    return mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
+  }
   // X (N x R) <- orthonormal basis of the part of X orthogonal to the
-  // orthonormal columns of Y0 (N x R); B blocks i0..i0+2 are scratch.
+  // orthonormal columns of Y0 (N x R); blocks 0..2 are scratch.  Block
+  // Gram-Schmidt with re-orthogonalisation: two projections, a
+  // rank-revealing pivoted Cholesky pass (dependent directions become zero
+  // columns), one more projection (the pivoted pass combines nearly
+  // dependent columns with large coefficients, which magnifies what is left
+  // of their Y0 components), then a plain CholeskyQR pass for orthogonality
+  // to the panel's precision.
   cudaError_t orth_against(int N, T* X, const T* Y0) const {
     const int R = (int)s->R;
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = project_out(N, X, Y0);
+    if (e == cudaSuccess) e = project_out(N, X, Y0);
     for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
-      e = gram(N, R, R, Y0, N, X, N, 1.0, 0.0, blk(0), R);                                // C = Y0^T X
-      if (e == cudaSuccess) {
-        // X <- X - Y0 C   (panel_mul computes Y0 (-C) + X)
-        negate<<<(R * R + 255) / 256, 256, 0, st>>>(R * R, blk(0));
-        e = mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
-      }
-    }
-    // shifted CholeskyQR3 (Fukaya et al., SIAM J. Sci. Comput. 2020): the
-    // first pass shifted by 11 (N a + a (a+1)) u tr(G) with u the Gram's
-    // rounding unit (double-float sums of exact FP32 products: 2^-44; FP64:
-    // 2^-53), then two plain passes
-    const double ug = sizeof(T) == 4 ? 5.7e-14 : 1.1e-16;
-    const double shift = 11.0 * ((double)N * R + (double)R * (R + 1)) * ug;
-    for (int pass = 0; pass < 3 && e == cudaSuccess; ++pass) {
-      e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);                                 // G = X^T X
-      if (e == cudaSuccess) e = cholinv(R, blk(1), blk(2), pass == 0 ? shift : 0.0);
-      if (e == cudaSuccess) e = mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);        // Z = X B
+      if (pass == 1) e = project_out(N, X, Y0);
+      if (e == cudaSuccess) e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);         // G = X^T X
+      if (e == cudaSuccess) e = (pass == 0) ? pchol(R, blk(1), blk(2)) : cholinv(R, blk(1), blk(2), 0.0);
+      if (e == cudaSuccess)
+        e = (pass == 0) ? mul_precise(N, R, R, X, N, blk(2), R, tp(s->Zp), N)            // Z = X B
+                        : mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);
       if (e == cudaSuccess) {
         copy_cols<T><<<304, 256, 0, st>>>(N, R, tp(s->Zp), N, X, N);
         e = cudaGetLastError();
       }
     }
     return e;
+  }
+
+  static size_t burg_smem(int k, int p) {
+    return (size_t)(34 * (k + 1) + 32 * (k + 1) + 34 * 32 + 32 * 33 + 32 + 32 * (p + 1) + 32 * (k + 1)) * sizeof(T);
+  }
+  cudaError_t burg_attr() const {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    const int mx = (int)burg_smem(128, 128);
+    cudaError_t e = cudaFuncSetAttribute(burg_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(burg_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    done = (e == cudaSuccess);
+    return e;
+  }
+  // one RK substep sequence of a panel flow y' = f(y) (N x R): y in P[0],
+  // stage input P[1], derivative P[2], accumulator P[3]; f writes P[2].
+  template <class F>
+  cudaError_t rk_panel(int64_t len, T* P, const F& f) const {
+    const Scheme& sc = s->sc;
+    const T h = T(s->bh_dt / sc.nsub);
+    T* y = P;
+    T* z = P + len;
+    T* k = P + 2 * len;
+    T* acc = P + 3 * len;
+    const int g = 304;
+    cudaError_t e = cudaSuccess;
+    for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
+      for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
+        if ((e = f(st_ == 0 ? y : z, k)) != cudaSuccess) break;
+        if (st_ == 0) axpbz<T><<<g, 256, 0, st>>>(len, T(sc.b[0]), k, T(0), nullptr, acc);
+        else axpbz<T><<<g, 256, 0, st>>>(len, T(1), acc, T(sc.b[st_]), k, acc);
+        if (st_ + 1 < sc.nstages) axpbz<T><<<g, 256, 0, st>>>(len, T(1), y, T(h * T(sc.a[st_ + 1])), k, z);
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) {
+        axpbz<T><<<g, 256, 0, st>>>(len, T(1), y, h, acc, y);
+        e = cudaGetLastError();
+      }
+    }
+    return e;
+  }
+
+  // FP32 panels: U and V are reused from step to step as the first half of
+  // the augmented bases, so their rounding-level loss of orthogonality
+  // (~u32 per step) would accumulate; one Newton-Schulz step per step keeps
+  // it at u32.  (FP64 panels: u64 per step, left alone.)
+  cudaError_t refresh() const {
+    if constexpr (!std::is_same<T, float>::value) return cudaSuccess;
+    const int n = (int)s->n, m = (int)s->m, R = (int)s->R;
+    T* U = tp(s->U);
+    T* V = tp(s->V);
+    double* Gu = blk(14);
+    double* Gv = blk(15);
+    double* Xu = Gu + (int64_t)R * R;
+    double* Xv = Gv + (int64_t)R * R;
+    cudaError_t e = gram(n, R, R, U, n, U, n, 1.0, 0.0, Gu, R);
+    if (e == cudaSuccess) e = gram(m, R, R, V, m, V, m, 1.0, 0.0, Gv, R);
+    if (e != cudaSuccess) return e;
+    static bool attr_set = false;
+    if (!attr_set) {
+      e = cudaFuncSetAttribute(ns_refresh, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(3 * SMAX * SMAX * sizeof(float)));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    ns_refresh<<<1, 1024, 3 * (size_t)R * R * sizeof(float), st>>>(R, s->d_rank, Gu, Gv, Xu, Xv,
+                                                                  reinterpret_cast<float*>(s->S), blk(23));
+    if ((e = mul(n, R, R, U, n, Xu, R, T(0), tp(s->Zp), n)) != cudaSuccess) return e;
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, tp(s->Zp), n, U, n);
+    if ((e = mul(m, R, R, V, m, Xv, R, T(0), tp(s->Zp), m)) != cudaSuccess) return e;
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, tp(s->Zp), m, V, m);
+    return cudaGetLastError();
+  }
+
+  cudaError_t burgers_step() const {
+    const int n = (int)s->n, m = (int)s->m, R = (int)s->R, w = 2 * R;
+    T* U = tp(s->U);
+    T* V = tp(s->V);
+    T* S = tp(s->S);
+    T* Uh = tp(s->Uh);
+    T* Vh = tp(s->Vh);
+    T* Xk = tp(s->Xk);
+    T* Xl = tp(s->Xl);
+    const T* nu = static_cast<const T*>(s->nu);
+    const double bh = s->bh, ba = s->balpha, bb = s->bbeta;
+    cudaError_t e = burg_attr();
+    if (e == cudaSuccess) e = refresh();
+    if (e != cudaSuccess) return e;
+    small_to_f64<T><<<16, 256, 0, st>>>(R, S, 0, blk(16));
+    small_to_f64<T><<<16, 256, 0, st>>>(R, S, 1, blk(17));
+    // K step: K0 = U0 S0, K' = F(K V0^T) V0
+    T* Kp = tp(s->Kp);
+    if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
+    const int ntile = (n + 31) / 32;
+    e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, T* out) {
+      burg_rows<T><<<dim3(ntile, kCS), 256, burg_smem(R, 0), st>>>(n, m, R, kCS, Z, V, nu, bh, ba, bb, nullptr, 0,
+                                                                    tp(s->kpart), nullptr);
+      sum_parts<T><<<304, 256, 0, st>>>((int64_t)n * R, kCS, tp(s->kpart), out);
+      return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    // L step: L0 = V0 S0^T, L' = F(U0 L^T)^T U0
+    T* Lp = tp(s->Lp);
+    if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
+    e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, T* out) {
+      burg_cols<T><<<(m + 31) / 32, 256, burg_smem(R, 0), st>>>(n, m, R, U, Z, nu, bh, ba, bb, out);
+      return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    // augmented bases Uhat = [U0 | orth((I - U0 U0^T) K1)], Vhat likewise
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, Kp, n, Xk, n);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, Lp, m, Xl, m);
+    if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
+    if ((e = orth_against(m, Xl, V)) != cudaSuccess) return e;
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, U, n, Uh, n);
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, Xk, n, Uh + (int64_t)R * n, n);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, V, m, Vh, m);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, Vh + (int64_t)R * m, m);
+    if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
+    if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
+    // S step on the augmented bases from S~0 = Mh S0 Nh^T (FP64 w x w):
+    // S' = Uhat^T F(Uhat S Vhat^T) Vhat, stage inputs formed as Uhat Z
+    small_msn<<<1, 1024, 0, st>>>(w, R, blk(3), blk(16), blk(4), blk(22), blk(18));
+    {
+      const Scheme& sc = s->sc;
+      const double h = s->bh_dt / sc.nsub;
+      double* Sy = blk(18);
+      double* Sz = blk(19);
+      double* Sk = blk(20);
+      double* Sa = blk(21);
+      const int64_t len = (int64_t)w * w;
+      const int nct = ntile * 2;  // two column splits
+      for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
+        for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
+          const double* Z = (st_ == 0) ? Sy : Sz;
+          if ((e = mul(n, w, w, Uh, n, Z, w, T(0), tp(s->Zp), n)) != cudaSuccess) break;
+          burg_rows<T><<<dim3(ntile, 2), 256, burg_smem(w, w), st>>>(n, m, w, 2, tp(s->Zp), Vh, nu, bh, ba, bb, Uh,
+                                                                     w, nullptr, s->spart);
+          sum_parts<double><<<64, 256, 0, st>>>(len, nct, s->spart, Sk);
+          if (st_ == 0) axpbz<double><<<64, 256, 0, st>>>(len, sc.b[0], Sk, 0.0, nullptr, Sa);
+          else axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sa, sc.b[st_], Sk, Sa);
+          if (st_ + 1 < sc.nstages) axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sy, h * sc.a[st_ + 1], Sk, Sz);
+          e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+          axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sy, h, Sa, Sy);
+          e = cudaGetLastError();
+        }
+      }
+      if (e != cudaSuccess) return e;
+    }
+    // SVD and truncation of S~1 (core_step with Mh = Nh = 0 and D = S~1)
+    cudaMemsetAsync(blk(3), 0, sizeof(double) * (size_t)w * R, st);
+    cudaMemsetAsync(blk(4), 0, sizeof(double) * (size_t)w * R, st);
+    cudaMemcpyAsync(blk(5), blk(18), sizeof(double) * (size_t)w * w, cudaMemcpyDeviceToDevice, st);
+    if ((e = core(w)) != cudaSuccess) return e;
+    if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
+    return mul(m, w, R, Vh, m, blk(9), w, T(0), V, m);
+  }
+
+  cudaError_t core(int w) const {
+    const int R = (int)s->R;
+    T* S = tp(s->S);
+    cudaError_t e;
+    // the active 2r x 2r matrix in shared memory when it fits (200 KB)
+    const int abytes = 200 * 1024;
+    static bool attr_set = false;
+    if (!attr_set) {
+      if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+          cudaSuccess)
+        return e;
+      attr_set = true;
+    }
+    ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
+    // blocks 10..12: FP32 copies and double-float products of the mixed-precision SVD
+    core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, scr,
+                                             scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes, blk(10));
+    return cudaGetLastError();
   }
 
   cudaError_t step(const T* A0, const T* A1) const {
@@ -687,7 +1306,8 @@ struct StreamOps {
     T* Vh = tp(s->Vh);
     T* Xk = tp(s->Xk);
     T* Xl = tp(s->Xl);
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = refresh();
+    if (e != cudaSuccess) return e;
     // data passes 1 and 2: dY V0, dY^T U0
     pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, A1, A0, V, m, Xk);
     pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, A1, A0, U, n, Xl);
@@ -705,22 +1325,7 @@ struct StreamOps {
     // data pass 3: Z = dY Vhat; D = Uhat^T Z
     pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, w, A1, A0, Vh, m, tp(s->Zp));
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
-    {
-      // the active 2r x 2r matrix in shared memory when it fits (200 KB)
-      const int abytes = 200 * 1024;
-      static bool attr_set = false;
-      if (!attr_set) {
-        if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-            cudaSuccess)
-          return e;
-        attr_set = true;
-      }
-      ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
-      // blocks 10..13: FP32 copies and double-float products of the mixed-precision SVD
-      core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, scr,
-                                               scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes, blk(10));
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = core(w)) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
     if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
     return mul(m, w, R, Vh, m, blk(9), w, T(0), V, m);
@@ -774,8 +1379,70 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   return LRI_OK;
 }
 
+lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0, int64_t r_max,
+                              double tol, int32_t r_min, double h, double alpha, double beta,
+                              const lri_scheme* scheme) {
+  if (!out || !scheme) return LRI_ERR_ARG;
+  *out = nullptr;
+  if (r_max > 64) return LRI_ERR_ARG;  // the flow tiles take panels of at most 2 r_max = 128 columns
+  if (!(h > 0.0) || !std::isfinite(h) || !std::isfinite(alpha) || !std::isfinite(beta)) return LRI_ERR_ARG;
+  if (scheme->nstages < 1 || scheme->nstages > 4 || scheme->nsub < 1) return LRI_ERR_ARG;
+  lri_status st = lri_stream_create(out, dtype, n, m, r0, r_max, tol, r_min);
+  if (st != LRI_OK) return st;
+  lri_stream* s = *out;
+  s->burgers = true;
+  s->bh = h;
+  s->balpha = alpha;
+  s->bbeta = beta;
+  s->sc.nstages = scheme->nstages;
+  s->sc.nsub = scheme->nsub;
+  for (int i = 0; i < 4; ++i) {
+    s->sc.a[i] = scheme->a[i];
+    s->sc.b[i] = scheme->b[i];
+    s->sc.c[i] = scheme->c[i];
+  }
+  const int64_t R = r_max, ntile = (n + 31) / 32;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes < 16 ? 16 : bytes);
+  };
+  alloc(&s->Kp, s->es * n * R * 4);
+  alloc(&s->Lp, s->es * m * R * 4);
+  alloc(&s->kpart, s->es * kCS * n * R);
+  alloc((void**)&s->spart, sizeof(double) * ntile * 2 * 4 * R * R);
+  if (e != cudaSuccess) {
+    lri_stream_destroy(s);
+    *out = nullptr;
+    return LRI_ERR_CUDA;
+  }
+  return LRI_OK;
+}
+
+lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void* nu) {
+  if (!s || !s->burgers || !nu) return LRI_ERR_ARG;
+  s->nu = nu;
+  return lri_stream_bind(s, U, S, V);
+}
+
+lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stream) {
+  if (!s || !s->burgers || nsteps < 0 || !std::isfinite(dt)) return LRI_ERR_ARG;
+  if (!s->bound || !s->nu) return LRI_ERR_STATE;
+  s->bh_dt = dt;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
+    if (s->dtype == LRI_F32) e = StreamOps<float>{s, st}.burgers_step();
+    else e = StreamOps<double>{s, st}.burgers_step();
+  }
+  return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
+}
+
 lri_status lri_stream_destroy(lri_stream* s) {
   if (!s) return LRI_ERR_ARG;
+  cudaFree(s->Kp);
+  cudaFree(s->Lp);
+  cudaFree(s->kpart);
+  cudaFree(s->spart);
   cudaFree(s->d_rank);
   cudaFree(s->d_status);
   cudaFree(s->Uh);

@@ -167,6 +167,37 @@ def burgers_uq(n: int, m: int, seed: int = 3):
     return 1.0 / n, nu, X0
 
 
+def burgers_uq_factors(n: int, m: int, r: int, seed: int = 3):
+    """The initial data of ``burgers_uq`` (same seed, same samples) as an
+    SVD-like rank-r factorisation without forming X0: X0 = B C^T with
+    B = [sin 2 pi x, sin 4 pi x, cos 4 pi x] and C = [1, a cos phi, a sin phi]
+    (exact rank 3), thin QR of both and the SVD of the 3 x 3 core; the
+    columns 4..r of U and V complete them with seeded orthonormal directions
+    at singular value 0.  Returns (h, nu, U, s, V)."""
+    g = np.random.default_rng(seed)
+    x = np.arange(n) / n
+    nu = g.uniform(0.005, 0.02, m)
+    a = g.uniform(0.0, 0.5, m)
+    phi = g.uniform(0.0, 2 * np.pi, m)
+    B = np.stack([np.sin(2 * np.pi * x), np.sin(4 * np.pi * x), np.cos(4 * np.pi * x)], axis=1)
+    C = np.stack([np.ones(m), a * np.cos(phi), a * np.sin(phi)], axis=1)
+    Qb, Rb = np.linalg.qr(B)
+    Qc, Rc = np.linalg.qr(C)
+    P, s3, Qt = np.linalg.svd(Rb @ Rc.T)
+    g2 = np.random.default_rng(seed + 1000)
+
+    def complete(Q):
+        Z = g2.standard_normal((Q.shape[0], r - 3))
+        for _ in range(2):
+            Z -= Q @ (Q.T @ Z)
+        return np.hstack([Q, np.linalg.qr(Z)[0]])
+
+    U = complete(Qb @ P)
+    V = complete(Qc @ Qt.T)
+    s = np.concatenate([s3, np.zeros(r - 3)])
+    return 1.0 / n, nu, U, s, V
+
+
 def data_stream_device(n: int, m: int, nsnap: int, seed: int = 2, K: int = 64, sub: int = 128,
                        noise: float = 1e-4, dtype=None, device="cuda"):
     """The data-compression stream of ``data_stream`` generated on the device
