@@ -393,11 +393,18 @@ def run_burgers(args):
         tcpu.append(time.perf_counter() - t0)
     cpu_step = (m / ms_cols) * (tcpu[0] + (nsub - 1) * max(tcpu[1] - tcpu[0], 0.0))
 
-    # flow contractions of one step at rank r: every RK stage of the K and L
-    # substeps forms the r-column tiles of K V^T and contracts F with V
-    # (2 n m r FMA each), of the S substep the same with 2r columns
+    # flops of the structured flow at active rank r (w = 2r, pairs P(k) =
+    # k (k + 1) / 2), per RK stage: K substep (Dxx K) N_nu and KR(K, K) T'_V
+    # (n r^2 + n P(r) r multiply-adds), L substep the same over m rows, S
+    # substep A = Uhat S and Uhat^T M (2 n w^2), A_xx S N_nu (2 w^3) and
+    # KR(A, A) T'_Vhat (n P(w) w); once per step the tensors T'_V, T'_L
+    # (m P(r) r, n P(r) r) and T'_Vhat (m P(w) w)
     def step_flops(r):
-        return nsub * 4 * (2 * n * m * r * 2 + 2 * n * m * (2 * r)) * 2.0
+        P = lambda k: k * (k + 1) // 2
+        w = 2 * r
+        stage = (n * r * r + n * P(r) * r) + (m * r * r + m * P(r) * r) + (2 * n * w * w + 2 * w ** 3 + n * P(w) * w)
+        once = m * P(r) * r + n * P(r) * r + m * P(w) * w
+        return 2.0 * (nsub * 4 * stage + once)
     achieved = step_flops(rank_end) / (ms * 1e-3) / 1e12
     line = {"metric": "rank-adaptive BUG steps/s (Burgers UQ, n=4096, m=16384, r 16..64)", "value": 1e3 / ms,
             "unit": "steps/s", "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": ms, "higher_is_better": True,

@@ -702,181 +702,315 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Periodic Burgers flow on one large instance, spread over the GPU (the
-// multi-CTA form of the batch engine's burgers_contract):
-//   Y = XL ZR^T (N x M, rows = grid points), F(Y) = (Dxx Y) diag(nu)
-//   + alpha (Dx Y).*Y + beta Dx(Y.*Y), periodic central differences.
-// burg_rows: part[cs] (N x k) = F(rows of tile) ZR(columns of split cs), or,
-//   with CL, part[cta] (p x k, FP64) = CL(rows)^T F ZR(columns of split cs);
-// burg_cols: out (M x k) = F^T XL, complete per column tile.
-// Y and F exist only as 32 x 32 shared-memory tiles (with a periodic halo
-// row on each side).  k, p <= 128.
+// Periodic Burgers flow on one large instance, spread over the GPU:
+//   F(Y) = (Dxx Y) diag(nu) + alpha (Dx Y).*Y + beta Dx(Y.*Y),
+// periodic central differences Dx = tridiag(-1, 0, 1) / 2h (Dx^T = -Dx),
+// Dxx = tridiag(1, -2, 1) / h^2 (symmetric), one column per sample.
+// The substep flows never form the N x M matrix Y.  With Y = K V^T:
+//   (Dxx Y) diag(nu) V      = (Dxx K) (V^T diag(nu) V)
+//   ((Dx Y).*Y) V, row i    = sum_{a,b} (Dx K)_ia K_ib T_V[a,b,:]
+//   (Y.*Y) V, row i         = sum_{a,b} K_ia K_ib T_V[a,b,:]
+// with the symmetric tensor T_V[a,b,c] = sum_j V_ja V_jb V_jc, formed once
+// per step.  The L and S substeps have the same structure (their tensors
+// below).  Per RK stage this costs O((N + M) r^3 / 2) against O(N M r) for
+// the dense tiles; the tensors cost O(M r^3 / 2) once per step.
+// Tensors are stored over packed pairs a <= b of the active columns (ka of
+// them: r, or 2r for the augmented bases, whose active columns are the first
+// r of each half), with the off-diagonal pairs counted twice:
+//   T'[p(a,b), c] = c_ab T[a,b,c],  c_ab = 1 (a = b), 2 (a < b),
+// and the Khatri-Rao rows KR(P,Q)_i,p(a,b) = (P_ia Q_ib + P_ib Q_ia) / 2, so
+// sum_{a,b} P_ia Q_ib T[a,b,c] = sum_p KR(P,Q)_ip T'[p,c] for T symmetric
+// in (a,b).  All launch shapes depend on r_max only; the active rank is read
+// on the device, so a step is one fixed launch sequence.
 // ---------------------------------------------------------------------------
-constexpr int BNACC = 16;  // accumulators per thread: 32 x 128 / 256
+constexpr int KR_ROWS = 1024;  // rows per split of the tensor sums
 
-template <typename T>
-__device__ __forceinline__ void burg_stage_x(int N, int k, const T* XL, int i0, int rows, T* xs, int ldk) {
-  for (int e = threadIdx.x; e < (rows + 2) * k; e += 256) {
-    const int ii = e % (rows + 2), a = e / (rows + 2);
-    int g = i0 - 1 + ii;
-    g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
-    xs[ii * ldk + a] = XL[g + (int64_t)a * N];
-  }
+// active column j (0 <= j < ka) -> panel column: the first r of each half
+__device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
+__device__ __forceinline__ int active_cols(const int32_t* rank, int R, int aug) {
+  const int r = min(R, (int)*rank);
+  return aug ? 2 * r : r;
+}
+// packed pair p (0 <= p < ka (ka + 1) / 2) -> (a, b), a <= b < ka, row-wise:
+// pairs of a start at a ka - a (a - 1) / 2
+__device__ __forceinline__ void pair_ab(int p, int ka, int& a, int& b) {
+  const double q = 2.0 * ka + 1.0;
+  int x = (int)((q - sqrt(q * q - 8.0 * p)) * 0.5);
+  x = max(0, min(x, ka - 1));
+  while (x > 0 && x * ka - x * (x - 1) / 2 > p) --x;
+  while (x + 1 < ka && (x + 1) * ka - (x + 1) * x / 2 <= p) ++x;
+  a = x;
+  b = a + (p - (a * ka - a * (a - 1) / 2));
 }
 
+// part[s] (pairs x ka, ld PP) = sum over the rows of split s of
+// KR(P,Q)^T Y (active columns of Y).  Grid (pair tiles of 64, column tiles
+// of 64, row splits of KR_ROWS rows); tiles beyond the active sizes exit.
 template <typename T>
-__device__ __forceinline__ void burg_stage_z(int M, int k, const T* ZR, const T* nu, int j0, int cols, T* zs,
-                                             T* nus, int ldk) {
-  for (int e = threadIdx.x; e < 32 * k; e += 256) {
-    const int jj = e % 32, a = e / 32;
-    zs[jj * ldk + a] = (jj < cols) ? ZR[(j0 + jj) + (int64_t)a * M] : T(0);
-  }
-  for (int jj = threadIdx.x; jj < 32; jj += 256) nus[jj] = (jj < cols) ? nu[j0 + jj] : T(0);
-}
-
-// Y tile (rows+2 x 32) then F tile (rows x 32, ld 33)
-template <typename T>
-__device__ __forceinline__ void burg_flow_tile(int k, int rows, const T* xs, const T* zs, const T* nus, T* ys,
-                                               T* fs, int ldk, T ih2, T ihx, T al, T be) {
-  for (int o = threadIdx.x; o < (rows + 2) * 32; o += 256) {
-    const int ii = o >> 5, jj = o & 31;
-    T acc = T(0);
-    for (int a = 0; a < k; ++a) acc = fma(xs[ii * ldk + a], zs[jj * ldk + a], acc);
-    ys[o] = acc;
-  }
-  __syncthreads();
-  for (int o = threadIdx.x; o < rows * 32; o += 256) {
-    const int ii = o >> 5, jj = o & 31;
-    const T ym = ys[ii * 32 + jj], y0 = ys[(ii + 1) * 32 + jj], yp = ys[(ii + 2) * 32 + jj];
-    T f = nus[jj] * (((ym + yp) - (y0 + y0)) * ih2);
-    f = fma(al * ((yp - ym) * ihx), y0, f);
-    f = fma(be, (yp * yp - ym * ym) * ihx, f);
-    fs[ii * 33 + jj] = f;
-  }
-  __syncthreads();
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) burg_rows(int N, int M, int k, int csplit, const T* __restrict__ XL,
-                                                 const T* __restrict__ ZR, const T* __restrict__ nu, double h,
-                                                 double alpha, double beta, const T* __restrict__ CL, int p,
-                                                 T* __restrict__ part, double* __restrict__ spart) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int ldk = k + 1, ldp = p + 1;
-  T* xs = reinterpret_cast<T*>(smraw);  // 34 x ldk
-  T* zs = xs + 34 * ldk;                // 32 x ldk
-  T* ys = zs + 32 * ldk;                // 34 x 32
-  T* fs = ys + 34 * 32;                 // 32 x 33
-  T* nus = fs + 32 * 33;                // 32
-  T* cs = nus + 32;                     // 32 x ldp (CL rows)
-  T* ts = cs + 32 * ldp;                // 32 x ldk ((F ZR) rows)
+__global__ void __launch_bounds__(256) kr_gram_part(int N, int R, int aug, const int32_t* __restrict__ rank,
+                                                    const T* __restrict__ P, const T* __restrict__ Q,
+                                                    const T* __restrict__ Y, int PP, T* __restrict__ part) {
+  const int ka = active_cols(rank, R, aug), r = min(R, (int)*rank);
+  const int np = ka * (ka + 1) / 2;
+  const int p0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  if (p0 >= np || c0 >= ka) return;
+  __shared__ int pa[64], pb[64];
+  __shared__ __align__(16) T krs[32][64];
+  __shared__ __align__(16) T ys[32][64];
   const int tid = threadIdx.x;
-  const int i0 = blockIdx.x * 32, rows = min(32, N - i0);
-  const int cs_id = blockIdx.y;
-  const int per = (M + csplit - 1) / csplit;
-  const int c0 = cs_id * per, c1 = min(M, c0 + per);
-  const T ih2 = T(1.0 / (h * h)), ihx = T(0.5 / h), al = T(alpha), be = T(beta);
-  T acc[BNACC];
+  if (tid < 64) {
+    int a = 0, b = 0;
+    if (p0 + tid < np) pair_ab(p0 + tid, ka, a, b);
+    pa[tid] = act_col(a, r, R);
+    pb[tid] = act_col(b, r, R);
+  }
+  const int tp = tid & 15, tc = tid >> 4;  // pairs 4 tp.., columns 4 tc..
+  T acc[4][4];
 #pragma unroll
-  for (int u = 0; u < BNACC; ++u) acc[u] = T(0);
-  burg_stage_x(N, k, XL, i0, rows, xs, ldk);
-  for (int j0 = c0; j0 < c1; j0 += 32) {
-    const int cols = min(32, c1 - j0);
-    burg_stage_z(M, k, ZR, nu, j0, cols, zs, nus, ldk);
-    __syncthreads();
-    burg_flow_tile(k, rows, xs, zs, nus, ys, fs, ldk, ih2, ihx, al, be);
+  for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int u = 0; u < BNACC; ++u) {
-      const int o = tid + u * 256;
-      if (o < 32 * k) {
-        const int i = o & 31, c = o >> 5;
-        if (i < rows) {
-          T sacc = acc[u];
-          for (int jj = 0; jj < cols; ++jj) sacc = fma(fs[i * 33 + jj], zs[jj * ldk + c], sacc);
-          acc[u] = sacc;
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  const int j_lo = blockIdx.z * KR_ROWS, j_hi = min(N, j_lo + KR_ROWS);
+  __syncthreads();
+  for (int j0 = j_lo; j0 < j_hi; j0 += 32) {
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int jj = e & 31, pp = e >> 5;
+      const int j = j0 + jj;
+      T kv = T(0), yv = T(0);
+      if (j < j_hi) {
+        if (p0 + pp < np) {
+          const T pa_ = P[j + (int64_t)pa[pp] * N], pb_ = P[j + (int64_t)pb[pp] * N];
+          const T qa_ = Q[j + (int64_t)pa[pp] * N], qb_ = Q[j + (int64_t)pb[pp] * N];
+          kv = T(0.5) * (pa_ * qb_ + pb_ * qa_);
         }
+        if (c0 + pp < ka) yv = Y[j + (int64_t)act_col(c0 + pp, r, R) * N];
       }
+      krs[jj][pp] = kv;
+      ys[jj][pp] = yv;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < 32; ++jj) {
+      T kv[4], yv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) kv[u] = krs[jj][tp * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) yv[v] = ys[jj][tc * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(kv[u], yv[v], acc[u][v]);
     }
     __syncthreads();
   }
-  if (!CL) {
-    T* dst = part + (int64_t)cs_id * N * k;
+  T* dst = part + (int64_t)blockIdx.z * PP * (2 * R);
 #pragma unroll
-    for (int u = 0; u < BNACC; ++u) {
-      const int o = tid + u * 256;
-      if (o < 32 * k) {
-        const int i = o & 31, c = o >> 5;
-        if (i < rows) dst[(i0 + i) + (int64_t)c * N] = acc[u];
-      }
-    }
-    return;
-  }
-  // part (p x k, FP64) = CL(rows)^T (F ZR)(rows)
+  for (int u = 0; u < 4; ++u) {
+    const int p = p0 + tp * 4 + u;
+    if (p >= np) continue;
 #pragma unroll
-  for (int u = 0; u < BNACC; ++u) {
-    const int o = tid + u * 256;
-    if (o < 32 * k) {
-      const int i = o & 31, c = o >> 5;
-      ts[i * ldk + c] = (i < rows) ? acc[u] : T(0);
+    for (int v = 0; v < 4; ++v) {
+      const int c = c0 + tc * 4 + v;
+      if (c < ka) dst[p + (int64_t)c * PP] = acc[u][v];
     }
-  }
-  for (int e = tid; e < 32 * p; e += 256) {
-    const int ii = e & 31, a = e >> 5;
-    cs[ii * ldp + a] = (ii < rows) ? CL[(i0 + ii) + (int64_t)a * N] : T(0);
-  }
-  __syncthreads();
-  double* dst = spart + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * p * k;
-  for (int o = tid; o < p * k; o += 256) {
-    const int a = o % p, c = o / p;
-    double sacc = 0.0;
-    for (int ii = 0; ii < rows; ++ii) sacc = fma((double)cs[ii * ldp + a], (double)ts[ii * ldk + c], sacc);
-    dst[o] = sacc;
   }
 }
 
+// Tout[p, c] = (acc ? Tout[p, c] : 0) + coef c_ab sum_s part[s][p, c] (FP64
+// sums of the split partials), over the active pairs and columns.
 template <typename T>
-__global__ void __launch_bounds__(256) burg_cols(int N, int M, int k, const T* __restrict__ XL,
-                                                 const T* __restrict__ ZR, const T* __restrict__ nu, double h,
-                                                 double alpha, double beta, T* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int ldk = k + 1;
-  T* xs = reinterpret_cast<T*>(smraw);
-  T* zs = xs + 34 * ldk;
-  T* ys = zs + 32 * ldk;
-  T* fs = ys + 34 * 32;
-  T* nus = fs + 32 * 33;
-  const int tid = threadIdx.x;
-  const int j0 = blockIdx.x * 32, cols = min(32, M - j0);
-  const T ih2 = T(1.0 / (h * h)), ihx = T(0.5 / h), al = T(alpha), be = T(beta);
-  T acc[BNACC];
-#pragma unroll
-  for (int u = 0; u < BNACC; ++u) acc[u] = T(0);
-  burg_stage_z(M, k, ZR, nu, j0, cols, zs, nus, ldk);
-  for (int i0 = 0; i0 < N; i0 += 32) {
-    const int rows = min(32, N - i0);
-    burg_stage_x(N, k, XL, i0, rows, xs, ldk);
-    __syncthreads();
-    burg_flow_tile(k, rows, xs, zs, nus, ys, fs, ldk, ih2, ihx, al, be);
-    // acc(jj, c) += sum_ii F(ii, jj) XL(i0+ii, c)
-#pragma unroll
-    for (int u = 0; u < BNACC; ++u) {
-      const int o = tid + u * 256;
-      if (o < 32 * k) {
-        const int jj = o & 31, c = o >> 5;
-        T sacc = acc[u];
-        for (int ii = 0; ii < rows; ++ii) sacc = fma(fs[ii * 33 + jj], xs[(ii + 1) * ldk + c], sacc);
-        acc[u] = sacc;
-      }
-    }
-    __syncthreads();
+__global__ void kr_reduce(int R, int aug, const int32_t* __restrict__ rank, int nsplit, int PP,
+                          const T* __restrict__ part, double coef, int acc, T* __restrict__ Tout) {
+  const int ka = active_cols(rank, R, aug);
+  const int np = ka * (ka + 1) / 2;
+  const int64_t len = (int64_t)np * ka;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(o % np), c = (int)(o / np);
+    int a, b;
+    pair_ab(p, ka, a, b);
+    double sum = 0.0;
+    for (int s = 0; s < nsplit; ++s) sum += (double)part[(int64_t)s * PP * (2 * R) + p + (int64_t)c * PP];
+    const double v = coef * ((a == b) ? 1.0 : 2.0) * sum;
+    T* d = Tout + p + (int64_t)c * PP;
+    *d = acc ? T((double)*d + v) : T(v);
   }
+}
+
+// part[z] (N x 2R panel, active columns) = KR(P,Q) T' over the pairs of
+// split z.  Grid (row tiles of 64, column tiles of 64, pair splits); each
+// CTA stages the active columns of its 64 rows of P and Q (64 x ka each),
+// then per chunk of 32 pairs forms the Khatri-Rao chunk and a 64 x 64
+// register-blocked product (4 x 4 per thread).  Dynamic shared memory
+// 2 * 64 * (2R + 1) T.
+template <typename T>
+__global__ void __launch_bounds__(256) kr_apply_part(int N, int R, int aug, const int32_t* __restrict__ rank,
+                                                     const T* __restrict__ P, const T* __restrict__ Q,
+                                                     const T* __restrict__ Tp, int PP, T* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ka = active_cols(rank, R, aug), r = min(R, (int)*rank);
+  const int np = ka * (ka + 1) / 2;
+  const int i0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int per = (np + gridDim.z - 1) / gridDim.z;
+  const int q_lo = blockIdx.z * per, q_hi = min(np, q_lo + per);
+  if (c0 >= ka) return;
+  const int ldk = ka + 1;
+  T* ps = reinterpret_cast<T*>(smraw);  // 64 x ldk
+  T* qs = ps + 64 * ldk;                // 64 x ldk
+  __shared__ int pa[32], pb[32];
+  __shared__ __align__(16) T krs[32][64];
+  __shared__ __align__(16) T ts[32][64];
+  const int tid = threadIdx.x;
+  const int rows = min(64, N - i0);
+  for (int e = tid; e < 64 * ka; e += 256) {
+    const int ii = e & 63, a = e >> 6;
+    const int64_t off = (int64_t)act_col(a, r, R) * N + i0 + ii;
+    ps[ii * ldk + a] = (ii < rows) ? P[off] : T(0);
+    qs[ii * ldk + a] = (ii < rows) ? Q[off] : T(0);
+  }
+  const int tr = tid >> 4, tc = tid & 15;  // rows 4 tr.., columns 4 tc..
+  T acc[4][4];
 #pragma unroll
-  for (int u = 0; u < BNACC; ++u) {
-    const int o = tid + u * 256;
-    if (o < 32 * k) {
-      const int jj = o & 31, c = o >> 5;
-      if (jj < cols) out[(j0 + jj) + (int64_t)c * M] = acc[u];
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  for (int q0 = q_lo; q0 < q_hi; q0 += 32) {
+    __syncthreads();
+    if (tid < 32) {
+      int a = 0, b = 0;
+      if (q0 + tid < q_hi) pair_ab(q0 + tid, ka, a, b);
+      pa[tid] = a;
+      pb[tid] = b;
     }
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int pp = e & 31, cc = e >> 5;
+      ts[pp][cc] = (q0 + pp < q_hi && c0 + cc < ka) ? Tp[(q0 + pp) + (int64_t)(c0 + cc) * PP] : T(0);
+    }
+    __syncthreads();
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int ii = e & 63, pp = e >> 6;
+      const int a = pa[pp], b = pb[pp];
+      krs[pp][ii] = (q0 + pp < q_hi)
+                        ? T(0.5) * (ps[ii * ldk + a] * qs[ii * ldk + b] + ps[ii * ldk + b] * qs[ii * ldk + a])
+                        : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int pp = 0; pp < 32; ++pp) {
+      T kv[4], tv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) kv[u] = krs[pp][tr * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) tv[v] = ts[pp][tc * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(kv[u], tv[v], acc[u][v]);
+    }
+  }
+  T* dst = part + (int64_t)blockIdx.z * N * (2 * R);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = i0 + tr * 4 + u;
+    if (i >= N) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = c0 + tc * 4 + v;
+      if (c < ka) dst[i + (int64_t)act_col(c, r, R) * N] = acc[u][v];
+    }
+  }
+}
+
+// Dxx X and Dx X (periodic) on the active columns: d2 = c2 Dxx X, d1 = c1 Dx X
+// (either may be null); the other columns are set to zero.
+template <typename T>
+__global__ void stencil_panel(int N, int R, int aug, const int32_t* __restrict__ rank, const T* __restrict__ X,
+                              double c2, T* __restrict__ d2, double c1, T* __restrict__ d1) {
+  const int r = min(R, (int)*rank);
+  const int wcols = aug ? 2 * R : R;
+  const int64_t len = (int64_t)N * wcols;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % N), col = (int)(o / N);
+    const bool act = (col % R) < r;
+    const T* x = X + (int64_t)col * N;
+    const T xm = act ? x[(i == 0) ? N - 1 : i - 1] : T(0), xp = act ? x[(i == N - 1) ? 0 : i + 1] : T(0);
+    if (d2) d2[o] = act ? T(c2) * ((xm + xp) - T(2) * x[i]) : T(0);
+    if (d1) d1[o] = act ? T(c1) * (xp - xm) : T(0);
+  }
+}
+
+// out = lin + alpha sum_z part1[z] + beta Dx(sum_z part2[z]) on the active
+// columns (lin, part1, part2 may be null), zero elsewhere; ihx = 1 / 2h.
+template <typename T>
+__global__ void flow_combine(int N, int R, int aug, const int32_t* __restrict__ rank, const T* __restrict__ lin,
+                             const T* __restrict__ part1, const T* __restrict__ part2, int nz, double alpha,
+                             double beta, double ihx, T* __restrict__ out) {
+  const int r = min(R, (int)*rank);
+  const int wcols = aug ? 2 * R : R;
+  const int64_t len = (int64_t)N * wcols, zs = (int64_t)N * 2 * R;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % N), col = (int)(o / N);
+    if ((col % R) >= r) {
+      out[o] = T(0);
+      continue;
+    }
+    T v = lin ? lin[o] : T(0);
+    if (part1) {
+      T s = T(0);
+      for (int z = 0; z < nz; ++z) s += part1[z * zs + o];
+      v = fma(T(alpha), s, v);
+    }
+    if (part2) {
+      const int64_t om = o - i + ((i == 0) ? N - 1 : i - 1), op = o - i + ((i == N - 1) ? 0 : i + 1);
+      T sm = T(0), sp = T(0);
+      for (int z = 0; z < nz; ++z) {
+        sm += part2[z * zs + om];
+        sp += part2[z * zs + op];
+      }
+      v = fma(T(beta * ihx), sp - sm, v);
+    }
+    out[o] = v;
+  }
+}
+
+// out[j, c] = nu_j lin[j, c] + sum_z part[z][j, c] (L substep: F(U L^T)^T U =
+// diag(nu) L (U^T Dxx U) + KR(L, L) T'_L), active columns, zero elsewhere.
+template <typename T>
+__global__ void flow_combine_rows(int M, int R, const int32_t* __restrict__ rank, const T* __restrict__ nu,
+                                  const T* __restrict__ lin, const T* __restrict__ part, int nz,
+                                  T* __restrict__ out) {
+  const int r = min(R, (int)*rank);
+  const int64_t len = (int64_t)M * R, zs = (int64_t)M * 2 * R;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(o % M), col = (int)(o / M);
+    if (col >= r) {
+      out[o] = T(0);
+      continue;
+    }
+    T v = nu[j] * lin[o];
+    if (part)
+      for (int z = 0; z < nz; ++z) v += part[z * zs + o];
+    out[o] = v;
+  }
+}
+
+// Y (N x cols) = diag(w) X
+template <typename T>
+__global__ void scale_rows(int N, int cols, const T* __restrict__ X, const T* __restrict__ w, T* __restrict__ Y) {
+  const int64_t len = (int64_t)N * cols;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x)
+    Y[o] = w[o % N] * X[o];
+}
+
+// C (M x N, ld ldc) = A B with A (M x K, ld lda), B (K x N, ld ldb), FP64;
+// one thread per entry (the w x w products of the S substep).
+__global__ void small_gemm_f64(int M, int N, int K, const double* __restrict__ A, int lda,
+                               const double* __restrict__ B, int ldb, double* __restrict__ C, int ldc) {
+  const int64_t len = (int64_t)M * N;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % M), j = (int)(o / M);
+    double s = 0.0;
+    for (int k = 0; k < K; ++k) s = fma(A[i + (int64_t)k * lda], B[k + (int64_t)j * ldb], s);
+    C[i + (int64_t)j * ldc] = s;
   }
 }
 
@@ -1007,18 +1141,22 @@ struct lri_stream {
   double bh = 0.0, balpha = 0.0, bbeta = 0.0, bh_dt = 0.0;
   lri::Scheme sc{};
   const void* nu = nullptr;
-  void* Kp = nullptr;      // n x R x 4: y, stage input, stage derivative, accumulator
-  void* Lp = nullptr;      // m x R x 4
-  void* kpart = nullptr;   // kCS x n x R partial K-stage derivatives
-  double* spart = nullptr; // (n/32 * kCS) x (2R)^2 partial S-stage derivatives
+  void* Kp = nullptr;   // n x R x 4: y, stage input, stage derivative, accumulator
+  void* Lp = nullptr;   // m x R x 4
+  void* tv = nullptr;   // flow tensors T'_V, T'_L, T'_Vhat: PP x 2R each (PP = 2R (2R + 1) / 2 pairs)
+  void* tl = nullptr;
+  void* th = nullptr;
+  void* kgp = nullptr;  // split partials of the tensor sums: ceil(max(n, m) / KR_ROWS) x PP x 2R
+  void* kap = nullptr;  // pair-split partials of the Khatri-Rao products: 2 x kZmax x max(n, m) x 2R
+  void* pw = nullptr;   // 3 work panels of max(n, m) x 2R
 };
 
 
 namespace lri {
 namespace {
 
-constexpr int kBlocksSmall = 24;  // FP64 scratch of (2R)^2 each (14, 15, 23: refresh; 16..22: the Burgers S step)
-constexpr int kCS = 4;            // column splits of the K-side Burgers contraction
+constexpr int kBlocksSmall = 24;  // FP64 scratch of (2R)^2 each (14, 15, 23: refresh; 13..23: the Burgers step)
+constexpr int kZmax = 4;          // pair splits of the Khatri-Rao products (fill the GPU for short panels)
 
 template <typename T>
 struct StreamOps {
@@ -1119,17 +1257,37 @@ struct StreamOps {
     return e;
   }
 
-  static size_t burg_smem(int k, int p) {
-    return (size_t)(34 * (k + 1) + 32 * (k + 1) + 34 * 32 + 32 * 33 + 32 + 32 * (p + 1) + 32 * (k + 1)) * sizeof(T);
+  // Burgers flow helpers (see the kernels' notes)
+  int64_t pairs_max() const { return (2 * s->R) * (2 * s->R + 1) / 2; }
+  // Tout (+)= coef * (packed tensor of KR(P,Q)^T Y over N rows)
+  cudaError_t tensor(int N, int aug, const T* P, const T* Q, const T* Y, double coef, int acc, T* Tout) const {
+    const int R = (int)s->R, ka = aug ? 2 * R : R;
+    const int np = ka * (ka + 1) / 2;
+    dim3 grid((np + 63) / 64, (ka + 63) / 64, (N + KR_ROWS - 1) / KR_ROWS);
+    kr_gram_part<T><<<grid, 256, 0, st>>>(N, R, aug, s->d_rank, P, Q, Y, (int)pairs_max(), tp(s->kgp));
+    kr_reduce<T><<<304, 256, 0, st>>>(R, aug, s->d_rank, (int)grid.z, (int)pairs_max(), tp(s->kgp), coef, acc,
+                                       Tout);
+    return cudaGetLastError();
   }
-  cudaError_t burg_attr() const {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    const int mx = (int)burg_smem(128, 128);
-    cudaError_t e = cudaFuncSetAttribute(burg_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(burg_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    done = (e == cudaSuccess);
-    return e;
+  int kz(int N, int aug) const {
+    const int R = (int)s->R, ka = aug ? 2 * R : R;
+    const int tiles = ((N + 63) / 64) * ((ka + 63) / 64);
+    return std::max(1, std::min(kZmax, (2 * 152 + tiles - 1) / tiles));
+  }
+  // part[z] = KR(P,Q) T' over pair split z (z < kz(N, aug))
+  cudaError_t apply(int N, int aug, const T* P, const T* Q, const T* Tp, T* part) const {
+    const int R = (int)s->R, ka = aug ? 2 * R : R;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(kr_apply_part<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(2 * 64 * (2 * 64 + 1) * sizeof(T)));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    dim3 grid((N + 63) / 64, (ka + 63) / 64, kz(N, aug));
+    kr_apply_part<T><<<grid, 256, 2 * 64 * (ka + 1) * sizeof(T), st>>>(N, R, aug, s->d_rank, P, Q, Tp,
+                                                                      (int)pairs_max(), part);
+    return cudaGetLastError();
   }
   // one RK substep sequence of a panel flow y' = f(y) (N x R): y in P[0],
   // stage input P[1], derivative P[2], accumulator P[3]; f writes P[2].
@@ -1193,6 +1351,7 @@ struct StreamOps {
 
   cudaError_t burgers_step() const {
     const int n = (int)s->n, m = (int)s->m, R = (int)s->R, w = 2 * R;
+    const int64_t nm = std::max(n, m);
     T* U = tp(s->U);
     T* V = tp(s->V);
     T* S = tp(s->S);
@@ -1202,27 +1361,54 @@ struct StreamOps {
     T* Xl = tp(s->Xl);
     const T* nu = static_cast<const T*>(s->nu);
     const double bh = s->bh, ba = s->balpha, bb = s->bbeta;
-    cudaError_t e = burg_attr();
-    if (e == cudaSuccess) e = refresh();
+    const double ih2 = 1.0 / (bh * bh), ihx = 0.5 / bh;
+    const bool nonlin = (ba != 0.0 || bb != 0.0);
+    T* P0 = tp(s->pw);
+    T* P1 = P0 + nm * w;
+    T* P2 = P1 + nm * w;
+    T* kap1 = tp(s->kap);
+    T* kap2 = kap1 + (int64_t)kZmax * nm * w;
+    const int g = 304;
+    cudaError_t e = refresh();
     if (e != cudaSuccess) return e;
     small_to_f64<T><<<16, 256, 0, st>>>(R, S, 0, blk(16));
     small_to_f64<T><<<16, 256, 0, st>>>(R, S, 1, blk(17));
-    // K step: K0 = U0 S0, K' = F(K V0^T) V0
+    // operators of the K substep (V0 fixed): N_nu = V0^T diag(nu) V0, T'_V
+    double* Nnu = blk(13);
+    scale_rows<T><<<g, 256, 0, st>>>(m, R, V, nu, P0);
+    if ((e = gram(m, R, R, V, m, P0, m, 1.0, 0.0, Nnu, R)) != cudaSuccess) return e;
+    if (nonlin && (e = tensor(m, 0, V, V, V, 1.0, 0, tp(s->tv))) != cudaSuccess) return e;
+    // operators of the L substep (U0 fixed): A_xx = U0^T Dxx U0,
+    // T_L = alpha sym(KR(Dx U0, U0))^T U0 - beta KR(U0, U0)^T Dx U0
+    double* Axx = blk(14);
+    stencil_panel<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, U, ih2, P0, ihx, P1);
+    if ((e = gram(n, R, R, U, n, P0, n, 1.0, 0.0, Axx, R)) != cudaSuccess) return e;
+    if (ba != 0.0 && (e = tensor(n, 0, P1, U, U, ba, 0, tp(s->tl))) != cudaSuccess) return e;
+    if (bb != 0.0 && (e = tensor(n, 0, U, U, P1, -bb, ba != 0.0, tp(s->tl))) != cudaSuccess) return e;
+    // K step: K0 = U0 S0, K' = (Dxx K) N_nu + alpha KR(Dx K, K) T'_V + beta Dx(KR(K, K) T'_V)
     T* Kp = tp(s->Kp);
     if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
-    const int ntile = (n + 31) / 32;
+    const int zk = kz(n, 0);
     e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, T* out) {
-      burg_rows<T><<<dim3(ntile, kCS), 256, burg_smem(R, 0), st>>>(n, m, R, kCS, Z, V, nu, bh, ba, bb, nullptr, 0,
-                                                                    tp(s->kpart), nullptr);
-      sum_parts<T><<<304, 256, 0, st>>>((int64_t)n * R, kCS, tp(s->kpart), out);
+      stencil_panel<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, Z, ih2, P0, ihx, ba != 0.0 ? P1 : nullptr);
+      cudaError_t e2 = mul(n, R, R, P0, n, Nnu, R, T(0), P2, n);
+      if (e2 == cudaSuccess && ba != 0.0) e2 = apply(n, 0, P1, Z, tp(s->tv), kap1);
+      if (e2 == cudaSuccess && bb != 0.0) e2 = apply(n, 0, Z, Z, tp(s->tv), kap2);
+      if (e2 != cudaSuccess) return e2;
+      flow_combine<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, P2, ba != 0.0 ? kap1 : nullptr,
+                                         bb != 0.0 ? kap2 : nullptr, zk, ba, bb, ihx, out);
       return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
-    // L step: L0 = V0 S0^T, L' = F(U0 L^T)^T U0
+    // L step: L0 = V0 S0^T, L' = diag(nu) L A_xx + KR(L, L) T'_L
     T* Lp = tp(s->Lp);
     if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
+    const int zl = kz(m, 0);
     e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, T* out) {
-      burg_cols<T><<<(m + 31) / 32, 256, burg_smem(R, 0), st>>>(n, m, R, U, Z, nu, bh, ba, bb, out);
+      cudaError_t e2 = mul(m, R, R, Z, m, Axx, R, T(0), P2, m);
+      if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
+      if (e2 != cudaSuccess) return e2;
+      flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, out);
       return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -1237,9 +1423,18 @@ struct StreamOps {
     copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, Vh + (int64_t)R * m, m);
     if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
     if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
+    // operators of the S substep: A_xx = Uhat^T Dxx Uhat, N_nu = Vhat^T diag(nu) Vhat, T'_Vhat
+    double* Axxh = blk(15);
+    double* Nnuh = blk(23);
+    double* Stmp = blk(22);
+    stencil_panel<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, Uh, ih2, P0, 0.0, nullptr);
+    if ((e = gram(n, w, w, Uh, n, P0, n, 1.0, 0.0, Axxh, w)) != cudaSuccess) return e;
+    scale_rows<T><<<g, 256, 0, st>>>(m, w, Vh, nu, P0);
+    if ((e = gram(m, w, w, Vh, m, P0, m, 1.0, 0.0, Nnuh, w)) != cudaSuccess) return e;
+    if (nonlin && (e = tensor(m, 1, Vh, Vh, Vh, 1.0, 0, tp(s->th))) != cudaSuccess) return e;
     // S step on the augmented bases from S~0 = Mh S0 Nh^T (FP64 w x w):
-    // S' = Uhat^T F(Uhat S Vhat^T) Vhat, stage inputs formed as Uhat Z
-    small_msn<<<1, 1024, 0, st>>>(w, R, blk(3), blk(16), blk(4), blk(22), blk(18));
+    // S' = A_xx S N_nu + Uhat^T [alpha KR(Dx A, A) T'_Vhat + beta Dx(KR(A, A) T'_Vhat)], A = Uhat S
+    small_msn<<<1, 1024, 0, st>>>(w, R, blk(3), blk(16), blk(4), Stmp, blk(18));
     {
       const Scheme& sc = s->sc;
       const double h = s->bh_dt / sc.nsub;
@@ -1248,14 +1443,23 @@ struct StreamOps {
       double* Sk = blk(20);
       double* Sa = blk(21);
       const int64_t len = (int64_t)w * w;
-      const int nct = ntile * 2;  // two column splits
+      const int zs = kz(n, 1);
       for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
         for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
           const double* Z = (st_ == 0) ? Sy : Sz;
-          if ((e = mul(n, w, w, Uh, n, Z, w, T(0), tp(s->Zp), n)) != cudaSuccess) break;
-          burg_rows<T><<<dim3(ntile, 2), 256, burg_smem(w, w), st>>>(n, m, w, 2, tp(s->Zp), Vh, nu, bh, ba, bb, Uh,
-                                                                     w, nullptr, s->spart);
-          sum_parts<double><<<64, 256, 0, st>>>(len, nct, s->spart, Sk);
+          small_gemm_f64<<<64, 256, 0, st>>>(w, w, w, Z, w, Nnuh, w, Stmp, w);
+          small_gemm_f64<<<64, 256, 0, st>>>(w, w, w, Axxh, w, Stmp, w, Sk, w);
+          if (nonlin) {
+            if ((e = mul(n, w, w, Uh, n, Z, w, T(0), P0, n)) != cudaSuccess) break;
+            if (ba != 0.0) {
+              stencil_panel<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, P0, 0.0, nullptr, ihx, P1);
+              if ((e = apply(n, 1, P1, P0, tp(s->th), kap1)) != cudaSuccess) break;
+            }
+            if (bb != 0.0 && (e = apply(n, 1, P0, P0, tp(s->th), kap2)) != cudaSuccess) break;
+            flow_combine<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, nullptr, ba != 0.0 ? kap1 : nullptr,
+                                               bb != 0.0 ? kap2 : nullptr, zs, ba, bb, ihx, P2);
+            if ((e = gram(n, w, w, Uh, n, P2, n, 1.0, 1.0, Sk, w)) != cudaSuccess) break;
+          }
           if (st_ == 0) axpbz<double><<<64, 256, 0, st>>>(len, sc.b[0], Sk, 0.0, nullptr, Sa);
           else axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sa, sc.b[st_], Sk, Sa);
           if (st_ + 1 < sc.nstages) axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sy, h * sc.a[st_ + 1], Sk, Sz);
@@ -1401,15 +1605,19 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
     s->sc.b[i] = scheme->b[i];
     s->sc.c[i] = scheme->c[i];
   }
-  const int64_t R = r_max, ntile = (n + 31) / 32;
+  const int64_t R = r_max, nm = std::max(n, m), PP = (2 * R) * (2 * R + 1) / 2;
   cudaError_t e = cudaSuccess;
   auto alloc = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMalloc(p, bytes < 16 ? 16 : bytes);
   };
   alloc(&s->Kp, s->es * n * R * 4);
   alloc(&s->Lp, s->es * m * R * 4);
-  alloc(&s->kpart, s->es * kCS * n * R);
-  alloc((void**)&s->spart, sizeof(double) * ntile * 2 * 4 * R * R);
+  alloc(&s->tv, s->es * PP * 2 * R);
+  alloc(&s->tl, s->es * PP * 2 * R);
+  alloc(&s->th, s->es * PP * 2 * R);
+  alloc(&s->kgp, s->es * ((nm + KR_ROWS - 1) / KR_ROWS) * PP * 2 * R);
+  alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
+  alloc(&s->pw, s->es * 3 * nm * 2 * R);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
@@ -1441,8 +1649,12 @@ lri_status lri_stream_destroy(lri_stream* s) {
   if (!s) return LRI_ERR_ARG;
   cudaFree(s->Kp);
   cudaFree(s->Lp);
-  cudaFree(s->kpart);
-  cudaFree(s->spart);
+  cudaFree(s->tv);
+  cudaFree(s->tl);
+  cudaFree(s->th);
+  cudaFree(s->kgp);
+  cudaFree(s->kap);
+  cudaFree(s->pw);
   cudaFree(s->d_rank);
   cudaFree(s->d_status);
   cudaFree(s->Uh);
