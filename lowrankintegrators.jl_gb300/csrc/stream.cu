@@ -836,86 +836,159 @@ __global__ void kr_reduce(int R, int aug, const int32_t* __restrict__ rank, int 
   }
 }
 
-// part[z] (N x 2R panel, active columns) = KR(P,Q) T' over the pairs of
-// split z.  Grid (row tiles of 64, column tiles of 64, pair splits); each
-// CTA stages the active columns of its 64 rows of P and Q (64 x ka each),
-// then per chunk of 32 pairs forms the Khatri-Rao chunk and a 64 x 64
-// register-blocked product (4 x 4 per thread).  Dynamic shared memory
-// 2 * 64 * (2R + 1) T.
+// part[z] (N x 2R panel, active columns) = scale * sum_{a in split z}
+// diag(X[:, a]) Y[:, a:ka] T'[p(a, a..ka-1), :] -- the packed Khatri-Rao
+// product KR(X,X) T' for Y = X; for X != Y the symmetrised one needs the
+// sum of (X, Y) and (Y, X) at scale 1/2.  The pairs of a are contiguous rows
+// of T', so the inner loop is a plain GEMM of the staged rows of Y with
+// 32-row chunks of T' (double-buffered through registers), and the
+// Khatri-Rao products are never formed.  Grid (row tiles of BM, column tiles
+// of 64, splits of the a range with about equal pair counts); 256 threads,
+// 8 x 4 (FP32) or 4 x 4 (FP64) outputs per thread.  Dynamic shared memory:
+// the active columns of the tile's rows of Y (and of X when distinct),
+// ka x BM each.
 template <typename T>
+struct KrTile {
+  static constexpr int BM = (sizeof(T) == 4) ? 128 : 64;
+  static constexpr int TM = BM / 16;  // rows per thread
+};
+constexpr int KR_KB = 32;
+
+// n consecutive values from 16-byte aligned shared memory (n a multiple of 4)
+template <int n>
+__device__ __forceinline__ void ld_vec(const float* p, float* out) {
+#pragma unroll
+  for (int q = 0; q < n / 4; ++q) {
+    const float4 v = reinterpret_cast<const float4*>(p)[q];
+    out[4 * q] = v.x;
+    out[4 * q + 1] = v.y;
+    out[4 * q + 2] = v.z;
+    out[4 * q + 3] = v.w;
+  }
+}
+template <int n>
+__device__ __forceinline__ void ld_vec(const double* p, double* out) {
+#pragma unroll
+  for (int q = 0; q < n / 2; ++q) {
+    const double2 v = reinterpret_cast<const double2*>(p)[q];
+    out[2 * q] = v.x;
+    out[2 * q + 1] = v.y;
+  }
+}
+
+template <typename T, bool SAME>
 __global__ void __launch_bounds__(256) kr_apply_part(int N, int R, int aug, const int32_t* __restrict__ rank,
-                                                     const T* __restrict__ P, const T* __restrict__ Q,
-                                                     const T* __restrict__ Tp, int PP, T* __restrict__ part) {
+                                                     const T* __restrict__ X, const T* __restrict__ Y,
+                                                     const T* __restrict__ Tp, int PP, double scale, int accum,
+                                                     T* __restrict__ part) {
+  constexpr int BM = KrTile<T>::BM, TM = KrTile<T>::TM;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ka = active_cols(rank, R, aug), r = min(R, (int)*rank);
   const int np = ka * (ka + 1) / 2;
-  const int i0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
-  const int per = (np + gridDim.z - 1) / gridDim.z;
-  const int q_lo = blockIdx.z * per, q_hi = min(np, q_lo + per);
+  const int i0 = blockIdx.x * BM, c0 = blockIdx.y * 64;
   if (c0 >= ka) return;
-  const int ldk = ka + 1;
-  T* ps = reinterpret_cast<T*>(smraw);  // 64 x ldk
-  T* qs = ps + 64 * ldk;                // 64 x ldk
-  __shared__ int pa[32], pb[32];
-  __shared__ __align__(16) T krs[32][64];
-  __shared__ __align__(16) T ts[32][64];
+  // a range of this split: the a whose pair rows start in [z np / Z, (z+1) np / Z)
+  auto start = [&](int a) { return a * ka - a * (a - 1) / 2; };
+  auto first_a = [&](int64_t pb) {
+    int x = 0;
+    while (x < ka && start(x) < pb) ++x;
+    return x;
+  };
+  const int a_lo = first_a((int64_t)blockIdx.z * np / gridDim.z);
+  const int a_hi = first_a((int64_t)(blockIdx.z + 1) * np / gridDim.z);
+  T* ys = reinterpret_cast<T*>(smraw);        // ka x BM (column b: the tile's rows)
+  T* xs = SAME ? ys : ys + (size_t)ka * BM;   // ka x BM
+  __shared__ __align__(16) T ts[2][KR_KB][64];
   const int tid = threadIdx.x;
-  const int rows = min(64, N - i0);
-  for (int e = tid; e < 64 * ka; e += 256) {
-    const int ii = e & 63, a = e >> 6;
-    const int64_t off = (int64_t)act_col(a, r, R) * N + i0 + ii;
-    ps[ii * ldk + a] = (ii < rows) ? P[off] : T(0);
-    qs[ii * ldk + a] = (ii < rows) ? Q[off] : T(0);
+  const int rows = min(BM, N - i0);
+  for (int e = tid; e < BM * ka; e += 256) {
+    const int ii = e % BM, b = e / BM;
+    const int64_t off = (int64_t)act_col(b, r, R) * N + i0 + ii;
+    ys[e] = (ii < rows) ? Y[off] : T(0);
+    if (!SAME) xs[e] = (ii < rows) ? X[off] : T(0);
   }
-  const int tr = tid >> 4, tc = tid & 15;  // rows 4 tr.., columns 4 tc..
-  T acc[4][4];
+  const int tr = tid >> 4, tc = tid & 15;  // rows TM tr.., columns 4 tc..
+  T acc[TM][4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < TM; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
-  for (int q0 = q_lo; q0 < q_hi; q0 += 32) {
-    __syncthreads();
-    if (tid < 32) {
-      int a = 0, b = 0;
-      if (q0 + tid < q_hi) pair_ab(q0 + tid, ka, a, b);
-      pa[tid] = a;
-      pb[tid] = b;
+  // chunk sequence: for a in [a_lo, a_hi), b0 = a, a + KB, ... < ka
+  int a = a_lo, b0 = a_lo;
+  T pre[KR_KB * 64 / 256];
+  auto load_chunk = [&](int ca, int cb0) {
+#pragma unroll
+    for (int q = 0; q < KR_KB * 64 / 256; ++q) {
+      const int e = tid + q * 256;
+      const int bb = e >> 6, cc = e & 63;
+      const int b = cb0 + bb;
+      pre[q] = (ca < a_hi && b < ka && c0 + cc < ka) ? Tp[(start(ca) + (b - ca)) + (int64_t)(c0 + cc) * PP] : T(0);
     }
-    for (int e = tid; e < 32 * 64; e += 256) {
-      const int pp = e & 31, cc = e >> 5;
-      ts[pp][cc] = (q0 + pp < q_hi && c0 + cc < ka) ? Tp[(q0 + pp) + (int64_t)(c0 + cc) * PP] : T(0);
+  };
+  auto store_chunk = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < KR_KB * 64 / 256; ++q) {
+      const int e = tid + q * 256;
+      ts[buf][e >> 6][e & 63] = pre[q];
     }
-    __syncthreads();
-    for (int e = tid; e < 32 * 64; e += 256) {
-      const int ii = e & 63, pp = e >> 6;
-      const int a = pa[pp], b = pb[pp];
-      krs[pp][ii] = (q0 + pp < q_hi)
-                        ? T(0.5) * (ps[ii * ldk + a] * qs[ii * ldk + b] + ps[ii * ldk + b] * qs[ii * ldk + a])
-                        : T(0);
+  };
+  if (a < a_hi) load_chunk(a, b0);
+  __syncthreads();
+  store_chunk(0);
+  __syncthreads();
+  int buf = 0;
+  T g[TM][4];
+#pragma unroll
+  for (int u = 0; u < TM; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) g[u][v] = T(0);
+  while (a < a_hi) {
+    // next chunk position, prefetched into registers during this one
+    int na = a, nb0 = b0 + KR_KB;
+    if (nb0 >= ka) { ++na; nb0 = na; }
+    if (na < a_hi) load_chunk(na, nb0);
+    const int kc = min(KR_KB, ka - b0);
+    for (int bb = 0; bb < kc; ++bb) {
+      T yv[TM], tv[4];
+      ld_vec<TM>(ys + (size_t)(b0 + bb) * BM + tr * TM, yv);
+      ld_vec<4>(&ts[buf][bb][tc * 4], tv);
+#pragma unroll
+      for (int u = 0; u < TM; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) g[u][v] = fma(yv[u], tv[v], g[u][v]);
     }
-    __syncthreads();
-#pragma unroll 4
-    for (int pp = 0; pp < 32; ++pp) {
-      T kv[4], tv[4];
+    if (na != a) {  // a done: acc += X[:, a] g
+      const T* xrow = xs + (size_t)a * BM + tr * TM;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) kv[u] = krs[pp][tr * 4 + u];
+      for (int u = 0; u < TM; ++u) {
+        const T xv = xrow[u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) tv[v] = ts[pp][tc * 4 + v];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(kv[u], tv[v], acc[u][v]);
+        for (int v = 0; v < 4; ++v) {
+          acc[u][v] = fma(xv, g[u][v], acc[u][v]);
+          g[u][v] = T(0);
+        }
+      }
+    }
+    a = na;
+    b0 = nb0;
+    if (a < a_hi) {
+      store_chunk(buf ^ 1);
+      __syncthreads();
+      buf ^= 1;
     }
   }
   T* dst = part + (int64_t)blockIdx.z * N * (2 * R);
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int i = i0 + tr * 4 + u;
+  for (int u = 0; u < TM; ++u) {
+    const int i = i0 + tr * TM + u;
     if (i >= N) continue;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int c = c0 + tc * 4 + v;
-      if (c < ka) dst[i + (int64_t)act_col(c, r, R) * N] = acc[u][v];
+      if (c < ka) {
+        T* d = dst + i + (int64_t)act_col(c, r, R) * N;
+        *d = accum ? fma(T(scale), acc[u][v], *d) : T(scale) * acc[u][v];
+      }
     }
   }
 }
@@ -1001,16 +1074,136 @@ __global__ void scale_rows(int N, int cols, const T* __restrict__ X, const T* __
     Y[o] = w[o % N] * X[o];
 }
 
-// C (M x N, ld ldc) = A B with A (M x K, ld lda), B (K x N, ld ldb), FP64;
-// one thread per entry (the w x w products of the S substep).
-__global__ void small_gemm_f64(int M, int N, int K, const double* __restrict__ A, int lda,
-                               const double* __restrict__ B, int ldb, double* __restrict__ C, int ldc) {
-  const int64_t len = (int64_t)M * N;
+// C = A B on the active block of w x w FP64 matrices (ld w = 2R; active
+// indices: the first r of each half); one thread per entry.  The other
+// entries of C are left alone.
+__global__ void small_gemm_act(int R, const int32_t* __restrict__ rank, const double* __restrict__ A,
+                               const double* __restrict__ B, double* __restrict__ C) {
+  const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
+  const int64_t len = (int64_t)ka * ka;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(o % M), j = (int)(o / M);
+    const int i = act_col((int)(o % ka), r, R), j = act_col((int)(o / ka), r, R);
     double s = 0.0;
-    for (int k = 0; k < K; ++k) s = fma(A[i + (int64_t)k * lda], B[k + (int64_t)j * ldb], s);
-    C[i + (int64_t)j * ldc] = s;
+    for (int k = 0; k < ka; ++k) {
+      const int kk = act_col(k, r, R);
+      s = fma(A[i + (int64_t)kk * w], B[kk + (int64_t)j * w], s);
+    }
+    C[i + (int64_t)j * w] = s;
+  }
+}
+
+// out[:, c] = sum_{k active} X[:, k] B[k, c] for the active columns c of an N
+// x R (aug = 0) or N x 2R (aug = 1) panel; B FP64 with ld ldb.  Grid (row
+// blocks of 32, column tiles of 64); tiles beyond the active columns exit,
+// inactive output columns are left alone.
+template <typename T>
+__global__ void __launch_bounds__(256) panel_mul_act(int N, int R, int aug, const int32_t* __restrict__ rank,
+                                                     const T* __restrict__ X, const double* __restrict__ B,
+                                                     int ldb, T* __restrict__ out) {
+  const int ka = active_cols(rank, R, aug), r = min(R, (int)*rank);
+  const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+  if (c0 >= ka) return;
+  __shared__ T xs[32][33];
+  __shared__ T bs[32][65];
+  const int tid = threadIdx.x;
+  const int ri = tid & 15, cj = tid >> 4;
+  T acc[2][4];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = T(0);
+  for (int k0 = 0; k0 < ka; k0 += 32) {
+    const int kc = min(32, ka - k0);
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int ii = e % 32, k = e / 32;
+      const int i = i0 + ii;
+      xs[ii][k] = (i < N && k < kc) ? X[i + (int64_t)act_col(k0 + k, r, R) * N] : T(0);
+    }
+    for (int e = tid; e < 32 * 64; e += 256) {
+      const int k = e % 32, cc = e / 32;
+      bs[k][cc] = (k < kc && c0 + cc < ka)
+                      ? T(B[act_col(k0 + k, r, R) + (int64_t)act_col(c0 + cc, r, R) * ldb])
+                      : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+      const T x0 = xs[ri][k], x1 = xs[ri + 16][k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const T wv = bs[k][cj + 16 * q];
+        acc[0][q] = fma(x0, wv, acc[0][q]);
+        acc[1][q] = fma(x1, wv, acc[1][q]);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int i = i0 + ri + 16 * p;
+    if (i >= N) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + cj + 16 * q;
+      if (c < ka) out[i + (int64_t)act_col(c, r, R) * N] = acc[p][q];
+    }
+  }
+}
+
+// part[z][a, c] = X[:, a]^T Y[:, c] over the rows of split z, on the active
+// w x w block (aug panels N x 2R; part ld 2R), one CTA per 32 x 32 tile of
+// active entries and split of GA_ROWS rows: sums of 32-row chunks in T,
+// added up in FP64 (an RK stage derivative: FP32 chunk sums are well inside
+// the FP32 step's accuracy).  gram_act_reduce adds the splits to C.
+constexpr int GA_ROWS = 128;
+template <typename T>
+__global__ void __launch_bounds__(256) gram_act(int N, int R, const int32_t* __restrict__ rank,
+                                                const T* __restrict__ X, const T* __restrict__ Y,
+                                                double* __restrict__ part) {
+  const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
+  const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  if (a0 >= ka || c0 >= ka) return;
+  __shared__ T xs[32][33];
+  __shared__ T ys[32][33];
+  const int tid = threadIdx.x;
+  const int ta = tid & 31, tcb = tid >> 5;  // entry (ta, tcb + 8 q)
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const int i_lo = blockIdx.z * GA_ROWS, i_hi = min(N, i_lo + GA_ROWS);
+  for (int i0 = i_lo; i0 < i_hi; i0 += 32) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int ii = e % 32, k = e / 32;
+      const int i = i0 + ii;
+      xs[k][ii] = (i < i_hi && a0 + k < ka) ? X[i + (int64_t)act_col(a0 + k, r, R) * N] : T(0);
+      ys[k][ii] = (i < i_hi && c0 + k < ka) ? Y[i + (int64_t)act_col(c0 + k, r, R) * N] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      T sacc = T(0);
+#pragma unroll 8
+      for (int ii = 0; ii < 32; ++ii) sacc = fma(xs[ta][ii], ys[tcb + 8 * q][ii], sacc);
+      acc[q] += (double)sacc;
+    }
+    __syncthreads();
+  }
+  double* dst = part + (int64_t)blockIdx.z * w * w;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int a = a0 + ta, c = c0 + tcb + 8 * q;
+    if (a < ka && c < ka) dst[act_col(a, r, R) + (int64_t)act_col(c, r, R) * w] = acc[q];
+  }
+}
+
+// C[a, c] += sum_z part[z][a, c] on the active block (fixed order)
+__global__ void gram_act_reduce(int R, const int32_t* __restrict__ rank, int nz, const double* __restrict__ part,
+                                double* __restrict__ C) {
+  const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
+  const int64_t len = (int64_t)ka * ka;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t idx = act_col((int)(o % ka), r, R) + (int64_t)act_col((int)(o / ka), r, R) * w;
+    double sacc = 0.0;
+    for (int z = 0; z < nz; ++z) sacc += part[z * (int64_t)w * w + idx];
+    C[idx] += sacc;
   }
 }
 
@@ -1146,7 +1339,7 @@ struct lri_stream {
   void* tv = nullptr;   // flow tensors T'_V, T'_L, T'_Vhat: PP x 2R each (PP = 2R (2R + 1) / 2 pairs)
   void* tl = nullptr;
   void* th = nullptr;
-  void* kgp = nullptr;  // split partials of the tensor sums: ceil(max(n, m) / KR_ROWS) x PP x 2R
+  void* kgp = nullptr;  // split partials of the tensor sums (ceil(max(n, m) / KR_ROWS) x PP x 2R) and of gram_act
   void* kap = nullptr;  // pair-split partials of the Khatri-Rao products: 2 x kZmax x max(n, m) x 2R
   void* pw = nullptr;   // 3 work panels of max(n, m) x 2R
 };
@@ -1156,7 +1349,7 @@ namespace lri {
 namespace {
 
 constexpr int kBlocksSmall = 24;  // FP64 scratch of (2R)^2 each (14, 15, 23: refresh; 13..23: the Burgers step)
-constexpr int kZmax = 4;          // pair splits of the Khatri-Rao products (fill the GPU for short panels)
+constexpr int kZmax = 8;          // pair splits of the Khatri-Rao products (fill the GPU for short panels)
 
 template <typename T>
 struct StreamOps {
@@ -1271,22 +1464,32 @@ struct StreamOps {
   }
   int kz(int N, int aug) const {
     const int R = (int)s->R, ka = aug ? 2 * R : R;
-    const int tiles = ((N + 63) / 64) * ((ka + 63) / 64);
+    const int tiles = ((N + KrTile<T>::BM - 1) / KrTile<T>::BM) * ((ka + 63) / 64);
     return std::max(1, std::min(kZmax, (2 * 152 + tiles - 1) / tiles));
   }
-  // part[z] = KR(P,Q) T' over pair split z (z < kz(N, aug))
-  cudaError_t apply(int N, int aug, const T* P, const T* Q, const T* Tp, T* part) const {
+  // part[z] (=, or += with accum) scale * sum_{a in split z} diag(X[:, a]) Y[:, a:] T'_a
+  // (z < kz(N, aug)): KR(X, X) T' for Y = X
+  cudaError_t apply(int N, int aug, const T* X, const T* Y, const T* Tp, T* part, double scale = 1.0,
+                    int accum = 0) const {
     const int R = (int)s->R, ka = aug ? 2 * R : R;
+    constexpr int BM = KrTile<T>::BM;
     static bool attr_set = false;
     if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(kr_apply_part<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(2 * 64 * (2 * 64 + 1) * sizeof(T)));
+      const int mx = (int)(2 * (2 * 64) * BM * sizeof(T));
+      cudaError_t e = cudaFuncSetAttribute(kr_apply_part<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kr_apply_part<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    dim3 grid((N + 63) / 64, (ka + 63) / 64, kz(N, aug));
-    kr_apply_part<T><<<grid, 256, 2 * 64 * (ka + 1) * sizeof(T), st>>>(N, R, aug, s->d_rank, P, Q, Tp,
-                                                                      (int)pairs_max(), part);
+    dim3 grid((N + BM - 1) / BM, (ka + 63) / 64, kz(N, aug));
+    const size_t smem = (size_t)ka * BM * sizeof(T) * (X == Y ? 1 : 2);
+    if (X == Y)
+      kr_apply_part<T, true><<<grid, 256, smem, st>>>(N, R, aug, s->d_rank, X, Y, Tp, (int)pairs_max(), scale,
+                                                      accum, part);
+    else
+      kr_apply_part<T, false><<<grid, 256, smem, st>>>(N, R, aug, s->d_rank, X, Y, Tp, (int)pairs_max(), scale,
+                                                       accum, part);
     return cudaGetLastError();
   }
   // one RK substep sequence of a panel flow y' = f(y) (N x R): y in P[0],
@@ -1391,8 +1594,10 @@ struct StreamOps {
     const int zk = kz(n, 0);
     e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, T* out) {
       stencil_panel<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, Z, ih2, P0, ihx, ba != 0.0 ? P1 : nullptr);
-      cudaError_t e2 = mul(n, R, R, P0, n, Nnu, R, T(0), P2, n);
-      if (e2 == cudaSuccess && ba != 0.0) e2 = apply(n, 0, P1, Z, tp(s->tv), kap1);
+      panel_mul_act<T><<<dim3((n + 31) / 32, (R + 63) / 64), 256, 0, st>>>(n, R, 0, s->d_rank, P0, Nnu, R, P2);
+      cudaError_t e2 = cudaGetLastError();
+      if (e2 == cudaSuccess && ba != 0.0) e2 = apply(n, 0, P1, Z, tp(s->tv), kap1, 0.5, 0);
+      if (e2 == cudaSuccess && ba != 0.0) e2 = apply(n, 0, Z, P1, tp(s->tv), kap1, 0.5, 1);
       if (e2 == cudaSuccess && bb != 0.0) e2 = apply(n, 0, Z, Z, tp(s->tv), kap2);
       if (e2 != cudaSuccess) return e2;
       flow_combine<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, P2, ba != 0.0 ? kap1 : nullptr,
@@ -1405,7 +1610,8 @@ struct StreamOps {
     if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
     const int zl = kz(m, 0);
     e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, T* out) {
-      cudaError_t e2 = mul(m, R, R, Z, m, Axx, R, T(0), P2, m);
+      panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
+      cudaError_t e2 = cudaGetLastError();
       if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
       if (e2 != cudaSuccess) return e2;
       flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, out);
@@ -1447,18 +1653,24 @@ struct StreamOps {
       for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
         for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
           const double* Z = (st_ == 0) ? Sy : Sz;
-          small_gemm_f64<<<64, 256, 0, st>>>(w, w, w, Z, w, Nnuh, w, Stmp, w);
-          small_gemm_f64<<<64, 256, 0, st>>>(w, w, w, Axxh, w, Stmp, w, Sk, w);
+          small_gemm_act<<<64, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
+          small_gemm_act<<<64, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
           if (nonlin) {
-            if ((e = mul(n, w, w, Uh, n, Z, w, T(0), P0, n)) != cudaSuccess) break;
+            panel_mul_act<T><<<dim3((n + 31) / 32, (w + 63) / 64), 256, 0, st>>>(n, R, 1, s->d_rank, Uh, Z, w, P0);
             if (ba != 0.0) {
               stencil_panel<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, P0, 0.0, nullptr, ihx, P1);
-              if ((e = apply(n, 1, P1, P0, tp(s->th), kap1)) != cudaSuccess) break;
+              if ((e = apply(n, 1, P1, P0, tp(s->th), kap1, 0.5, 0)) != cudaSuccess) break;
+              if ((e = apply(n, 1, P0, P1, tp(s->th), kap1, 0.5, 1)) != cudaSuccess) break;
             }
             if (bb != 0.0 && (e = apply(n, 1, P0, P0, tp(s->th), kap2)) != cudaSuccess) break;
             flow_combine<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, nullptr, ba != 0.0 ? kap1 : nullptr,
                                                bb != 0.0 ? kap2 : nullptr, zs, ba, bb, ihx, P2);
-            if ((e = gram(n, w, w, Uh, n, P2, n, 1.0, 1.0, Sk, w)) != cudaSuccess) break;
+            {
+              const int nzg = (n + GA_ROWS - 1) / GA_ROWS;
+              double* gpart = reinterpret_cast<double*>(s->kgp);  // free during the S substep
+              gram_act<T><<<dim3((w + 31) / 32, (w + 31) / 32, nzg), 256, 0, st>>>(n, R, s->d_rank, Uh, P2, gpart);
+              gram_act_reduce<<<64, 256, 0, st>>>(R, s->d_rank, nzg, gpart, Sk);
+            }
           }
           if (st_ == 0) axpbz<double><<<64, 256, 0, st>>>(len, sc.b[0], Sk, 0.0, nullptr, Sa);
           else axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sa, sc.b[st_], Sk, Sa);
@@ -1575,6 +1787,7 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   const int32_t r32 = (int32_t)r0;
   if (e == cudaSuccess) e = cudaMemcpy(s->d_rank, &r32, sizeof(r32), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(s->small, 0, sizeof(double) * kBlocksSmall * 4 * R * R);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     return LRI_ERR_CUDA;
@@ -1615,7 +1828,9 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
   alloc(&s->tv, s->es * PP * 2 * R);
   alloc(&s->tl, s->es * PP * 2 * R);
   alloc(&s->th, s->es * PP * 2 * R);
-  alloc(&s->kgp, s->es * ((nm + KR_ROWS - 1) / KR_ROWS) * PP * 2 * R);
+  // (also the split partials of the S substep's Gram: ceil(n / GA_ROWS) x (2R)^2 FP64)
+  alloc(&s->kgp, std::max<int64_t>(s->es * ((nm + KR_ROWS - 1) / KR_ROWS) * PP * 2 * R,
+                                   (int64_t)sizeof(double) * ((n + GA_ROWS - 1) / GA_ROWS) * 4 * R * R));
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
   if (e != cudaSuccess) {
