@@ -1342,6 +1342,11 @@ struct lri_stream {
   void* kgp = nullptr;  // split partials of the tensor sums (ceil(max(n, m) / KR_ROWS) x PP x 2R) and of gram_act
   void* kap = nullptr;  // pair-split partials of the Khatri-Rao products: 2 x kZmax x max(n, m) x 2R
   void* pw = nullptr;   // 3 work panels of max(n, m) x 2R
+  // one captured Burgers step (launch shapes depend on r_max only; the rank
+  // is read on the device), replayed while dt and the bound factors stay
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  double graph_dt = 0.0;
 };
 
 
@@ -1751,6 +1756,35 @@ struct StreamOps {
 }  // namespace
 }  // namespace lri
 
+static cudaError_t burgers_step_on(lri_stream* s, cudaStream_t st) {
+  return (s->dtype == LRI_F32) ? StreamOps<float>{s, st}.burgers_step() : StreamOps<double>{s, st}.burgers_step();
+}
+
+static void drop_graph(lri_stream* s) {
+  if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+  s->step_exec = nullptr;
+}
+
+// Capture one step on the private stream (nothing runs); on any failure the
+// steps run eagerly.
+static void capture_step(lri_stream* s) {
+  drop_graph(s);
+  if (!s->cap && cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess) {
+    s->cap = nullptr;
+    return;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return;
+  const cudaError_t e = burgers_step_on(s, s->cap);
+  const cudaError_t ec = cudaStreamEndCapture(s->cap, &g);
+  if (e == cudaSuccess && ec == cudaSuccess && g) {
+    if (cudaGraphInstantiate(&s->step_exec, g, 0) != cudaSuccess) s->step_exec = nullptr;
+    else s->graph_dt = s->bh_dt;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();  // a failed capture leaves no sticky error; clear the last one
+}
+
 extern "C" {
 
 lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0, int64_t r_max,
@@ -1843,6 +1877,7 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
 
 lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void* nu) {
   if (!s || !s->burgers || !nu) return LRI_ERR_ARG;
+  drop_graph(s);
   s->nu = nu;
   return lri_stream_bind(s, U, S, V);
 }
@@ -1850,18 +1885,26 @@ lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void
 lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stream) {
   if (!s || !s->burgers || nsteps < 0 || !std::isfinite(dt)) return LRI_ERR_ARG;
   if (!s->bound || !s->nu) return LRI_ERR_STATE;
+  if (s->step_exec && s->graph_dt != dt) drop_graph(s);
   s->bh_dt = dt;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
-    if (s->dtype == LRI_F32) e = StreamOps<float>{s, st}.burgers_step();
-    else e = StreamOps<double>{s, st}.burgers_step();
+  int k = 0;
+  if (!s->step_exec && nsteps > 1) {
+    // first step eagerly (one-time kernel attributes), then capture
+    e = burgers_step_on(s, st);
+    ++k;
+    if (e == cudaSuccess) capture_step(s);
   }
+  for (; k < nsteps && e == cudaSuccess; ++k)
+    e = s->step_exec ? cudaGraphLaunch(s->step_exec, st) : burgers_step_on(s, st);
   return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
 }
 
 lri_status lri_stream_destroy(lri_stream* s) {
   if (!s) return LRI_ERR_ARG;
+  drop_graph(s);
+  if (s->cap) cudaStreamDestroy(s->cap);
   cudaFree(s->Kp);
   cudaFree(s->Lp);
   cudaFree(s->tv);
@@ -1885,6 +1928,7 @@ lri_status lri_stream_destroy(lri_stream* s) {
 
 lri_status lri_stream_bind(lri_stream* s, void* U, void* S, void* V) {
   if (!s || !U || !S || !V) return LRI_ERR_ARG;
+  drop_graph(s);  // the captured step holds the factor pointers
   s->U = U;
   s->S = S;
   s->V = V;
