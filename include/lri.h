@@ -261,11 +261,15 @@ LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
 /* One large Burgers instance (the Burgers-UQ workload: n grid points x m
  * samples too large for the batch) on the same engine: rank-adaptive BUG
  * (rank_adaptive_unconventional.jl:194-233) for LRI_OP_BURGERS_PERIODIC with
- * the given substep scheme; every flow evaluation F(K V^T) V, F(U L^T)^T U,
- * Uhat^T F(Uhat S Vhat^T) Vhat is a grid of 32 x 32 tiles of Y formed in
- * shared memory, never the n x m matrix.  r_max <= 64.  bind: the caller's
- * U, S, V (as lri_stream_bind) and nu (m viscosities, device).  Destroy with
- * lri_stream_destroy; rank and status as for the stream. */
+ * the given substep scheme.  The flow evaluations F(K V^T) V, F(U L^T)^T U,
+ * Uhat^T F(Uhat S Vhat^T) Vhat never form the n x m matrix: the diffusion
+ * term is (Dxx K)(V^T diag(nu) V), the quadratic terms are Khatri-Rao
+ * products with the symmetric tensor sum_j v_j (x) v_j (x) v_j built once per
+ * step (likewise for the L and S substeps).  r_max <= 64.  bind: the
+ * caller's U, S, V (as lri_stream_bind) and nu (m viscosities, device).
+ * lri_burgers_step with nsteps > 1 runs the first step, captures one step
+ * as a CUDA graph and replays it (kept while dt and the binding stay).
+ * Destroy with lri_stream_destroy; rank and status as for the stream. */
 LRI_API lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_t m, int64_t r0,
                                       int64_t r_max, double tol, int32_t r_min, double h, double alpha,
                                       double beta, const lri_scheme* scheme);

@@ -1683,9 +1683,18 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 // column against a larger one (the FP32 preconditioning sweeps of the mixed
 // SVD, which stop after a few sweeps anyway and leave the larger columns'
 // orthogonality to the polish).
+// A sweep whose largest rotation measure |a_p^T a_q| / (|a_p| |a_q|) is
+// delta leaves the columns orthogonal to O(P delta^2) (each later rotation of
+// the sweep re-creates products of size delta times another delta), so the
+// iteration also ends after a sweep with delta <= conv_delta (default
+// sqrt(eps): P delta^2 is then the rotation threshold itself) instead of
+// spending one more sweep to find nothing to rotate.
+// tiny_abs raises the noise level below which columns are left alone to an
+// absolute squared norm (the caller's truncation level: columns that
+// truncation drops whatever their directions).
 template <typename T, int NTH = NT>
 __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag, int max_sweeps = 40,
-                                        bool skip_noise = true) {
+                                        bool skip_noise = true, double conv_delta = -1.0, double tiny_abs = 0.0) {
   constexpr int NWJ = NTH / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // rotation threshold: P ulps (the rounding level of a length-P dot
@@ -1707,11 +1716,17 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   fro2 = T(0);
   for (int wv = 0; wv < NWJ; ++wv) fro2 += red[wv];
   __syncthreads();
-  const T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
+  T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
+  if (T(tiny_abs) > tiny) tiny = T(tiny_abs);
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
+  const float delta_stop = (float)((conv_delta >= 0.0) ? conv_delta : sqrt(Prec<T>::eps));
+  __shared__ unsigned int dmax_bits;  // largest rotation measure of the sweep (non-negative float bits)
   bool converged = false;
   for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
-    if (tid == 0) *flag = 0;
+    if (tid == 0) {
+      *flag = 0;
+      dmax_bits = 0u;
+    }
     __syncthreads();
     for (int rnd = 0; rnd < Pe - 1; ++rnd) {
       for (int pr = warp; pr < Pe / 2; pr += NWJ) {
@@ -1750,12 +1765,16 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
             vp[i] = cs * x - sn * y;
             vq[i] = sn * x + cs * y;
           }
-          if (lane == 0) *flag = 1;
+          if (lane == 0) {
+            *flag = 1;
+            const float dl = (float)(double)fabs(ga) / ((float)(double)sqrt(al) * (float)(double)sqrt(be));
+            atomicMax(&dmax_bits, __float_as_uint(dl));
+          }
         }
       }
       __syncthreads();
     }
-    converged = (*flag == 0);
+    converged = (*flag == 0) || (__uint_as_float(dmax_bits) <= delta_stop);
     __syncthreads();
   }
   // singular values = column norms
@@ -1790,8 +1809,11 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
 // squared residuals sum to P - j >= 1, so one of them passes).  Any unit
 // direction orthogonal to the others serves: sigma_j is below rounding.
 // scr: P + r1 values of scratch (global or shared).
+// tiny_abs: the absolute squared noise level given to jacobi_svd (columns
+// below 4 tiny_abs are treated the same way).
 template <typename T, int NTH = NT>
-__device__ __noinline__ void complete_left(int P, int r1, T* a, const T* sigma, const int* perm, T* scr) {
+__device__ __noinline__ void complete_left(int P, int r1, T* a, const T* sigma, const int* perm, T* scr,
+                                           double tiny_abs = 0.0) {
   constexpr int NWJ = NTH / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   __shared__ int j0s;
@@ -1808,7 +1830,7 @@ __device__ __noinline__ void complete_left(int P, int r1, T* a, const T* sigma, 
       const double sv = (double)sigma[j];
       fro2 += sv * sv;
     }
-    const double thr2 = 16.0 * Prec<T>::eps * Prec<T>::eps * fro2;
+    const double thr2 = fmax(16.0 * Prec<T>::eps * Prec<T>::eps * fro2, 4.0 * tiny_abs);
     int j0 = r1;
     while (j0 > 0) {
       const double sv = (double)sigma[perm[j0 - 1]];

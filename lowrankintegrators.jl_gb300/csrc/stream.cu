@@ -463,7 +463,8 @@ __device__ void sq_mul(int P, const ST* A, bool ta, const ST* B, ST* C) {
 // singular values FP32 cannot resolve need sweeps to convergence).
 // t1, t2: P*P double-float scratch.
 __device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* perm, int* flag, float* a32,
-                                 float* v32, float* sig32, dfloat* t1, dfloat* t2, int polish_sweeps) {
+                                 float* v32, float* sig32, dfloat* t1, dfloat* t2, int polish_sweeps,
+                                 double tiny_abs = 0.0) {
   for (int o = threadIdx.x; o < P * P; o += NTS) a32[o] = a[o].hi + a[o].lo;
   __syncthreads();
   // FP32 sweeps as a preconditioner: near FP32's resolution limit they need
@@ -486,7 +487,8 @@ __device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* 
   sq_mul<dfloat>(P, a, false, t1, t2);                                               // a X
   for (int o = threadIdx.x; o < P * P; o += NTS) a[o] = t2[o];
   __syncthreads();
-  const bool ok = jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, polish_sweeps);  // polish: a = U S, V_p
+  // polish: a = U S, V_p; to the orthogonality FP32 panels can use (P 1e-10)
+  const bool ok = jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, polish_sweeps, true, 1e-5, tiny_abs);
   sq_mul<dfloat>(P, t1, false, v, t2);                                               // V = X V_p
   for (int o = threadIdx.x; o < P * P; o += NTS) v[o] = t2[o];
   __syncthreads();
@@ -646,6 +648,10 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     a[o] = ST(sacc);
   }
   __syncthreads();
+  // columns with sigma^2 <= tol^2 / (4 wa) are dropped by the truncation
+  // whatever their directions (together they hold less than tol^2 / 4): the
+  // sweeps leave pairs with such a column alone
+  const double tiny_abs = tol * tol / (4.0 * wa);
   bool ok;
   if constexpr (sizeof(ST) == 8 && !std::is_same<ST, double>::value) {
     // double-float: FP32 sweeps, double-float polish (scratch after a in
@@ -657,9 +663,10 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     // largest are beyond what the FP32 sweeps resolve, and their left vectors
     // a_j / sigma_j need the double-float accuracy)
     ok = jacobi_svd_mixed(wa, a, v, sig, perm, &flag, a32, v32, sig32,
-                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa, 40);
+                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa, 40,
+                          tiny_abs);
   } else {
-    ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag);
+    ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag, 40, true, -1.0, tiny_abs);
   }
   if (tid == 0) {
     if (!ok) atomicOr(status, ST_SVD_NOCONV);
@@ -682,7 +689,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   __syncthreads();
   const int r1 = r_new;
   // left vectors a_j / sigma_j in place (P1 as scratch before it is written)
-  complete_left<ST, NTS>(wa, r1, a, sig, perm, reinterpret_cast<ST*>(P1));
+  complete_left<ST, NTS>(wa, r1, a, sig, perm, reinterpret_cast<ST*>(P1), tiny_abs);
   for (int o = tid; o < w * R; o += NTS) P1[o] = Q1[o] = 0.0;
   __syncthreads();
   for (int o = tid; o < wa * r1; o += NTS) {
