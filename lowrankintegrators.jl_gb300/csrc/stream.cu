@@ -668,9 +668,8 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   } else {
     ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag, 40, true, -1.0, tiny_abs);
   }
-  if (tid == 0) {
-    if (!ok) atomicOr(status, ST_SVD_NOCONV);
-    // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R]
+  // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R] (thread 0)
+  auto decide_rank = [&]() {
     const double tol2 = tol * tol;
     double acc = 0.0;
     int rr = wa;
@@ -683,13 +682,37 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     if (r1 > R) r1 = R;
     if (r1 < rmin) r1 = rmin;
     if (r1 > wa) r1 = wa;
-    r_new = r1;
-    *rank = r1;
+    return r1;
+  };
+  __shared__ int redo;
+  if (tid == 0) {
+    r_new = decide_rank();
+    const double sv = to_d(sig[perm[r_new - 1]]);
+    redo = (tiny_abs > 0.0 && sv * sv <= 4.0 * tiny_abs);  // the minimum rank keeps skipped columns
+  }
+  __syncthreads();
+  double tiny_left = tiny_abs;
+  if (redo) {
+    // continue the sweeps without the truncation-level skip (v <- v v2)
+    ST* v2 = reinterpret_cast<ST*>(mx) + (size_t)wa * wa;
+    ST* t2 = reinterpret_cast<ST*>(mx) + (size_t)2 * wa * wa;
+    const double conv = std::is_same<ST, double>::value ? -1.0 : 1e-5;
+    ok = jacobi_svd<ST, NTS>(wa, a, v2, sig, perm, &flag, 40, true, conv, 0.0);
+    sq_mul<ST>(wa, v, false, v2, t2);
+    for (int o = tid; o < wa * wa; o += NTS) v[o] = t2[o];
+    __syncthreads();
+    if (tid == 0) r_new = decide_rank();
+    tiny_left = 0.0;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (!ok) atomicOr(status, ST_SVD_NOCONV);
+    *rank = r_new;
   }
   __syncthreads();
   const int r1 = r_new;
   // left vectors a_j / sigma_j in place (P1 as scratch before it is written)
-  complete_left<ST, NTS>(wa, r1, a, sig, perm, reinterpret_cast<ST*>(P1), tiny_abs);
+  complete_left<ST, NTS>(wa, r1, a, sig, perm, reinterpret_cast<ST*>(P1), tiny_left);
   for (int o = tid; o < w * R; o += NTS) P1[o] = Q1[o] = 0.0;
   __syncthreads();
   for (int o = tid; o < wa * r1; o += NTS) {
