@@ -1041,58 +1041,80 @@ __global__ void stencil_panel(int N, int R, int aug, const int32_t* __restrict__
   }
 }
 
+// One explicit RK stage update fused into the kernel that assembles the
+// stage derivative v (tableau with sub-diagonal a only, as lri_scheme):
+// acc = (first ? 0 : acc) + b v; before the last stage the next stage input
+// z = y + h a_{s+1} v, at the last stage y += h acc.
+template <typename T>
+struct RkStage {
+  T b, ha, h;
+  int first, last;
+  T* y;
+  T* z;
+  T* acc;
+};
+template <typename T>
+__device__ __forceinline__ void rk_apply(const RkStage<T>& c, int64_t o, T v) {
+  const T a = c.first ? c.b * v : fma(c.b, v, c.acc[o]);
+  if (c.last) {
+    c.y[o] = fma(c.h, a, c.y[o]);
+  } else {
+    c.acc[o] = a;
+    c.z[o] = fma(c.ha, v, c.y[o]);
+  }
+}
+
 // out = lin + alpha sum_z part1[z] + beta Dx(sum_z part2[z]) on the active
 // columns (lin, part1, part2 may be null), zero elsewhere; ihx = 1 / 2h.
 template <typename T>
 __global__ void flow_combine(int N, int R, int aug, const int32_t* __restrict__ rank, const T* __restrict__ lin,
                              const T* __restrict__ part1, const T* __restrict__ part2, int nz, double alpha,
-                             double beta, double ihx, T* __restrict__ out) {
+                             double beta, double ihx, T* __restrict__ out, RkStage<T> rk) {
   const int r = min(R, (int)*rank);
   const int wcols = aug ? 2 * R : R;
   const int64_t len = (int64_t)N * wcols, zs = (int64_t)N * 2 * R;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(o % N), col = (int)(o / N);
-    if ((col % R) >= r) {
-      out[o] = T(0);
-      continue;
-    }
-    T v = lin ? lin[o] : T(0);
-    if (part1) {
-      T s = T(0);
-      for (int z = 0; z < nz; ++z) s += part1[z * zs + o];
-      v = fma(T(alpha), s, v);
-    }
-    if (part2) {
-      const int64_t om = o - i + ((i == 0) ? N - 1 : i - 1), op = o - i + ((i == N - 1) ? 0 : i + 1);
-      T sm = T(0), sp = T(0);
-      for (int z = 0; z < nz; ++z) {
-        sm += part2[z * zs + om];
-        sp += part2[z * zs + op];
+    T v = T(0);
+    if ((col % R) < r) {
+      v = lin ? lin[o] : T(0);
+      if (part1) {
+        T sacc = T(0);
+        for (int z = 0; z < nz; ++z) sacc += part1[z * zs + o];
+        v = fma(T(alpha), sacc, v);
       }
-      v = fma(T(beta * ihx), sp - sm, v);
+      if (part2) {
+        const int64_t om = o - i + ((i == 0) ? N - 1 : i - 1), op = o - i + ((i == N - 1) ? 0 : i + 1);
+        T sm = T(0), sp = T(0);
+        for (int z = 0; z < nz; ++z) {
+          sm += part2[z * zs + om];
+          sp += part2[z * zs + op];
+        }
+        v = fma(T(beta * ihx), sp - sm, v);
+      }
     }
-    out[o] = v;
+    if (rk.y) rk_apply(rk, o, v);
+    else out[o] = v;
   }
 }
 
-// out[j, c] = nu_j lin[j, c] + sum_z part[z][j, c] (L substep: F(U L^T)^T U =
-// diag(nu) L (U^T Dxx U) + KR(L, L) T'_L), active columns, zero elsewhere.
+// v[j, c] = nu_j lin[j, c] + sum_z part[z][j, c] (L substep: F(U L^T)^T U =
+// diag(nu) L (U^T Dxx U) + KR(L, L) T'_L) on the active columns, zero
+// elsewhere, fused with the RK stage update.
 template <typename T>
 __global__ void flow_combine_rows(int M, int R, const int32_t* __restrict__ rank, const T* __restrict__ nu,
-                                  const T* __restrict__ lin, const T* __restrict__ part, int nz,
-                                  T* __restrict__ out) {
+                                  const T* __restrict__ lin, const T* __restrict__ part, int nz, RkStage<T> rk) {
   const int r = min(R, (int)*rank);
   const int64_t len = (int64_t)M * R, zs = (int64_t)M * 2 * R;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
     const int j = (int)(o % M), col = (int)(o / M);
-    if (col >= r) {
-      out[o] = T(0);
-      continue;
+    T v = T(0);
+    if (col < r) {
+      v = nu[j] * lin[o];
+      if (part)
+        for (int z = 0; z < nz; ++z) v += part[z * zs + o];
     }
-    T v = nu[j] * lin[o];
-    if (part)
-      for (int z = 0; z < nz; ++z) v += part[z * zs + o];
-    out[o] = v;
+    rk_apply(rk, o, v);
   }
 }
 
@@ -1105,20 +1127,41 @@ __global__ void scale_rows(int N, int cols, const T* __restrict__ X, const T* __
 }
 
 // C = A B on the active block of w x w FP64 matrices (ld w = 2R; active
-// indices: the first r of each half); one thread per entry.  The other
-// entries of C are left alone.
-__global__ void small_gemm_act(int R, const int32_t* __restrict__ rank, const double* __restrict__ A,
-                               const double* __restrict__ B, double* __restrict__ C) {
+// indices: the first r of each half), products summed in T (the S flow's
+// A_xx S N_nu, a stage derivative: FP32 sums for FP32 panels); one CTA per
+// 32 x 32 tile of the active block.  The other entries of C are left alone.
+template <typename T>
+__global__ void __launch_bounds__(256) small_gemm_act(int R, const int32_t* __restrict__ rank,
+                                                      const double* __restrict__ A, const double* __restrict__ B,
+                                                      double* __restrict__ C) {
   const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
-  const int64_t len = (int64_t)ka * ka;
-  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
-    const int i = act_col((int)(o % ka), r, R), j = act_col((int)(o / ka), r, R);
-    double s = 0.0;
-    for (int k = 0; k < ka; ++k) {
-      const int kk = act_col(k, r, R);
-      s = fma(A[i + (int64_t)kk * w], B[kk + (int64_t)j * w], s);
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  if (i0 >= ka || j0 >= ka) return;
+  __shared__ T as[32][33];
+  __shared__ T bs[32][33];
+  const int tid = threadIdx.x, ti = tid & 31, tj = tid >> 5;
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  for (int k0 = 0; k0 < ka; k0 += 32) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int x = e & 31, y = e >> 5;
+      as[x][y] = (i0 + x < ka && k0 + y < ka)
+                     ? T(A[act_col(i0 + x, r, R) + (int64_t)act_col(k0 + y, r, R) * w]) : T(0);
+      bs[x][y] = (k0 + x < ka && j0 + y < ka)
+                     ? T(B[act_col(k0 + x, r, R) + (int64_t)act_col(j0 + y, r, R) * w]) : T(0);
     }
-    C[i + (int64_t)j * w] = s;
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+      const T a = as[ti][k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = fma(a, bs[k][tj + 8 * q], acc[q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + ti, j = j0 + tj + 8 * q;
+    if (i < ka && j < ka) C[act_col(i, r, R) + (int64_t)act_col(j, r, R) * w] = (double)acc[q];
   }
 }
 
@@ -1224,16 +1267,18 @@ __global__ void __launch_bounds__(256) gram_act(int N, int R, const int32_t* __r
   }
 }
 
-// C[a, c] += sum_z part[z][a, c] on the active block (fixed order)
-__global__ void gram_act_reduce(int R, const int32_t* __restrict__ rank, int nz, const double* __restrict__ part,
-                                double* __restrict__ C) {
+// S-flow stage: v[a, c] = C[a, c] + sum_z part[z][a, c] (fixed order; C holds
+// A_xx S N_nu) on the active block, then the RK stage update of the FP64
+// w x w stage arrays.
+__global__ void s_stage_finish(int R, const int32_t* __restrict__ rank, int nz, const double* __restrict__ part,
+                               const double* __restrict__ C, RkStage<double> rk) {
   const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
   const int64_t len = (int64_t)ka * ka;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
     const int64_t idx = act_col((int)(o % ka), r, R) + (int64_t)act_col((int)(o / ka), r, R) * w;
-    double sacc = 0.0;
-    for (int z = 0; z < nz; ++z) sacc += part[z * (int64_t)w * w + idx];
-    C[idx] += sacc;
+    double v = C[idx];
+    for (int z = 0; z < nz; ++z) v += part[z * (int64_t)w * w + idx];
+    rk_apply(rk, idx, v);
   }
 }
 
@@ -1528,30 +1573,22 @@ struct StreamOps {
     return cudaGetLastError();
   }
   // one RK substep sequence of a panel flow y' = f(y) (N x R): y in P[0],
-  // stage input P[1], derivative P[2], accumulator P[3]; f writes P[2].
+  // stage input P[1], accumulator P[3]; f(stage input, RkStage) launches
+  // the kernels of one stage, the last of which applies the stage update.
   template <class F>
   cudaError_t rk_panel(int64_t len, T* P, const F& f) const {
     const Scheme& sc = s->sc;
     const T h = T(s->bh_dt / sc.nsub);
     T* y = P;
     T* z = P + len;
-    T* k = P + 2 * len;
     T* acc = P + 3 * len;
-    const int g = 304;
     cudaError_t e = cudaSuccess;
-    for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
+    for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub)
       for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
-        if ((e = f(st_ == 0 ? y : z, k)) != cudaSuccess) break;
-        if (st_ == 0) axpbz<T><<<g, 256, 0, st>>>(len, T(sc.b[0]), k, T(0), nullptr, acc);
-        else axpbz<T><<<g, 256, 0, st>>>(len, T(1), acc, T(sc.b[st_]), k, acc);
-        if (st_ + 1 < sc.nstages) axpbz<T><<<g, 256, 0, st>>>(len, T(1), y, T(h * T(sc.a[st_ + 1])), k, z);
-        e = cudaGetLastError();
+        const bool last = (st_ + 1 == sc.nstages);
+        const RkStage<T> c{T(sc.b[st_]), last ? T(0) : T(h * T(sc.a[st_ + 1])), h, st_ == 0, last, y, z, acc};
+        e = f(st_ == 0 ? y : z, c);
       }
-      if (e == cudaSuccess) {
-        axpbz<T><<<g, 256, 0, st>>>(len, T(1), y, h, acc, y);
-        e = cudaGetLastError();
-      }
-    }
     return e;
   }
 
@@ -1627,7 +1664,7 @@ struct StreamOps {
     T* Kp = tp(s->Kp);
     if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
     const int zk = kz(n, 0);
-    e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, T* out) {
+    e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, const RkStage<T>& rk) {
       stencil_panel<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, Z, ih2, P0, ihx, ba != 0.0 ? P1 : nullptr);
       panel_mul_act<T><<<dim3((n + 31) / 32, (R + 63) / 64), 256, 0, st>>>(n, R, 0, s->d_rank, P0, Nnu, R, P2);
       cudaError_t e2 = cudaGetLastError();
@@ -1636,7 +1673,7 @@ struct StreamOps {
       if (e2 == cudaSuccess && bb != 0.0) e2 = apply(n, 0, Z, Z, tp(s->tv), kap2);
       if (e2 != cudaSuccess) return e2;
       flow_combine<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, P2, ba != 0.0 ? kap1 : nullptr,
-                                         bb != 0.0 ? kap2 : nullptr, zk, ba, bb, ihx, out);
+                                         bb != 0.0 ? kap2 : nullptr, zk, ba, bb, ihx, nullptr, rk);
       return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -1644,12 +1681,12 @@ struct StreamOps {
     T* Lp = tp(s->Lp);
     if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
     const int zl = kz(m, 0);
-    e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, T* out) {
+    e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
       panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
       cudaError_t e2 = cudaGetLastError();
       if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
       if (e2 != cudaSuccess) return e2;
-      flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, out);
+      flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, rk);
       return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -1683,13 +1720,17 @@ struct StreamOps {
       double* Sz = blk(19);
       double* Sk = blk(20);
       double* Sa = blk(21);
-      const int64_t len = (int64_t)w * w;
       const int zs = kz(n, 1);
+      const int nzg = (n + GA_ROWS - 1) / GA_ROWS;
+      double* gpart = reinterpret_cast<double*>(s->kgp);  // free during the S substep
+      const dim3 gsm((w + 31) / 32, (w + 31) / 32);
       for (int sub = 0; sub < sc.nsub && e == cudaSuccess; ++sub) {
         for (int st_ = 0; st_ < sc.nstages && e == cudaSuccess; ++st_) {
           const double* Z = (st_ == 0) ? Sy : Sz;
-          small_gemm_act<<<64, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
-          small_gemm_act<<<64, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
+          const bool last = (st_ + 1 == sc.nstages);
+          const RkStage<double> rk{sc.b[st_], last ? 0.0 : h * sc.a[st_ + 1], h, st_ == 0, last, Sy, Sz, Sa};
+          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
+          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
           if (nonlin) {
             panel_mul_act<T><<<dim3((n + 31) / 32, (w + 63) / 64), 256, 0, st>>>(n, R, 1, s->d_rank, Uh, Z, w, P0);
             if (ba != 0.0) {
@@ -1699,21 +1740,10 @@ struct StreamOps {
             }
             if (bb != 0.0 && (e = apply(n, 1, P0, P0, tp(s->th), kap2)) != cudaSuccess) break;
             flow_combine<T><<<g, 256, 0, st>>>(n, R, 1, s->d_rank, nullptr, ba != 0.0 ? kap1 : nullptr,
-                                               bb != 0.0 ? kap2 : nullptr, zs, ba, bb, ihx, P2);
-            {
-              const int nzg = (n + GA_ROWS - 1) / GA_ROWS;
-              double* gpart = reinterpret_cast<double*>(s->kgp);  // free during the S substep
-              gram_act<T><<<dim3((w + 31) / 32, (w + 31) / 32, nzg), 256, 0, st>>>(n, R, s->d_rank, Uh, P2, gpart);
-              gram_act_reduce<<<64, 256, 0, st>>>(R, s->d_rank, nzg, gpart, Sk);
-            }
+                                               bb != 0.0 ? kap2 : nullptr, zs, ba, bb, ihx, P2, RkStage<T>{});
+            gram_act<T><<<dim3((w + 31) / 32, (w + 31) / 32, nzg), 256, 0, st>>>(n, R, s->d_rank, Uh, P2, gpart);
           }
-          if (st_ == 0) axpbz<double><<<64, 256, 0, st>>>(len, sc.b[0], Sk, 0.0, nullptr, Sa);
-          else axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sa, sc.b[st_], Sk, Sa);
-          if (st_ + 1 < sc.nstages) axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sy, h * sc.a[st_ + 1], Sk, Sz);
-          e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) {
-          axpbz<double><<<64, 256, 0, st>>>(len, 1.0, Sy, h, Sa, Sy);
+          s_stage_finish<<<64, 256, 0, st>>>(R, s->d_rank, nonlin ? nzg : 0, gpart, Sk, rk);
           e = cudaGetLastError();
         }
       }
