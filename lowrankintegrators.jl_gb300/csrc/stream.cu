@@ -386,6 +386,10 @@ __device__ __forceinline__ double to_d(double x) { return x; }
 __device__ __forceinline__ double to_d(dfloat x) { return (double)x; }
 
 constexpr int NTS = 1024;  // threads of the single-CTA kernels
+constexpr size_t CORE_MAT = 160 * 1024;  // core_step's shared-memory matrix area (+ 40 KB of tiles)
+
+// active column j (0 <= j < ka) -> panel column: the first r of each half
+__device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
 
 // One CholeskyQR factor: G + shift_rel * trace(G) I = R^T R (a x a, ld a),
 // Bout = R^{-1}; columns with G_jj <= tol_rel * max G_jj are decoupled
@@ -442,29 +446,51 @@ __global__ void __launch_bounds__(NTS) chol_inv_factor(int a, const double* __re
   for (int o = tid; o < a * a; o += NTS) Bout[o] = to_d(Ri[o]);
 }
 
-// C (P x P, ld P) = op(A) B with op(A) = A or A^T, all in ST, NTS threads.
+// C (P x P, ld P) = op(A) B with op(A) = A or A^T, all in ST, NTS = 1024
+// threads: 32 x 32 output tiles (one entry per thread) over 32-wide k
+// chunks staged in shared memory (tile: 2 * 32 * 33 ST).  C must not alias
+// A or B.
 template <typename ST>
-__device__ void sq_mul(int P, const ST* A, bool ta, const ST* B, ST* C) {
-  for (int o = threadIdx.x; o < P * P; o += NTS) {
-    const int i = o % P, j = o / P;
-    ST acc(0.0);
-    for (int k = 0; k < P; ++k) acc = fma_acc(ta ? A[k + i * P] : A[i + k * P], B[k + j * P], acc);
-    C[o] = renorm(acc);
-  }
+__device__ void sq_mul(int P, const ST* A, bool ta, const ST* B, ST* C, ST* tile) {
+  static_assert(NTS == 1024, "one 32 x 32 tile per pass");
+  ST* As = tile;
+  ST* Bs = tile + 32 * 33;
+  const int tid = threadIdx.x, ti = tid & 31, tj = tid >> 5;
+  const int nt = (P + 31) / 32;
+  for (int tI = 0; tI < nt; ++tI)
+    for (int tJ = 0; tJ < nt; ++tJ) {
+      ST acc(0.0);
+      for (int k0 = 0; k0 < P; k0 += 32) {
+        {
+          const int i = tI * 32 + ti, k = k0 + tj;
+          As[ti * 33 + tj] = (i < P && k < P) ? (ta ? A[k + i * P] : A[i + k * P]) : ST(0.0);
+          const int kk = k0 + ti, j = tJ * 32 + tj;
+          Bs[ti * 33 + tj] = (kk < P && j < P) ? B[kk + j * P] : ST(0.0);
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) acc = fma_acc(As[ti * 33 + k], Bs[k * 33 + tj], acc);
+        __syncthreads();
+      }
+      const int i = tI * 32 + ti, j = tJ * 32 + tj;
+      if (i < P && j < P) C[i + j * P] = renorm(acc);
+    }
   __syncthreads();
 }
 
-// SVD of the P x P double-float matrix a (in place; right vectors to v): the
-// Jacobi sweeps run in FP32 (a32, v32: P*P floats each), the FP32 right
-// vectors are made orthonormal to double-float precision by two Newton-Schulz
-// steps X <- X (3I - X^T X) / 2, a <- a X, and double-float sweeps polish the
-// rotated matrix (its columns are then orthogonal to FP32 precision, so one
-// sweep squares that for well-separated singular values; directions whose
-// singular values FP32 cannot resolve need sweeps to convergence).
-// t1, t2: P*P double-float scratch.
-__device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* perm, int* flag, float* a32,
-                                 float* v32, float* sig32, dfloat* t1, dfloat* t2, int polish_sweeps,
-                                 double tiny_abs = 0.0) {
+// SVD of the P x P double-float matrix a (global, read only; right vectors
+// to v): the Jacobi sweeps run in FP32 (a32, v32: P*P floats each, shared
+// memory when they fit), the FP32 right vectors are made orthonormal to
+// double-float precision by two Newton-Schulz steps X <- X (3I - X^T X) / 2,
+// as = a X, and double-float sweeps polish the rotated matrix as (shared
+// memory when it fits; it may overlay a32/v32, which are dead by then).  The
+// columns of a X are orthogonal to FP32 precision, so one sweep squares that
+// for well-separated singular values; directions whose singular values FP32
+// cannot resolve need more sweeps.  t1, t2: P*P double-float scratch
+// (global); tile: sq_mul's shared-memory tiles.
+__device__ bool jacobi_svd_mixed(int P, const dfloat* a, dfloat* as, dfloat* v, dfloat* sig, int* perm, int* flag,
+                                 float* a32, float* v32, float* sig32, dfloat* t1, dfloat* t2, dfloat* tile,
+                                 int polish_sweeps, double tiny_abs = 0.0) {
   for (int o = threadIdx.x; o < P * P; o += NTS) a32[o] = a[o].hi + a[o].lo;
   __syncthreads();
   // FP32 sweeps as a preconditioner: near FP32's resolution limit they need
@@ -474,22 +500,22 @@ __device__ bool jacobi_svd_mixed(int P, dfloat* a, dfloat* v, dfloat* sig, int* 
   for (int o = threadIdx.x; o < P * P; o += NTS) t1[o] = dfloat(v32[o], 0.0f);  // X0 = V32
   __syncthreads();
   for (int it = 0; it < 2; ++it) {
-    sq_mul<dfloat>(P, t1, true, t1, t2);                                             // X^T X
+    sq_mul<dfloat>(P, t1, true, t1, t2, tile);                                       // X^T X
     for (int o = threadIdx.x; o < P * P; o += NTS) {
       const int i = o % P, j = o / P;
       t2[o] = ((i == j) ? dfloat(1.5f, 0.0f) : dfloat(0.0f, 0.0f)) - dfloat(0.5f, 0.0f) * t2[o];
     }
     __syncthreads();
-    sq_mul<dfloat>(P, t1, false, t2, v);                                             // X (3I - X^T X)/2
+    sq_mul<dfloat>(P, t1, false, t2, v, tile);                                       // X (3I - X^T X)/2
     for (int o = threadIdx.x; o < P * P; o += NTS) t1[o] = v[o];
     __syncthreads();
   }
-  sq_mul<dfloat>(P, a, false, t1, t2);                                               // a X
-  for (int o = threadIdx.x; o < P * P; o += NTS) a[o] = t2[o];
+  sq_mul<dfloat>(P, a, false, t1, t2, tile);                                         // a X
+  for (int o = threadIdx.x; o < P * P; o += NTS) as[o] = t2[o];
   __syncthreads();
   // polish: a = U S, V_p; to the orthogonality FP32 panels can use (P 1e-10)
-  const bool ok = jacobi_svd<dfloat, NTS>(P, a, v, sig, perm, flag, polish_sweeps, true, 1e-5, tiny_abs);
-  sq_mul<dfloat>(P, t1, false, v, t2);                                               // V = X V_p
+  const bool ok = jacobi_svd<dfloat, NTS>(P, as, v, sig, perm, flag, polish_sweeps, true, 1e-5, tiny_abs);
+  sq_mul<dfloat>(P, t1, false, v, t2, tile);                                         // V = X V_p
   for (int o = threadIdx.x; o < P * P; o += NTS) v[o] = t2[o];
   __syncthreads();
   return ok;
@@ -606,6 +632,37 @@ __global__ void __launch_bounds__(NTS) pchol_factor(int a, const double* __restr
   }
 }
 
+// The active block of S~ = Mh S0 Nh^T + D (FP64, compact wa x wa, ld wa),
+// wa = 2r, for core_step: form_t1 (T1 = S0 Nh^T, r x wa, ld r), then
+// form_core; one thread per entry over the whole GPU (the products are
+// r^2 wa + r wa^2 FP64 multiply-adds, far too slow on one SM).
+template <typename T>
+__global__ void form_t1(int R, const int32_t* __restrict__ rank, const T* __restrict__ S0,
+                        const double* __restrict__ Nh, double* __restrict__ T1) {
+  const int r = min(R, (int)*rank), wa = 2 * r, w = 2 * R;
+  const int64_t len = (int64_t)r * wa;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(o % r), j = (int)(o / r);
+    const int jj = act_col(j, r, R);
+    double sacc = 0.0;
+#pragma unroll 8
+    for (int k = 0; k < r; ++k) sacc = fma((double)S0[i + (int64_t)k * R], Nh[jj + (int64_t)k * w], sacc);
+    T1[o] = sacc;
+  }
+}
+__global__ void form_core(int R, const int32_t* __restrict__ rank, const double* __restrict__ Mh,
+                          const double* __restrict__ T1, const double* __restrict__ D, double* __restrict__ F) {
+  const int r = min(R, (int)*rank), wa = 2 * r, w = 2 * R;
+  const int64_t len = (int64_t)wa * wa;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
+    const int i = act_col((int)(o % wa), r, R), j = (int)(o / wa);
+    double sacc = D[i + (int64_t)act_col(j, r, R) * w];
+#pragma unroll 8
+    for (int k = 0; k < r; ++k) sacc = fma(Mh[i + (int64_t)k * w], T1[k + (int64_t)j * r], sacc);
+    F[o] = sacc;
+  }
+}
+
 // S-step core and truncation.  In: Mh = Uhat^T U0 (w x R), Nh = Vhat^T V0
 // (w x R), D = Uhat^T dY Vhat (w x w), S0 (R x R, T), rank (device).  Out:
 // P1, Q1 (w x R FP64: the kept left / right singular vectors, zero beyond
@@ -614,11 +671,10 @@ __global__ void __launch_bounds__(NTS) pchol_factor(int a, const double* __restr
 // O(w u) rotation error per sweep) with the w x w matrix in shared memory
 // when it fits, else in the global scratch ag; the right vectors in vg.
 template <typename T, typename ST>
-__global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict__ Mh, const double* __restrict__ Nh,
-                                                 const double* __restrict__ D, T* S0, int32_t* rank, double tol,
-                                                 int rmin, ST* __restrict__ ag, ST* __restrict__ vg,
+__global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict__ F, T* S0, int32_t* rank,
+                                                 double tol, int rmin, ST* __restrict__ ag, ST* __restrict__ vg,
                                                  double* __restrict__ P1, double* __restrict__ Q1, uint32_t* status,
-                                                 int smem_bytes, double* __restrict__ mx) {
+                                                 double* __restrict__ mx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ __align__(16) unsigned char sig_raw[2 * SMAX * sizeof(ST)];
   ST* sig = reinterpret_cast<ST*>(sig_raw);
@@ -630,23 +686,13 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   // active rows / columns: the first r of each half of [U0 | Q] ([V0 | Q])
   const int r = min(R, (int)*rank), wa = 2 * r;
   auto idx = [&](int i) { return (i < r) ? i : R + (i - r); };
-  const bool a_in_smem = (size_t)wa * wa * sizeof(ST) <= (size_t)smem_bytes;
-  ST* a = a_in_smem ? reinterpret_cast<ST*>(smraw) : ag;  // wa x wa
-  ST* v = vg;                                              // wa x wa
-  // T1 = S0 N^T (r x wa) into v; a = M T1 + D on the active block (FP64 products)
-  for (int o = tid; o < r * wa; o += NTS) {
-    const int i = o % r, j = o / r;
-    double sacc = 0.0;
-    for (int k = 0; k < r; ++k) sacc = fma((double)S0[i + (int64_t)k * R], Nh[idx(j) + (int64_t)k * w], sacc);
-    v[i + (int64_t)j * r] = ST(sacc);
-  }
-  __syncthreads();
-  for (int o = tid; o < wa * wa; o += NTS) {
-    const int i = o % wa, j = o / wa;
-    double sacc = D[idx(i) + (int64_t)idx(j) * w];
-    for (int k = 0; k < r; ++k) sacc = fma(Mh[idx(i) + (int64_t)k * w], to_d(v[k + (int64_t)j * r]), sacc);
-    a[o] = ST(sacc);
-  }
+  // shared memory: [0, CORE_MAT) the wa x wa matrix being rotated (or the
+  // two FP32 matrices of the mixed SVD) when it fits, then sq_mul's tiles
+  const bool a_in_smem = (size_t)wa * wa * sizeof(ST) <= CORE_MAT;
+  ST* tile = reinterpret_cast<ST*>(smraw + CORE_MAT);
+  ST* a = ag;  // wa x wa; the rotated matrix of the polish, below
+  ST* v = vg;  // wa x wa
+  for (int o = tid; o < wa * wa; o += NTS) a[o] = ST(F[o]);
   __syncthreads();
   // columns with sigma^2 <= tol^2 / (4 wa) are dropped by the truncation
   // whatever their directions (together they hold less than tol^2 / 4): the
@@ -654,18 +700,26 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   const double tiny_abs = tol * tol / (4.0 * wa);
   bool ok;
   if constexpr (sizeof(ST) == 8 && !std::is_same<ST, double>::value) {
-    // double-float: FP32 sweeps, double-float polish (scratch after a in
-    // shared memory when it fits, else in the global scratch mx)
-    float* a32 = reinterpret_cast<float*>(mx);
+    // double-float: FP32 sweeps, double-float polish; the FP32 pair and
+    // then the polished matrix in shared memory when they fit (same bytes)
+    float* a32 = a_in_smem ? reinterpret_cast<float*>(smraw) : reinterpret_cast<float*>(mx);
     float* v32 = a32 + wa * wa;
     __shared__ float sig32[2 * SMAX];
+    ST* as = a_in_smem ? reinterpret_cast<ST*>(smraw) : ag;
     // (double-float sweeps to convergence: kept singular values far below the
     // largest are beyond what the FP32 sweeps resolve, and their left vectors
     // a_j / sigma_j need the double-float accuracy)
-    ok = jacobi_svd_mixed(wa, a, v, sig, perm, &flag, a32, v32, sig32,
-                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa, 40,
+    ok = jacobi_svd_mixed(wa, ag, as, v, sig, perm, &flag, a32, v32, sig32,
+                          reinterpret_cast<ST*>(mx) + wa * wa, reinterpret_cast<ST*>(mx) + 2 * wa * wa, tile, 40,
                           tiny_abs);
+    a = as;
   } else {
+    if (a_in_smem) {
+      ST* as = reinterpret_cast<ST*>(smraw);
+      for (int o = tid; o < wa * wa; o += NTS) as[o] = a[o];
+      __syncthreads();
+      a = as;
+    }
     ok = jacobi_svd<ST, NTS>(wa, a, v, sig, perm, &flag, 40, true, -1.0, tiny_abs);
   }
   // smallest r1 with sum_{j > r1} sigma_j^2 < tol^2, then [rmin, R] (thread 0)
@@ -698,7 +752,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     ST* t2 = reinterpret_cast<ST*>(mx) + (size_t)2 * wa * wa;
     const double conv = std::is_same<ST, double>::value ? -1.0 : 1e-5;
     ok = jacobi_svd<ST, NTS>(wa, a, v2, sig, perm, &flag, 40, true, conv, 0.0);
-    sq_mul<ST>(wa, v, false, v2, t2);
+    sq_mul<ST>(wa, v, false, v2, t2, tile);
     for (int o = tid; o < wa * wa; o += NTS) v[o] = t2[o];
     __syncthreads();
     if (tid == 0) r_new = decide_rank();
@@ -755,8 +809,6 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
 // ---------------------------------------------------------------------------
 constexpr int KR_ROWS = 1024;  // rows per split of the tensor sums
 
-// active column j (0 <= j < ka) -> panel column: the first r of each half
-__device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
 __device__ __forceinline__ int active_cols(const int32_t* rank, int R, int aug) {
   const int r = min(R, (int)*rank);
   return aug ? 2 * r : r;
@@ -1762,19 +1814,21 @@ struct StreamOps {
     const int R = (int)s->R;
     T* S = tp(s->S);
     cudaError_t e;
-    // the active 2r x 2r matrix in shared memory when it fits (200 KB)
-    const int abytes = 200 * 1024;
+    const int abytes = 200 * 1024;  // CORE_MAT + tiles
     static bool attr_set = false;
     if (!attr_set) {
-      if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+      if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, abytes)) !=
           cudaSuccess)
         return e;
       attr_set = true;
     }
+    // S~ = Mh S0 Nh^T + D on the active block, over the whole GPU (T1 in block 14, S~ in block 13)
+    form_t1<T><<<64, 256, 0, st>>>(R, s->d_rank, S, blk(4), blk(14));
+    form_core<<<128, 256, 0, st>>>(R, s->d_rank, blk(3), blk(14), blk(5), blk(13));
     ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
     // blocks 10..12: FP32 copies and double-float products of the mixed-precision SVD
-    core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(3), blk(4), blk(5), S, s->d_rank, s->tol, s->rmin, scr,
-                                             scr + (int64_t)w * w, blk(8), blk(9), s->d_status, abytes, blk(10));
+    core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(13), S, s->d_rank, s->tol, s->rmin, scr, scr + (int64_t)w * w,
+                                             blk(8), blk(9), s->d_status, blk(10));
     return cudaGetLastError();
   }
 
