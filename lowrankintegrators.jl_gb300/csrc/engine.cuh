@@ -1719,6 +1719,13 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
   if (T(tiny_abs) > tiny) tiny = T(tiny_abs);
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
+  // lanes per pair G (32, 16, 8 or 4): enough pairs per pass for every warp,
+  // so the per-pair reductions and rotation arithmetic are shared by a warp's
+  // groups instead of repeated per pair
+  const int npair = Pe / 2;
+  int G = 32;
+  while (G > 4 && NWJ * (32 / G) < npair) G >>= 1;
+  const int gpw = 32 / G, gid = lane / G, gl = lane % G;
   const float delta_stop = (float)((conv_delta >= 0.0) ? conv_delta : sqrt(Prec<T>::eps));
   __shared__ unsigned int dmax_bits;  // largest rotation measure of the sweep (non-negative float bits)
   bool converged = false;
@@ -1729,22 +1736,33 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
     }
     __syncthreads();
     for (int rnd = 0; rnd < Pe - 1; ++rnd) {
-      for (int pr = warp; pr < Pe / 2; pr += NWJ) {
-        int p, q;
-        if (pr == 0) { p = rnd % (Pe - 1); q = Pe - 1; }
-        else { p = (rnd + pr) % (Pe - 1); q = (rnd - pr + (Pe - 1)) % (Pe - 1); }
-        if (p >= P || q >= P) continue;
-        if (p > q) { int tmp = p; p = q; q = tmp; }
+      // warp-uniform loop; each group of G lanes takes one pair
+      for (int base = warp * gpw; base < npair; base += NWJ * gpw) {
+        const int pr = base + gid;
+        int p = 0, q = 0;
+        bool valid = pr < npair;
+        if (valid) {
+          if (pr == 0) { p = rnd % (Pe - 1); q = Pe - 1; }
+          else { p = (rnd + pr) % (Pe - 1); q = (rnd - pr + (Pe - 1)) % (Pe - 1); }
+          valid = p < P && q < P;
+          if (p > q) { int tmp = p; p = q; q = tmp; }
+        }
+        if (!valid) p = q = 0;
         T* ap = a + p * P;
         T* aq = a + q * P;
         T al = T(0), be = T(0), ga = T(0);
-        for (int i = lane; i < P; i += 32) {
-          const T x = ap[i], y = aq[i];
-          al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
+        if (valid)
+          for (int i = gl; i < P; i += G) {
+            const T x = ap[i], y = aq[i];
+            al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
+          }
+        for (int o = G >> 1; o > 0; o >>= 1) {  // group sums (all lanes take part)
+          al += shfl_xor(al, o);
+          be += shfl_xor(be, o);
+          ga += shfl_xor(ga, o);
         }
-        al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
         // (sqrt(al) * sqrt(be): al * be can leave the FP32 exponent range)
-        const bool live = skip_noise ? (al > tiny && be > tiny) : (al > tiny || be > tiny);
+        const bool live = valid && (skip_noise ? (al > tiny && be > tiny) : (al > tiny || be > tiny));
         if (live && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
           const T zeta = (be - al) / (T(2) * ga);
           // for large |zeta| use tan = 1/(2 zeta): zeta^2 would leave the FP32
@@ -1753,19 +1771,19 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
                                                  : copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
           const T cs = T(1) / sqrt(T(1) + tt * tt);
           const T sn = cs * tt;
-          for (int i = lane; i < P; i += 32) {
+          for (int i = gl; i < P; i += G) {
             const T x = ap[i], y = aq[i];
             ap[i] = cs * x - sn * y;
             aq[i] = sn * x + cs * y;
           }
           T* vp = v + p * P;
           T* vq = v + q * P;
-          for (int i = lane; i < P; i += 32) {
+          for (int i = gl; i < P; i += G) {
             const T x = vp[i], y = vq[i];
             vp[i] = cs * x - sn * y;
             vq[i] = sn * x + cs * y;
           }
-          if (lane == 0) {
+          if (gl == 0) {
             *flag = 1;
             const float dl = (float)(double)fabs(ga) / ((float)(double)sqrt(al) * (float)(double)sqrt(be));
             atomicMax(&dmax_bits, __float_as_uint(dl));

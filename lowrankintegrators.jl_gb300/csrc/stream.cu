@@ -36,7 +36,7 @@ namespace lri {
 namespace {
 
 constexpr int SMAX = 96;      // largest r_max
-constexpr int GROWS = 512;    // rows per Gram partial block
+constexpr int GROWS = 128;    // rows per Gram partial block (a few hundred CTAs for the panels here)
 
 // ---------------------------------------------------------------------------
 // Streaming pass A: out (n x c) = dY B,  dY = A1 - A0 (n x m, col-major),
@@ -359,6 +359,12 @@ __global__ void __launch_bounds__(256) panel_mul_df(int N, int a, int c, const f
   }
 }
 
+// B = (3I - G) / 2 (R x R): one Newton-Schulz step X <- X B for G = X^T X
+__global__ void ns_factor(int R, const double* __restrict__ G, double* __restrict__ B) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < R * R) B[o] = ((o % R == o / R) ? 1.5 : 0.0) - 0.5 * G[o];
+}
+
 __global__ void negate(int k, double* x) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o < k) x[o] = -x[o];
@@ -513,8 +519,10 @@ __device__ bool jacobi_svd_mixed(int P, const dfloat* a, dfloat* as, dfloat* v, 
   sq_mul<dfloat>(P, a, false, t1, t2, tile);                                         // a X
   for (int o = threadIdx.x; o < P * P; o += NTS) as[o] = t2[o];
   __syncthreads();
-  // polish: a = U S, V_p; to the orthogonality FP32 panels can use (P 1e-10)
-  const bool ok = jacobi_svd<dfloat, NTS>(P, as, v, sig, perm, flag, polish_sweeps, true, 1e-5, tiny_abs);
+  // polish: a = U S, V_p, until the rotations are below 1e-4 (left vectors
+  // orthogonal to ~P 1e-8, singular values to ~1e-8 relative: the FP32
+  // panels' level; the factors' Newton-Schulz refresh absorbs the rest)
+  const bool ok = jacobi_svd<dfloat, NTS>(P, as, v, sig, perm, flag, polish_sweeps, true, 1e-4, tiny_abs);
   sq_mul<dfloat>(P, t1, false, v, t2, tile);                                         // V = X V_p
   for (int o = threadIdx.x; o < P * P; o += NTS) v[o] = t2[o];
   __syncthreads();
@@ -750,7 +758,7 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
     // continue the sweeps without the truncation-level skip (v <- v v2)
     ST* v2 = reinterpret_cast<ST*>(mx) + (size_t)wa * wa;
     ST* t2 = reinterpret_cast<ST*>(mx) + (size_t)2 * wa * wa;
-    const double conv = std::is_same<ST, double>::value ? -1.0 : 1e-5;
+    const double conv = std::is_same<ST, double>::value ? -1.0 : 1e-4;
     ok = jacobi_svd<ST, NTS>(wa, a, v2, sig, perm, &flag, 40, true, conv, 0.0);
     sq_mul<ST>(wa, v, false, v2, t2, tile);
     for (int o = tid; o < wa * wa; o += NTS) v[o] = t2[o];
@@ -1561,16 +1569,25 @@ struct StreamOps {
   // rank-revealing pivoted Cholesky pass (dependent directions become zero
   // columns), one more projection (the pivoted pass combines nearly
   // dependent columns with large coefficients, which magnifies what is left
-  // of their Y0 components), then a plain CholeskyQR pass for orthogonality
-  // to the panel's precision.
+  // of their Y0 components), then X^T X = I + E with |E| ~ 1e-3: for FP32
+  // panels two Newton-Schulz steps X <- X (3I - X^T X) / 2 (E -> ~E^2, below
+  // FP32 rounding after two; whole-GPU Grams and products only), for FP64
+  // panels one CholeskyQR pass.  Zero columns stay zero either way.
   cudaError_t orth_against(int N, T* X, const T* Y0) const {
     const int R = (int)s->R;
     cudaError_t e = project_out(N, X, Y0);
     if (e == cudaSuccess) e = project_out(N, X, Y0);
-    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+    const int npass = std::is_same<T, float>::value ? 3 : 2;
+    for (int pass = 0; pass < npass && e == cudaSuccess; ++pass) {
       if (pass == 1) e = project_out(N, X, Y0);
       if (e == cudaSuccess) e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);         // G = X^T X
-      if (e == cudaSuccess) e = (pass == 0) ? pchol(R, blk(1), blk(2)) : cholinv(R, blk(1), blk(2), 0.0);
+      if (e == cudaSuccess) {
+        if (pass == 0) e = pchol(R, blk(1), blk(2));
+        else if (std::is_same<T, float>::value) {
+          ns_factor<<<(R * R + 255) / 256, 256, 0, st>>>(R, blk(1), blk(2));
+          e = cudaGetLastError();
+        } else e = cholinv(R, blk(1), blk(2), 0.0);
+      }
       if (e == cudaSuccess)
         e = (pass == 0) ? mul_precise(N, R, R, X, N, blk(2), R, tp(s->Zp), N)            // Z = X B
                         : mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);
