@@ -1287,7 +1287,7 @@ __global__ void __launch_bounds__(256) panel_mul_act(int N, int R, int aug, cons
 // w x w block (aug panels N x 2R; part ld 2R), one CTA per 32 x 32 tile of
 // active entries and split of GA_ROWS rows: sums of 32-row chunks in T,
 // added up in FP64 (an RK stage derivative: FP32 chunk sums are well inside
-// the FP32 step's accuracy).  gram_act_reduce adds the splits to C.
+// the FP32 step's accuracy).  s_stage_finish adds the splits in a fixed order.
 constexpr int GA_ROWS = 128;
 template <typename T>
 __global__ void __launch_bounds__(256) gram_act(int N, int R, const int32_t* __restrict__ rank,
@@ -1340,23 +1340,6 @@ __global__ void s_stage_finish(int R, const int32_t* __restrict__ rank, int nz, 
     for (int z = 0; z < nz; ++z) v += part[z * (int64_t)w * w + idx];
     rk_apply(rk, idx, v);
   }
-}
-
-// out (len) = sum_{c < cs} part[c * len + .]
-template <typename T>
-__global__ void sum_parts(int64_t len, int cs, const T* __restrict__ part, T* __restrict__ out) {
-  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x) {
-    T s = part[o];
-    for (int c = 1; c < cs; ++c) s += part[(int64_t)c * len + o];
-    out[o] = s;
-  }
-}
-
-// y = a x + b z (z may be null), element-wise over len
-template <typename T>
-__global__ void axpbz(int64_t len, T a, const T* __restrict__ x, T b, const T* __restrict__ z, T* __restrict__ y) {
-  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < len; o += (int64_t)gridDim.x * blockDim.x)
-    y[o] = z ? fma(b, z[o], a * x[o]) : a * x[o];
 }
 
 // small FP64 helpers of the S step: X (R x R, T, ld R) -> Y (FP64, ld R), optionally transposed
