@@ -38,27 +38,52 @@ namespace {
 constexpr int SMAX = 96;      // largest r_max
 constexpr int GROWS = 128;    // rows per Gram partial block (a few hundred CTAs for the panels here)
 
+// active column j (0 <= j < ka) -> panel column: the first r of each half
+__device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
+
 // ---------------------------------------------------------------------------
-// Streaming pass A: out (n x c) = dY B,  dY = A1 - A0 (n x m, col-major),
-// B (m x c, ld ldb), c <= 2*SMAX.  CTA = 32 rows, loops over all columns.
+// Streaming pass A: out (n x cols) = dY B, dY = A1 - A0 (n x m, col-major),
+// B (m x cols, ld ldb) with cols = R (aug = 0) or 2R (aug = 1), on the active
+// columns only (the first r of each half; r read on the device): the
+// multiply-adds run for ceil(ka / 32) groups of 32 columns, inactive output
+// columns are written as zeros.  CTA = 32 rows, loops over all columns of dY.
 // ---------------------------------------------------------------------------
+template <typename T, int CGN>
+__device__ __forceinline__ void pass_rows_tile(const T (*ds)[33], const T (*bs)[2 * SMAX + 1], int BJ, int rg,
+                                               int cg, T (&acc)[4][6]) {
+#pragma unroll 4
+  for (int jj = 0; jj < BJ; ++jj) {
+    T x[4], w[CGN];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) x[p] = ds[jj][4 * rg + p];
+#pragma unroll
+    for (int u = 0; u < CGN; ++u) w[u] = bs[jj][cg + 32 * u];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int u = 0; u < CGN; ++u) acc[p][u] = fma(x[p], w[u], acc[p][u]);
+  }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) pass_rows(int n, int m, int c, const T* __restrict__ A1,
-                                                 const T* __restrict__ A0, const T* __restrict__ B, int ldb,
-                                                 T* __restrict__ out) {
-  // 4 rows x CG columns per thread (c <= 192); BJ keeps the static shared
-  // memory under 48 KB for both types
-  constexpr int BI = 32, BJ = sizeof(T) == 8 ? 16 : 32, CG = 6;
+__global__ void __launch_bounds__(256) pass_rows(int n, int m, int R, int aug, const int32_t* __restrict__ rank,
+                                                 const T* __restrict__ A1, const T* __restrict__ A0,
+                                                 const T* __restrict__ B, int ldb, T* __restrict__ out) {
+  // 4 rows x up to 6 column groups per thread (ka <= 192); BJ keeps the
+  // static shared memory under 48 KB for both types
+  constexpr int BI = 32, BJ = sizeof(T) == 8 ? 16 : 32;
   __shared__ T ds[BJ][BI + 1];             // dY tile, column-major
-  __shared__ T bs[BJ][2 * SMAX + 1];       // B rows of the tile
+  __shared__ T bs[BJ][2 * SMAX + 1];       // B rows of the tile (active columns)
+  const int r = min(R, (int)*rank), ka = aug ? 2 * r : r, cols = aug ? 2 * R : R;
+  const int ncg = (ka + 31) / 32;
   const int tid = threadIdx.x;
   const int i0 = blockIdx.x * BI;
   const int rg = tid & 7, cg = tid >> 3;   // rows 4rg.., columns cg + 32u
-  T acc[4][CG];
+  T acc[4][6];
 #pragma unroll
   for (int p = 0; p < 4; ++p)
 #pragma unroll
-    for (int u = 0; u < CG; ++u) acc[p][u] = T(0);
+    for (int u = 0; u < 6; ++u) acc[p][u] = T(0);
   for (int j0 = 0; j0 < m; j0 += BJ) {
     for (int e = tid; e < BI * BJ; e += 256) {
       const int ii = e % BI, jj = e / BI;
@@ -70,23 +95,19 @@ __global__ void __launch_bounds__(256) pass_rows(int n, int m, int c, const T* _
       }
       ds[jj][ii] = v;
     }
-    for (int e = tid; e < BJ * c; e += 256) {
+    for (int e = tid; e < BJ * 32 * ncg; e += 256) {
       const int jj = e % BJ, k = e / BJ;
       const int j = j0 + jj;
-      bs[jj][k] = (j < m) ? B[j + (int64_t)k * ldb] : T(0);
+      bs[jj][k] = (j < m && k < ka) ? B[j + (int64_t)act_col(k, r, R) * ldb] : T(0);
     }
     __syncthreads();
-#pragma unroll 4
-    for (int jj = 0; jj < BJ; ++jj) {
-      T x[4], w[CG];
-#pragma unroll
-      for (int p = 0; p < 4; ++p) x[p] = ds[jj][4 * rg + p];
-#pragma unroll
-      for (int u = 0; u < CG; ++u) w[u] = (cg + 32 * u < c) ? bs[jj][cg + 32 * u] : T(0);
-#pragma unroll
-      for (int p = 0; p < 4; ++p)
-#pragma unroll
-        for (int u = 0; u < CG; ++u) acc[p][u] = fma(x[p], w[u], acc[p][u]);
+    switch (ncg) {
+      case 1: pass_rows_tile<T, 1>(ds, bs, BJ, rg, cg, acc); break;
+      case 2: pass_rows_tile<T, 2>(ds, bs, BJ, rg, cg, acc); break;
+      case 3: pass_rows_tile<T, 3>(ds, bs, BJ, rg, cg, acc); break;
+      case 4: pass_rows_tile<T, 4>(ds, bs, BJ, rg, cg, acc); break;
+      case 5: pass_rows_tile<T, 5>(ds, bs, BJ, rg, cg, acc); break;
+      default: pass_rows_tile<T, 6>(ds, bs, BJ, rg, cg, acc); break;
     }
     __syncthreads();
   }
@@ -95,24 +116,49 @@ __global__ void __launch_bounds__(256) pass_rows(int n, int m, int c, const T* _
     const int i = i0 + 4 * rg + p;
     if (i >= n) continue;
 #pragma unroll
-    for (int u = 0; u < CG; ++u) {
+    for (int u = 0; u < 6; ++u) {
       const int k = cg + 32 * u;
-      if (k < c) out[i + (int64_t)k * n] = acc[p][u];
+      if (k < ka) out[i + (int64_t)act_col(k, r, R) * n] = acc[p][u];
     }
+  }
+  // inactive columns of this CTA's rows
+  for (int e = tid; e < BI * cols; e += 256) {
+    const int ii = e % BI, col = e / BI;
+    const int i = i0 + ii;
+    if (i < n && (col % R) >= r) out[i + (int64_t)col * n] = T(0);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Streaming pass B: out (m x c) = dY^T X, X (n x c, ld ldx), c <= SMAX.
-// CTA = 16 columns of dY, loops over all rows.
+// Streaming pass B: out (m x R) = dY^T X, X (n x R, ld ldx), on the first r
+// columns (r read on the device; the others are written as zeros), r <=
+// SMAX.  CTA = 16 columns of dY, loops over all rows.
 // ---------------------------------------------------------------------------
+template <typename T, int NW>
+__device__ __forceinline__ void pass_cols_tile(const T (*ds)[65], const T (*xs)[129], int BI, int jg, int cg,
+                                               T (&acc)[4][2]) {
+#pragma unroll 4
+  for (int ii = 0; ii < BI; ++ii) {
+    T x[4], w[NW];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) x[p] = ds[4 * jg + p][ii];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) w[u] = xs[ii][cg + 64 * u];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int u = 0; u < NW; ++u) acc[p][u] = fma(x[p], w[u], acc[p][u]);
+  }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) pass_cols(int n, int m, int c, const T* __restrict__ A1,
-                                                 const T* __restrict__ A0, const T* __restrict__ X, int ldx,
-                                                 T* __restrict__ out) {
+__global__ void __launch_bounds__(256) pass_cols(int n, int m, int R, const int32_t* __restrict__ rank,
+                                                 const T* __restrict__ A1, const T* __restrict__ A0,
+                                                 const T* __restrict__ X, int ldx, T* __restrict__ out) {
   constexpr int BJ = 16, BI = sizeof(T) == 8 ? 32 : 64;
-  __shared__ T ds[BJ][BI + 1];
-  __shared__ T xs[BI][SMAX + 1];
+  __shared__ T ds[BJ][64 + 1];
+  __shared__ T xs[BI][129];  // columns cg + 64u < 128 of X (zero beyond r)
+  const int c = min(R, (int)*rank);
   const int tid = threadIdx.x;
   const int j0 = blockIdx.x * BJ;
   const int jg = tid & 3, cg = tid >> 2;   // columns 4jg.., outputs cg + 64u
@@ -130,33 +176,22 @@ __global__ void __launch_bounds__(256) pass_cols(int n, int m, int c, const T* _
       }
       ds[jj][ii] = v;
     }
-    for (int e = tid; e < BI * c; e += 256) {
+    for (int e = tid; e < BI * 128; e += 256) {
       const int ii = e % BI, k = e / BI;
       const int i = i0 + ii;
-      xs[ii][k] = (i < n) ? X[i + (int64_t)k * ldx] : T(0);
+      xs[ii][k] = (i < n && k < c) ? X[i + (int64_t)k * ldx] : T(0);
     }
     __syncthreads();
-#pragma unroll 4
-    for (int ii = 0; ii < BI; ++ii) {
-      T x[4], w[2];
-#pragma unroll
-      for (int p = 0; p < 4; ++p) x[p] = ds[4 * jg + p][ii];
-      w[0] = (cg < c) ? xs[ii][cg] : T(0);
-      w[1] = (cg + 64 < c) ? xs[ii][cg + 64] : T(0);
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        acc[p][0] = fma(x[p], w[0], acc[p][0]);
-        acc[p][1] = fma(x[p], w[1], acc[p][1]);
-      }
-    }
+    if (c <= 64) pass_cols_tile<T, 1>(ds, xs, BI, jg, cg, acc);
+    else pass_cols_tile<T, 2>(ds, xs, BI, jg, cg, acc);
     __syncthreads();
   }
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
     const int j = j0 + 4 * jg + p;
     if (j >= m) continue;
-    if (cg < c) out[j + (int64_t)cg * m] = acc[p][0];
-    if (cg + 64 < c) out[j + (int64_t)(cg + 64) * m] = acc[p][1];
+    if (cg < R) out[j + (int64_t)cg * m] = (cg < c) ? acc[p][0] : T(0);
+    if (cg + 64 < R) out[j + (int64_t)(cg + 64) * m] = (cg + 64 < c) ? acc[p][1] : T(0);
   }
 }
 
@@ -394,8 +429,6 @@ __device__ __forceinline__ double to_d(dfloat x) { return (double)x; }
 constexpr int NTS = 1024;  // threads of the single-CTA kernels
 constexpr size_t CORE_MAT = 160 * 1024;  // core_step's shared-memory matrix area (+ 40 KB of tiles)
 
-// active column j (0 <= j < ka) -> panel column: the first r of each half
-__device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
 
 // One CholeskyQR factor: G + shift_rel * trace(G) I = R^T R (a x a, ld a),
 // Bout = R^{-1}; columns with G_jj <= tol_rel * max G_jj are decoupled
@@ -1844,8 +1877,8 @@ struct StreamOps {
     cudaError_t e = refresh();
     if (e != cudaSuccess) return e;
     // data passes 1 and 2: dY V0, dY^T U0
-    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, A1, A0, V, m, Xk);
-    pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, A1, A0, U, n, Xl);
+    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_rank, A1, A0, V, m, Xk);
+    pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_rank, A1, A0, U, n, Xl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // Uhat = [U0 | orth((I - U0 U0^T) dY V0)], Vhat likewise
     if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
@@ -1858,7 +1891,7 @@ struct StreamOps {
     if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
     if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
     // data pass 3: Z = dY Vhat; D = Uhat^T Z
-    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, w, A1, A0, Vh, m, tp(s->Zp));
+    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 1, s->d_rank, A1, A0, Vh, m, tp(s->Zp));
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
     if ((e = core(w)) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
