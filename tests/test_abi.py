@@ -97,6 +97,23 @@ def test_create_rejects_bad_scheme_and_unsupported(lri):
     assert lib.lri_stream_create(C.byref(hs), native.LRI_DF, 8192, 4096, 16, 96, 1e-6, 1) == 2
     assert lib.lri_stream_create(C.byref(hs), native.LRI_F32, 100, 4096, 16, 64, 1e-6, 1) == 1
     assert lib.lri_stream_step(None, None, None, None) == 1
+    # the large Burgers engine: r_max above 64, bad grid spacing, non-finite
+    # coefficients, bad schemes, null handles (all rejected before any device work)
+    sch = lri.RK4(64).to_c()
+    bad = lri.RK4(1).to_c()
+    bad.nstages = 5
+    assert lib.lri_burgers_create(C.byref(hs), native.LRI_F32, 4096, 16384, 16, 65, 1e-4, 16,
+                                  1.0 / 4096, 0.0, -0.5, C.byref(sch)) == 1
+    assert lib.lri_burgers_create(C.byref(hs), native.LRI_F32, 4096, 16384, 16, 64, 1e-4, 16,
+                                  0.0, 0.0, -0.5, C.byref(sch)) == 1
+    assert lib.lri_burgers_create(C.byref(hs), native.LRI_F32, 4096, 16384, 16, 64, 1e-4, 16,
+                                  1.0 / 4096, float("nan"), -0.5, C.byref(sch)) == 1
+    assert lib.lri_burgers_create(C.byref(hs), native.LRI_F32, 4096, 16384, 16, 64, 1e-4, 16,
+                                  1.0 / 4096, 0.0, -0.5, C.byref(bad)) == 1
+    assert lib.lri_burgers_create(C.byref(hs), native.LRI_F32, 4096, 16384, 16, 64, 1e-4, 16,
+                                  1.0 / 4096, 0.0, -0.5, None) == 1
+    assert lib.lri_burgers_bind(None, None, None, None, None) == 1
+    assert lib.lri_burgers_step(None, 1e-4, 1, None) == 1
     assert lib.lri_batch_destroy(None) == 1
 
 
