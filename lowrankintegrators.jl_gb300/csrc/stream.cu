@@ -1,8 +1,9 @@
-// stream.cu - rank-adaptive BUG for one large data stream (MatrixDataProblem
-// whose snapshots are too large for the one-CTA instance engine), spread
-// over the whole GPU.
+// stream.cu - rank-adaptive BUG for one large instance spread over the whole
+// GPU: a data stream (MatrixDataProblem whose snapshots are too large for the
+// one-CTA instance engine, lri_stream_*) or a periodic Burgers flow
+// (MatrixDEProblem, lri_burgers_*).
 //
-// One step A(t) -> A(t+1) (src/integrators/rank_adaptive_unconventional.jl:
+// One data step A(t) -> A(t+1) (src/integrators/rank_adaptive_unconventional.jl:
 // 182-233 with the data substeps of data_integrator.jl:13-16):
 //   K1 = U0 S0 + dY V0,  L1 = V0 S0^T + dY^T U0          dY = A(t+1) - A(t)
 //   Uhat = orth[K1 | U0], Vhat = orth[L1 | V0]
@@ -10,17 +11,21 @@
 //   S~ = P Sigma Q^T, r1 = truncation, U1 = Uhat P1, V1 = Vhat Q1, S1 = Sigma1.
 // span[K1 | U0] = span[U0 | (I - U0 U0^T) dY V0], so Uhat is formed as
 // [U0 | Q] with Q an orthonormal basis of the part of dY V0 orthogonal to U0
-// (two classical Gram-Schmidt passes, then two eigenvalue-based
-// orthonormalisations X <- X D W Lambda^{-1/2}; directions with eigenvalues
-// below the rounding level become zero columns).  The step's result depends
-// only on span(Uhat), span(Vhat) as long as [K1 | U0] has full column rank.
+// (orth_against: projections, a rank-revealing pivoted Cholesky pass whose
+// dependent directions become zero columns, one more projection, then
+// Newton-Schulz or CholeskyQR).  The step's result depends only on
+// span(Uhat), span(Vhat).  The Burgers step has the same bases and core with
+// RK substeps whose flows use the exact low-rank structure of F (no n x m
+// matrix; see the flow kernels below).
 //
-// Kernels: three streaming passes over the snapshot pair (dY V0, dY^T U0,
-// dY Vhat; dY is formed in the loader and never stored), tall-skinny Gram
-// products X^T Y reduced in FP64 through per-block partials, row-parallel
-// panel products X B, and single-CTA FP64 kernels for the r x r / 2r x 2r
-// work.  Panel widths are fixed at r_max (Uhat, Vhat: 2 r_max) with zero
-// columns beyond the current rank, which stays on the device.
+// Kernels: streaming passes over the snapshot pair (dY V0, dY^T U0, dY Vhat;
+// dY is formed in the loader and never stored), tall-skinny Gram products
+// X^T Y reduced in FP64 through per-block partials, row-parallel panel
+// products X B, the Burgers flow kernels, and single-CTA kernels (double-float
+// for FP32 panels) for the r x r / 2r x 2r factorisations and the core SVD.
+// Panel widths are fixed at r_max (Uhat, Vhat: 2 r_max) with zero columns
+// beyond the current rank, which stays on the device; kernels that read it
+// work on the active columns only.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -337,7 +342,7 @@ __global__ void __launch_bounds__(256) panel_mul(int N, int a, int c, const T* _
 // out = X B for FP32 panels with double-float sums: B = Bh + Bl split into
 // floats, X Bh accumulated from exact products (TwoProduct), X Bl added to
 // the low part.  For orthonormalisation factors B whose entries are far
-// larger than the entries of X B (1 / sqrt of small eigenvalues of a nearly
+// larger than the entries of X B (the inverse Cholesky factor of a nearly
 // dependent panel): FP32 sums would lose u32 * |X| |B| to cancellation.
 __global__ void __launch_bounds__(256) panel_mul_df(int N, int a, int c, const float* __restrict__ X, int ldx,
                                                     const double* __restrict__ B, int ldb, float* __restrict__ out,
