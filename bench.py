@@ -18,6 +18,7 @@ import multiprocessing as mp
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -69,7 +70,7 @@ class ClockSampler:
     def __init__(self, device_index=0):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"lri_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

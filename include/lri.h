@@ -211,7 +211,7 @@ LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int
                                         const lri_scheme* scheme, void* stream, int32_t* status_out);
 
 /* Discrete adjoint of one BUG step (no counterpart in the reference, which
- * has no differentiation; the north-star's hand-written adjoint).  For an
+ * has no differentiation; gradients of a loss of Y(T) by a reverse sweep).  For an
  * LRI_F64, LRI_ALG_BUG, LRI_OP_SYLVESTER_TRIDIAG batch at fixed rank
  * (r = r_cap) whose operator A carries a diagonal shift theta
  * (F = (A0 + diag theta) X + X B^T, A as bound):
