@@ -308,7 +308,7 @@ def run_stream(args):
     print(json.dumps(line), flush=True)
 
 
-FP32_FFMA_TFLOPS = 74.6  # FP32 FMA-loop probe on this machine's GB300 (152 SMs at 2070 MHz)
+FP32_FFMA_TFLOPS = 74.6  # FP32 FMA-loop probe on a GB300 (152 SMs at 2070 MHz)
 
 
 def run_burgers(args):

@@ -1,4 +1,4 @@
-"""FP64 CPU discrete adjoint of the BUG step (the checker for the GPU adjoint).
+"""FP64 CPU discrete adjoint of the BUG step (the oracle for the GPU adjoint).
 
 TEST INFRASTRUCTURE ONLY, like ``lri_oracle``: only ``tests/`` and the
 benchmark's CPU leg may import it; the product never calls it.

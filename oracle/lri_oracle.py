@@ -1,6 +1,6 @@
 """FP64 CPU oracle: a NumPy restatement of LowRankIntegrators.jl's per-step hot path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker.  Only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This module checks the engine; only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it;
 the product (the CUDA library and its host wrapper) never calls it.
 
