@@ -1,4 +1,4 @@
-"""The CPU discrete adjoint of the BUG step (the GPU adjoint's checker):
+"""The CPU discrete adjoint of the BUG step (the oracle of the GPU adjoint):
 its forward step reproduces the oracle's bug_step, and its gradient matches
 FP64 central finite differences on random directions."""
 import numpy as np
