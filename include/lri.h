@@ -204,8 +204,15 @@ LRI_API lri_status lri_batch_status(lri_batch* b, void* stream);
  * before any stream capture.  All calls share the one array and leave their
  * contents in it (the call clears what must start at zero), so calls whose
  * work overlaps on the GPU (other streams, other host threads) race.
+ * The one scheme drives the K, L and S substeps, and the time of step k of
+ * a call is k * dt (each call starts at t = 0; the Sylvester flow is
+ * autonomous, so only the step count matters).  LRI_F32 is accurate to the
+ * FP32 level only while kappa(S0) <= 2^21; for worse-conditioned cores use
+ * LRI_F64 (the batch API's mixed form switches to double-float there).
  * status_out (host pointer, optional): when given, the call waits for its
- * steps and stores LRI_OK or LRI_ERR_NONFINITE there. */
+ * steps and stores the device status mapped as lri_batch_status does
+ * (LRI_OK, LRI_ERR_NONFINITE, LRI_ERR_BREAKDOWN, LRI_ERR_RANK_OVERFLOW, or
+ * LRI_ERR_ARG for a shape the kernel rejected); nsteps == 0 stores LRI_OK. */
 LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int64_t r, void* U, void* S, void* V,
                                         const void* A, const void* B, double dt, int32_t nsteps,
                                         const lri_scheme* scheme, void* stream, int32_t* status_out);
@@ -223,9 +230,11 @@ LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int
  *                   accumulates d loss / d theta
  * Each instance recomputes its step in stage form (RK stage inputs, both
  * QRs, basis changes, projections, S stages) and sweeps back through it;
- * the thin-QR adjoint is (Q_bar + Q copyltu(-Q_bar^T Q)) R^{-T}.  Workspace
- * is allocated on the first call.  Schemes with nstages * nsub > 16 and
- * other batch kinds return LRI_ERR_UNSUPPORTED. */
+ * the thin-QR adjoint is (Q_bar + Q copyltu(-Q_bar^T Q)) R^{-T}.  The
+ * workspace comes from lri_batch_adjoint_prepare (LRI_ERR_STATE without it);
+ * the step allocates nothing.  Schemes with nstages * nsub > 16 and other
+ * batch kinds return LRI_ERR_UNSUPPORTED. */
+LRI_API lri_status lri_batch_adjoint_prepare(lri_batch* b);
 LRI_API lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const void* S0, const void* V0,
                                           void* Ubar, void* Sbar, void* Vbar, void* theta_bar, void* stream);
 

@@ -808,6 +808,7 @@ def bug_gradient(prob: MatrixDEProblem, alg: UnconventionalAlgorithm, dt: float,
             b.step(t0 + done * dt, dt, seg)
             done += seg
         b.check_status()
+        _native.check(b.lib.lri_batch_adjoint_prepare(b.handle), "lri_batch_adjoint_prepare")
         loss, Ub, Sb, Vb = terminal_loss(b.download()[0], target)
         dev = b.device
         col = lambda X: torch.from_numpy(np.asarray(X, dtype=np.float64).ravel(order="F")).to(dev)

@@ -29,7 +29,7 @@ EXPORTED = [
     "lri_abi_version", "lri_status_str", "lri_device_info", "lri_batch_create", "lri_batch_destroy",
     "lri_batch_layout", "lri_batch_bind", "lri_batch_data_layout", "lri_batch_data_init", "lri_batch_step",
     "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step", "lri_bug_step_noalloc",
-    "lri_batch_prepare", "lri_batch_adjoint_step",
+    "lri_batch_prepare", "lri_batch_adjoint_prepare", "lri_batch_adjoint_step",
     "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
     "lri_stream_status", "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
 ]
@@ -110,6 +110,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_burgers_bind.argtypes = [P, P, P, P, P]
     lib.lri_burgers_step.restype = C.c_int
     lib.lri_burgers_step.argtypes = [P, C.c_double, C.c_int32, P]
+    lib.lri_batch_adjoint_prepare.restype = C.c_int
+    lib.lri_batch_adjoint_prepare.argtypes = [P]
     lib.lri_batch_adjoint_step.restype = C.c_int
     lib.lri_batch_adjoint_step.argtypes = [P, C.c_double, P, P, P, P, P, P, P, P]
     lib.lri_batch_prepare.restype = C.c_int

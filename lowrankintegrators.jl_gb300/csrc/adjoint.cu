@@ -463,12 +463,9 @@ cudaError_t launch_adjoint_step(const InstDesc* inst, const int64_t* adj_off, co
                                 const Scheme& sK, const Scheme& sL, const Scheme& sS, double dt, cudaStream_t st) {
   AdjArgs g{inst, adj_off, th_off, U0, S0, V0, Ub, Sb, Vb, thb, opA, opB, work, sK, sL, sS, dt};
   const size_t smem = sizeof(Smem<double>);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t e = set_smem_limit(adjoint_step_kernel, (int)smem, attr_done);
+  if (e != cudaSuccess) return e;
   adjoint_step_kernel<<<count, NT, smem, st>>>(g);
   return cudaGetLastError();
 }

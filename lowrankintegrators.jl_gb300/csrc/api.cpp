@@ -53,11 +53,10 @@ struct lri_batch {
   const void* opB = nullptr;
   bool bound = false;
   bool data_ready = false;
-  // discrete adjoint (allocated on the first lri_batch_adjoint_step)
+  // discrete adjoint (allocated by lri_batch_adjoint_prepare)
   double* d_adj_work = nullptr;
   int64_t* d_adj_off = nullptr;
   int64_t* d_th_off = nullptr;
-  int adj_ns_k = 0, adj_ns_l = 0;
   // graph cache
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -501,41 +500,61 @@ int32_t lri_batch_launches_per_step(const lri_batch* b) {
 
 }  // extern "C"
 
-lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const void* S0, const void* V0, void* Ubar,
-                                  void* Sbar, void* Vbar, void* theta_bar, void* stream) {
-  if (!b || !U0 || !S0 || !V0 || !Ubar || !Sbar || !Vbar || !theta_bar || !std::isfinite(dt)) return LRI_ERR_ARG;
-  if (!b->bound) return LRI_ERR_STATE;
+// Checks that the batch is one the adjoint covers; returns the stage counts.
+static lri_status adjoint_supported(const lri_batch* b, int* nsK, int* nsL) {
   if (b->desc.dtype != LRI_F64 || b->alg.kind != LRI_ALG_BUG || b->desc.op != LRI_OP_SYLVESTER_TRIDIAG)
     return LRI_ERR_UNSUPPORTED;
-  const int count = b->desc.count;
-  for (int i = 0; i < count; ++i)
+  for (int i = 0; i < b->desc.count; ++i)
     if (b->r[i] != b->rcap[i]) return LRI_ERR_UNSUPPORTED;  // fixed-rank BUG only
-  const int nsK = b->alg.K_alg.nstages * b->alg.K_alg.nsub, nsL = b->alg.L_alg.nstages * b->alg.L_alg.nsub;
+  *nsK = b->alg.K_alg.nstages * b->alg.K_alg.nsub;
+  *nsL = b->alg.L_alg.nstages * b->alg.L_alg.nsub;
   const int nsS = b->alg.S_alg.nstages * b->alg.S_alg.nsub;
   const int lim = lri::adjoint_max_stages();
-  if (nsK > lim || nsL > lim || nsS > lim) return LRI_ERR_UNSUPPORTED;
-  if (!b->d_adj_work || b->adj_ns_k != nsK || b->adj_ns_l != nsL) {
+  if (*nsK > lim || *nsL > lim || nsS > lim) return LRI_ERR_UNSUPPORTED;
+  return LRI_OK;
+}
+
+lri_status lri_batch_adjoint_prepare(lri_batch* b) {
+  if (!b) return LRI_ERR_ARG;
+  int nsK = 0, nsL = 0;
+  const lri_status ok = adjoint_supported(b, &nsK, &nsL);
+  if (ok != LRI_OK) return ok;
+  if (b->d_adj_work) return LRI_OK;  // the stage counts are fixed at create time
+  const int count = b->desc.count;
+  std::vector<int64_t> off(count), th(count);
+  int64_t tot = 0, toth = 0;
+  for (int i = 0; i < count; ++i) {
+    off[i] = tot;
+    tot += ((int64_t)lri::adjoint_work_elems(b->n[i], b->m[i], b->rcap[i], nsK, nsL) + 3) & ~int64_t(3);
+    th[i] = toth;
+    toth += b->n[i];
+  }
+  cudaError_t e = cudaMalloc((void**)&b->d_adj_work, sizeof(double) * (size_t)tot);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_adj_off, sizeof(int64_t) * count);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_th_off, sizeof(int64_t) * count);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_adj_off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_th_off, th.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
     cudaFree(b->d_adj_work);
     cudaFree(b->d_adj_off);
     cudaFree(b->d_th_off);
     b->d_adj_work = nullptr;
     b->d_adj_off = b->d_th_off = nullptr;
-    std::vector<int64_t> off(count), th(count);
-    int64_t tot = 0, toth = 0;
-    for (int i = 0; i < count; ++i) {
-      off[i] = tot;
-      tot += ((int64_t)lri::adjoint_work_elems(b->n[i], b->m[i], b->rcap[i], nsK, nsL) + 3) & ~int64_t(3);
-      th[i] = toth;
-      toth += b->n[i];
-    }
-    LRI_CUDA(cudaMalloc((void**)&b->d_adj_work, sizeof(double) * (size_t)tot));
-    LRI_CUDA(cudaMalloc((void**)&b->d_adj_off, sizeof(int64_t) * count));
-    LRI_CUDA(cudaMalloc((void**)&b->d_th_off, sizeof(int64_t) * count));
-    LRI_CUDA(cudaMemcpy(b->d_adj_off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice));
-    LRI_CUDA(cudaMemcpy(b->d_th_off, th.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice));
-    b->adj_ns_k = nsK;
-    b->adj_ns_l = nsL;
+    return LRI_ERR_CUDA;
   }
+  return LRI_OK;
+}
+
+lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const void* S0, const void* V0, void* Ubar,
+                                  void* Sbar, void* Vbar, void* theta_bar, void* stream) {
+  if (!b || !U0 || !S0 || !V0 || !Ubar || !Sbar || !Vbar || !theta_bar || !std::isfinite(dt)) return LRI_ERR_ARG;
+  if (!b->bound) return LRI_ERR_STATE;
+  int nsK = 0, nsL = 0;
+  const lri_status ok = adjoint_supported(b, &nsK, &nsL);
+  if (ok != LRI_OK) return ok;
+  if (!b->d_adj_work) return LRI_ERR_STATE;  // lri_batch_adjoint_prepare allocates the workspace
+  const int count = b->desc.count;
   return cuda_status(lri::launch_adjoint_step(
       b->d_inst, b->d_adj_off, b->d_th_off, count, static_cast<const double*>(U0), static_cast<const double*>(S0),
       static_cast<const double*>(V0), static_cast<double*>(Ubar), static_cast<double*>(Sbar),

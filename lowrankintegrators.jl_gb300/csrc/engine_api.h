@@ -5,6 +5,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace lri_df {
 struct dfloat;  // double-float value (dfloat.cuh); the host only passes pointers to it
 }  // namespace lri_df
@@ -67,6 +69,23 @@ struct StepArgs {
   Scheme sK, sL, sS;
   double bh, balpha, bbeta;
 };
+
+// Raises a kernel's dynamic shared-memory limit on the current device.  The
+// attribute is per device, so `done` keeps one bit per device ordinal (< 64;
+// higher ordinals set it on every call); several host threads may race to
+// set the same bit, which is harmless.  cudaFuncSetAttribute is not a stream
+// operation, so this is also safe while a stream is being captured.
+template <typename F>
+inline cudaError_t set_smem_limit(F* func, int bytes, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 template <typename T>
 cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream);

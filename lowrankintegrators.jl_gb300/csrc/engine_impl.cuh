@@ -831,12 +831,9 @@ size_t step_smem_bytes() {
 template <typename T>
 cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream) {
   const size_t smem = sizeof(Smem<T>);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(step_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  cudaError_t e = set_smem_limit(step_kernel<T>, (int)smem, attr_done);
+  if (e != cudaSuccess) return e;
   step_kernel<T><<<count, NT, smem, stream>>>(g);
   return cudaGetLastError();
 }

@@ -10,6 +10,7 @@
 // lri_batch_create.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 
@@ -35,8 +36,10 @@ struct NoallocHeader {
 constexpr size_t kHeaderBytes = 256;
 static_assert(sizeof(NoallocHeader) <= kHeaderBytes, "header must fit its slot");
 
+// Device address of the scratch array, per device ordinal.  Host threads may
+// look it up concurrently; they all store the same address.
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+std::atomic<void*> g_scratch_addr[kMaxDevices];
 
 __global__ void noalloc_init_kernel(NoallocHeader* h, lri::InstDesc d, int32_t r) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -120,18 +123,21 @@ extern "C" lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, 
   d.offY = 0;
   const int64_t elems = d.offSmall + lri::kSmallBlocks * al(r * r);
   if (kHeaderBytes + es * (size_t)elems > kScratchBytes) return LRI_ERR_ARG;  // beyond the fixed scratch
-  if (nsteps == 0) return LRI_OK;
+  if (nsteps == 0) {
+    if (status_out) *status_out = LRI_OK;
+    return LRI_OK;
+  }
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return LRI_ERR_CUDA;
-  if (!g_scratch_addr[dev]) {
+  void* addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
     // once per device, with that device current: the host-side symbol is a
     // stand-in, the kernels need the device address
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, lri_noalloc_scratch) != cudaSuccess || !p) return LRI_ERR_CUDA;
-    g_scratch_addr[dev] = p;
+    if (cudaGetSymbolAddress(&addr, lri_noalloc_scratch) != cudaSuccess || !addr) return LRI_ERR_CUDA;
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  unsigned char* base = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  unsigned char* base = static_cast<unsigned char*>(addr);
   cudaStream_t st = (cudaStream_t)stream;
   noalloc_init_kernel<<<1, 32, 0, st>>>(reinterpret_cast<NoallocHeader*>(base), d, (int32_t)r);
   if (cudaGetLastError() != cudaSuccess) return LRI_ERR_CUDA;
@@ -146,7 +152,12 @@ extern "C" lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, 
     if (cudaMemcpyAsync(&word, &h->status, sizeof(word), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return LRI_ERR_CUDA;
-    *status_out = (word & lri::ST_NONFINITE) ? LRI_ERR_NONFINITE : (word ? LRI_ERR_ARG : LRI_OK);
+    // same mapping as lri_batch_status
+    *status_out = (word & lri::ST_BAD_SHAPE)      ? LRI_ERR_ARG
+                  : (word & lri::ST_NONFINITE)    ? LRI_ERR_NONFINITE
+                  : (word & lri::ST_SVD_NOCONV)   ? LRI_ERR_BREAKDOWN
+                  : (word & lri::ST_RANK_OVERFLOW) ? LRI_ERR_RANK_OVERFLOW
+                                                  : LRI_OK;
   }
   return LRI_OK;
 }

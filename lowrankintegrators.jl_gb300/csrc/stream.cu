@@ -1551,13 +1551,9 @@ struct StreamOps {
   }
   using ST = typename SmallT<T>::type;
   cudaError_t pchol(int a, const double* G, double* B) const {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(pchol_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(2 * SMAX * SMAX * sizeof(ST)));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    cudaError_t e = set_smem_limit(pchol_factor<ST>, (int)(2 * SMAX * SMAX * sizeof(ST)), attr_done);
+    if (e != cudaSuccess) return e;
     // directions whose squared distance from the span of the others (unit
     // columns) is below tol_rel are treated as dependent.  The columns of
     // X B are orthonormal up to about (error of G) / tol_rel: about 1e-3 for
@@ -1569,14 +1565,10 @@ struct StreamOps {
     return cudaGetLastError();
   }
   cudaError_t cholinv(int a, const double* G, double* B, double shift_rel) const {
-    static bool attr_set = false;
+    static std::atomic<uint64_t> attr_done{0};
     const size_t smem = 2 * (size_t)a * a * sizeof(ST);
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(chol_inv_factor<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(2 * SMAX * SMAX * sizeof(ST)));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    cudaError_t e = set_smem_limit(chol_inv_factor<ST>, (int)(2 * SMAX * SMAX * sizeof(ST)), attr_done);
+    if (e != cudaSuccess) return e;
     chol_inv_factor<ST><<<1, NTS, smem, st>>>(a, G, 1e-20, shift_rel, B);
     return cudaGetLastError();
   }
@@ -1648,15 +1640,11 @@ struct StreamOps {
                     int accum = 0) const {
     const int R = (int)s->R, ka = aug ? 2 * R : R;
     constexpr int BM = KrTile<T>::BM;
-    static bool attr_set = false;
-    if (!attr_set) {
-      const int mx = (int)(2 * (2 * 64) * BM * sizeof(T));
-      cudaError_t e = cudaFuncSetAttribute(kr_apply_part<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(kr_apply_part<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_same{0}, attr_diff{0};
+    const int mx = (int)(2 * (2 * 64) * BM * sizeof(T));
+    cudaError_t ea = set_smem_limit(kr_apply_part<T, true>, mx, attr_same);
+    if (ea == cudaSuccess) ea = set_smem_limit(kr_apply_part<T, false>, mx, attr_diff);
+    if (ea != cudaSuccess) return ea;
     dim3 grid((N + BM - 1) / BM, (ka + 63) / 64, kz(N, aug));
     const size_t smem = (size_t)ka * BM * sizeof(T) * (X == Y ? 1 : 2);
     if (X == Y)
@@ -1703,13 +1691,9 @@ struct StreamOps {
     cudaError_t e = gram(n, R, R, U, n, U, n, 1.0, 0.0, Gu, R);
     if (e == cudaSuccess) e = gram(m, R, R, V, m, V, m, 1.0, 0.0, Gv, R);
     if (e != cudaSuccess) return e;
-    static bool attr_set = false;
-    if (!attr_set) {
-      e = cudaFuncSetAttribute(ns_refresh, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(3 * SMAX * SMAX * sizeof(float)));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    e = set_smem_limit(ns_refresh, (int)(3 * SMAX * SMAX * sizeof(float)), attr_done);
+    if (e != cudaSuccess) return e;
     ns_refresh<<<1, 1024, 3 * (size_t)R * R * sizeof(float), st>>>(R, s->d_rank, Gu, Gv, Xu, Xv,
                                                                   reinterpret_cast<float*>(s->S), blk(23));
     if ((e = mul(n, R, R, U, n, Xu, R, T(0), tp(s->Zp), n)) != cudaSuccess) return e;
@@ -1858,13 +1842,8 @@ struct StreamOps {
     T* S = tp(s->S);
     cudaError_t e;
     const int abytes = 200 * 1024;  // CORE_MAT + tiles
-    static bool attr_set = false;
-    if (!attr_set) {
-      if ((e = cudaFuncSetAttribute(core_step<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, abytes)) !=
-          cudaSuccess)
-        return e;
-      attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    if ((e = set_smem_limit(core_step<T, ST>, abytes, attr_done)) != cudaSuccess) return e;
     // S~ = Mh S0 Nh^T + D on the active block, over the whole GPU (T1 in block 14, S~ in block 13)
     form_t1<T><<<64, 256, 0, st>>>(R, s->d_rank, S, blk(4), blk(14));
     form_core<<<128, 256, 0, st>>>(R, s->d_rank, blk(3), blk(14), blk(5), blk(13));
