@@ -1,10 +1,20 @@
-"""Benchmark: batched BUG steps/sec on the 4096-instance Lyapunov ensemble.
+"""Benchmark: batched BUG steps/sec on the 4096-instance Lyapunov ensemble,
+followed (N = 1) by the other workloads in the same JSON line.
 
-Workload (one "step" = one BUG step of every instance, one kernel launch):
+Headline workload (one "step" = one BUG step of every instance, one kernel
+launch per precision class):
   4096 independent F_i(X) = A_i X + X B_i^T, n_i, m_i ~ U{64..1024},
   r_i ~ U{4..32}, tridiagonal A_i, B_i, X0_i with spectrum 2^-k (seed 4),
-  dt = 1e-2, RK4 substeps (nsub = 1), fast (FP32) form; the plain FP64 form
-  runs the same steps for the speed ratio and the accuracy check.
+  dt = 1e-2, RK4 substeps (nsub = 1), mixed form (FP32 for well-conditioned
+  cores, double-float for the others); the plain FP64 form runs the same
+  steps for the speed ratio and the accuracy check.
+
+``workloads`` (N = 1, unless --no-legs): the 256 x 256 Laplacian flow (FP64,
+1000 steps), the 8192 x 4096 data-compression stream (rank-adaptive, FP32),
+the 4096 x 16384 Burgers-UQ instance (rank 16..64) and the 2048 x 2048
+discrete-adjoint sweep with its finite-difference check, each with its own
+timing, clocks, accuracy and CPU sample.  --laplace / --stream / --burgers /
+--adjoint print one of them alone.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
 restatement of the reference integrator on the host cores instead.
@@ -127,25 +137,31 @@ def _pool_init():
 
 
 def _cpu_worker(args):
-    idx, steps = args
+    idx, steps, warmup = args
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     import workloads
     from oracle import lri_oracle as O
-    out = 0.0
+    integs = []
     for i in idx:
         e = workloads.lyapunov_ensemble(first=i, limit=1)[0]
         p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
-                              (0.0, DT * steps))
-        integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
-        t0 = time.perf_counter()
-        for _ in range(steps):
+                              (0.0, DT * (steps + warmup)))
+        integs.append(O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT))
+    for _ in range(warmup):
+        for integ in integs:
             O.step(integ, integ.alg, DT)
-        out += time.perf_counter() - t0
-    return out
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for integ in integs:
+            O.step(integ, integ.alg, DT)
+    return time.perf_counter() - t0
 
 
-def cpu_baseline(count, sample_every, steps, cores=None):
-    """Returns (batched steps/s extrapolated to `count` instances, cores, sample)."""
+def cpu_baseline(count, sample_every, steps, warmup=0, cores=None):
+    """The oracle on every `sample_every`-th instance of the ensemble, one
+    process per host core: `warmup` untimed steps, then `steps` timed steps
+    of every sampled instance.  Returns (batched steps/s extrapolated to
+    `count` instances, cores, description of the sample, timed steps)."""
     cores = cores or os.cpu_count() or 1
     sample = list(range(0, count, sample_every))
     chunks = [sample[k::cores] for k in range(cores)]
@@ -153,14 +169,15 @@ def cpu_baseline(count, sample_every, steps, cores=None):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(len(chunks), initializer=_pool_init) as pool:
-        busy = pool.map(_cpu_worker, [(c, steps) for c in chunks])
+        busy = pool.map(_cpu_worker, [(c, steps, warmup) for c in chunks])
     wall = time.perf_counter() - t0
     # instance-steps per second of the whole pool, scaled to the full ensemble
     inst_steps = len(sample) * steps
     per_inst_step = sum(busy) / inst_steps            # core-seconds per instance-step
     batched_per_s = len(chunks) / (per_inst_step * count)
-    desc = (f"{len(sample)} of {count} instances (every {sample_every}th) x {steps} steps, "
-            f"{len(chunks)} processes, {wall:.1f} s wall")
+    desc = (f"{len(sample)} of {count} instances (every {sample_every}th), {warmup} untimed + {steps} timed "
+            f"steps of each, {len(chunks)} processes, {wall:.1f} s wall; the ensemble's step time is the "
+            f"sample's core-seconds per instance-step x {count} / {len(chunks)} cores")
     return batched_per_s, len(chunks), desc
 
 
@@ -207,20 +224,26 @@ def weak_value(ws: int, steps: int, seconds: float) -> float:
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: the oracle (the NumPy FP64 restatement of the
+    reference integrator; Julia is not available) on the host cores, W
+    untimed and K timed steps of every 64th ensemble member, extrapolated to
+    the 4096-instance ensemble."""
     if rank != 0:
         return
-    val, cores, desc = cpu_baseline(args.count, args.cpu_sample_every, max(1, min(args.steps, 3)))
+    val, cores, desc = cpu_baseline(args.count, args.cpu_sample_every, args.steps, args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / val, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "lyapunov_ensemble_4096", "instances": args.count, "dt": DT,
-                       "scheme": f"RK4(nsub={NSUB})", "algorithm": "BUG"},
+                       "scheme": f"RK4(nsub={NSUB})", "algorithm": "BUG",
+                       "instances_timed": len(range(0, args.count, args.cpu_sample_every)),
+                       "steps_timed": args.steps},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_stream(args):
+def leg_stream(steps, warmup):
     """The data-compression workload on one GPU: n = 8192, m = 4096 FP32
     snapshots of the rotating-mode stream (500 on [0, 1], generated on the
     device), rank-adaptive BUG with tol 1e-6 and r <= 96 from the rank-64
@@ -233,7 +256,7 @@ def run_stream(args):
     from oracle import lri_oracle as O
     lri = ge.load_package()
     n, m, nsnap, R, tol = 8192, 4096, 500, 96, 1e-6
-    K, W = min(args.steps, nsnap - 1 - args.warmup), args.warmup
+    K, W = min(steps, nsnap - 1 - warmup), warmup
     snap = workloads.data_stream_device(n, m, nsnap)
     A = [snap(j) for j in range(W + K + 1)]
     torch.cuda.synchronize()
@@ -305,13 +328,13 @@ def run_stream(args):
                              "sample": "3 oracle steps at full size (NumPy FP64, threaded BLAS)"},
             "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": n * m * 4,
                     "d2h_bytes_per_step": 8}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 FP32_FFMA_TFLOPS = 74.6  # FP32 FMA-loop probe on a GB300 (152 SMs at 2070 MHz)
 
 
-def run_burgers(args):
+def leg_burgers(steps, warmup):
     """The Burgers-UQ workload on one GPU: u_t + (u^2/2)_x = nu u_xx,
     periodic, n = 4096 grid points, m = 16384 samples (nu_j ~ U[0.005, 0.02],
     u0_j = sin 2 pi x + a_j sin(4 pi x + phi_j)), rank-adaptive BUG with
@@ -330,7 +353,7 @@ def run_burgers(args):
     from oracle import lri_oracle as O
     lri = ge.load_package()
     n, m, r0, R, tol, dt, nsub = 4096, 16384, 16, 64, 1e-4, 1e-4, 64
-    K, W = args.steps, args.warmup
+    K, W = steps, warmup
     h, nu, U0, s0, V0 = workloads.burgers_uq_factors(n, m, r0)
     Y0 = lri.SVDLikeRepresentation(U0, np.diag(s0), V0)
     op = lri.BurgersOperator(h, nu, alpha=0.0, beta=-0.5)
@@ -430,15 +453,16 @@ def run_burgers(args):
             "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s",
                     "h2d_bytes_per_step": ((n + m) * r0 + r0 * r0 + m) * 4 // 3,
                     "d2h_bytes_per_step": ((n + m) * R + R * R) * 4 // 3}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def run_adjoint(args):
+def leg_adjoint():
     """The adjoint workload on one GPU: one loss + gradient sweep (forward
     with checkpoints every 20 steps, segment replays, 200 adjoint-step
-    launches), timed after a warm-up sweep, then the gradient against FP64
-    central differences on 32 random directions (64 perturbed forward solves
-    in one batch)."""
+    launches), timed after a warm-up sweep over the first 20 steps (same
+    kernels and graph shapes), then the gradient against FP64 central
+    differences on 32 random directions (64 perturbed forward solves in one
+    batch)."""
     import torch
     import __graft_entry__ as ge
     import workloads
@@ -449,12 +473,16 @@ def run_adjoint(args):
     target = lri.SVDLikeRepresentation(P, np.diag(d), Q)
     prob = lri.MatrixDEProblem(lri.SylvesterTridiagOperator(A0, A0, theta), lri.SVDLikeRepresentation(U, S, V),
                                (0.0, T))
-    lri.bug_gradient(prob, alg, dt, target, checkpoint_every=20)  # warm-up (builds, graph capture)
+    warm = lri.MatrixDEProblem(prob.f, prob.u0, (0.0, 20 * dt))
+    lri.bug_gradient(warm, alg, dt, target, checkpoint_every=20)  # warm-up (builds, graph capture)
     torch.cuda.synchronize()
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.__enter__()
     t0 = time.perf_counter()
     loss, thb, gr = lri.bug_gradient(prob, alg, dt, target, checkpoint_every=20)
     torch.cuda.synchronize()
     sweep = time.perf_counter() - t0
+    sampler.__exit__()
     t0 = time.perf_counter()
     lri.solve(prob, alg, dt, precision="fp64", save_everystep=False)
     torch.cuda.synchronize()
@@ -486,9 +514,133 @@ def run_adjoint(args):
             "gpu_launches": {"forward": nsteps, "replay": nsteps, "adjoint": nsteps},
             "fd_check": {"directions": len(dirs), "h": h, "worst_rel": float(max(rel)),
                          "median_rel": float(np.median(rel)), "batched_forward_solves_s": fd_time,
-                         "tolerance": 1e-4},
+                         "tolerance": 1e-4, "passed": bool(max(rel) <= 1e-4)},
+            "clocks": sampler.summary(),
             "loss": loss}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def leg_laplace(warmup):
+    """The stiff 256 x 256 workload: plain BUG in FP64 on F(X) = A X + X A^T,
+    A = Laplacian/h^2 - 0.1 I (h = 1/257), Y0 rank 8, dt = 1e-4, RK4 with 20
+    substeps, 1000 steps on [0, 0.1] as one CUDA graph on the device-resident
+    factors; accuracy of the first 100 steps against the oracle, whose time
+    for those steps is the CPU baseline; end to end through solve() from host
+    arrays with the final factors read back."""
+    import torch
+    import __graft_entry__ as ge
+    import workloads
+    from oracle import lri_oracle as O
+    lri = ge.load_package()
+    inst, dt, tspan, nsub = workloads.sylvester_256()
+    nsteps = lri.n_steps(tspan, dt)
+    alg = lri.UnconventionalAlgorithm(lri.RK4(nsub))
+    Y0 = lri.SVDLikeRepresentation(inst.U, inst.S, inst.V)
+    op = lri.SylvesterTridiagOperator(inst.A, inst.B)
+    OPK = lri._native.LRI_OP_SYLVESTER_TRIDIAG
+    stream = torch.cuda.current_stream()
+
+    def batch(prec):
+        b = lri.Batch([256], [256], [8], alg, OPK, prec)
+        b.upload([Y0], [op])
+        return b
+
+    res = {}
+    clocks = None
+    for prec in ("fp64", "df"):
+        b = batch(prec)
+        for k in range(warmup):
+            b.step(k * dt, dt, 1)
+        b.check_status()
+        b.upload([Y0], [op])
+        b.prepare(dt, nsteps)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(torch.cuda.current_device()) if prec == "fp64" else None
+        if sampler:
+            sampler.__enter__()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(0.0, dt, nsteps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+            clocks = sampler.summary()
+        b.check_status()
+        res[prec] = e0.elapsed_time(e1) / nsteps
+        b.close()
+    # accuracy over the first 100 steps, against the oracle and the oracle's
+    # own response to a 1e-16 relative perturbation of the core every step
+    k_acc = 100
+    b = batch("fp64")
+    b.step(0.0, dt, k_acc)
+    b.check_status()
+    yg = b.download()[0]
+    b.close()
+    Yo = O.SVDLikeRepresentation(inst.U, inst.S, inst.V)
+    mk = lambda: O.init(O.MatrixDEProblem(O.SylvesterTridiagOp(inst.A, inst.B), Yo, tspan),
+                        O.UnconventionalAlgorithm(O.RK4(nsub)), dt)
+    io, ip = mk(), mk()
+    g = np.random.default_rng(0)
+    t0 = time.perf_counter()
+    for _ in range(k_acc):
+        O.step(io, io.alg, dt)
+    cpu_s = (time.perf_counter() - t0) / k_acc
+    for _ in range(k_acc):
+        O.step(ip, ip.alg, dt)
+        ip.u.S = ip.u.S * (1 + 1e-16 * g.standard_normal(ip.u.S.shape))
+    err = O.rel_fro_err(yg.full(), io.u.full())
+    sens = O.rel_fro_err(ip.u.full(), io.u.full())
+    # e2e: the public solve() from host arrays (H2D of Y0 and operators, one
+    # graph of all steps, D2H of the final factors)
+    prob = lri.MatrixDEProblem(op, Y0, tspan)
+    lri.solve(prob, alg, dt, save_everystep=False)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lri.solve(prob, alg, dt, save_everystep=False)
+    e2e_s = time.perf_counter() - t0
+    ms = res["fp64"]
+    # per rhs evaluation 5nr (stencil) + 2nr^2 (K P^T); 3 substep flows x 4
+    # stages x nsub per step, plus QR and basis change ~14 (n + m) r^2
+    flops = 4 * nsub * 3 * (5 * 256 * 8 + 2 * 256 * 8 * 8) + 14 * 512 * 64
+    return {"metric": "BUG steps/s (256x256 Laplacian flow, r = 8, RK4 x 20 substeps, FP64)",
+            "value": 1e3 / ms, "unit": "steps/s", "n_gpus": 1, "steps": nsteps, "warmup": warmup,
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seed 1)",
+            "config": {"workload": "sylvester_256", "n": 256, "m": 256, "r": 8, "dt": dt, "scheme": "RK4(nsub=20)",
+                       "one_launch_per_step": True, "graph_steps": nsteps},
+            "double_float": {"ms_per_step": res["df"], "steps_per_s": 1e3 / res["df"]},
+            "accuracy": {"steps": k_acc, "rel_fro_vs_fp64_oracle": err, "oracle_self_sensitivity": sens,
+                         "bound": max(1e-11, 100.0 * sens),
+                         "passed": bool(err <= max(1e-11, 100.0 * sens))},
+            "roofline": {"bound": "latency", "note": "one instance of 66 KB state: a single CTA runs the whole "
+                                                     "step (one SM); flops per step %.3g, %.3f TFLOP/s"
+                                                     % (flops, flops / (ms * 1e-3) / 1e12)},
+            "gpu_launches": nsteps,
+            "clocks": clocks,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{k_acc} oracle steps (NumPy FP64)"},
+            "e2e": {"value": nsteps / e2e_s, "unit": "steps/s",
+                    "h2d_bytes_per_step": (2 * 256 * 8 + 64 + 6 * 256) * 8 / nsteps,
+                    "d2h_bytes_per_step": (2 * 256 * 8 + 64) * 8 / nsteps}}
+
+
+def run_leg(name, args):
+    """One of the other workloads; its own dict (or the error it raised)."""
+    import torch
+    try:
+        if name == "stream":
+            out = leg_stream(min(args.steps, 20), args.warmup)
+        elif name == "burgers":
+            out = leg_burgers(min(args.steps, 20), args.warmup)
+        elif name == "adjoint":
+            out = leg_adjoint()
+        else:
+            out = leg_laplace(args.warmup)
+    except Exception as exc:  # a failing leg must not hide the others
+        out = {"error": f"{type(exc).__name__}: {exc}"}
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -508,29 +660,28 @@ def main():
                     help="instead of the ensemble: the Burgers-UQ workload (n=4096, m=16384, rank 16..64)")
     ap.add_argument("--stream", action="store_true",
                     help="instead of the ensemble: the 8192 x 4096 data-compression stream (rank-adaptive)")
+    ap.add_argument("--laplace", action="store_true",
+                    help="instead of the ensemble: the 256 x 256 Laplacian flow (FP64, 1000 steps)")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="N = 1: skip the other workloads that follow the ensemble in the same JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
-    if args.adjoint:
+    legs = {"adjoint": args.adjoint, "stream": args.stream, "burgers": args.burgers, "laplace": args.laplace}
+    only = [k for k, v in legs.items() if v]
+    if only:
         if rank == 0:
-            run_adjoint(args)
-        return
-    if args.stream:
-        if rank == 0:
-            run_stream(args)
-        return
-    if args.burgers:
-        if rank == 0:
-            run_burgers(args)
+            for k in only:
+                print(json.dumps(run_leg(k, args)), flush=True)
         return
 
     # CPU baseline first: its spawn pool starts before any GPU work
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(args.count, args.cpu_sample_every, 2)
+        cpu = cpu_baseline(args.count, args.cpu_sample_every, 2, 1)
 
     import torch
     import __graft_entry__ as ge
@@ -720,6 +871,13 @@ def main():
     hbm, bf16, src = peaks()
     alg_bytes, alg_flops = algorithmic(shapes)
     t_launch = ms / K * 1e-3
+    # FP32 FMA peak: SMs x 128 lanes x 2 flops x the SM clock sampled during
+    # the timed region (nominal maximum when no sample was taken)
+    sms = torch.cuda.get_device_properties(dev_index).multi_processor_count
+    clk = (clocks or {}).get("sm_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * clk * 1e6 / 1e12
+    fp32_src = "%d SMs x 128 FP32 lanes x 2 x %.0f MHz (%s)" % (
+        sms, clk, "sampled SM clock" if (clocks or {}).get("sm_mhz") else "nominal maximum clock")
     achieved = alg_bytes / t_launch / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
@@ -750,8 +908,14 @@ def main():
                      "peak_source": src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "compulsory bytes per batched step (factors and operators read, factors "
-                             "written) / mixed step time; the kernels are CUDA-core bound: %.3g algorithmic "
-                             "flops per step, %.2f TFLOP/s" % (alg_flops, alg_flops / t_launch / 1e12)},
+                             "written) / mixed step time; the step kernels are FP32-issue bound on the CUDA "
+                             "cores, see compute"},
+        "compute": {"flops_per_step": alg_flops, "achieved_tflops": alg_flops / t_launch / 1e12,
+                    "fp32_fma_peak_tflops": fp32_peak, "fp32_peak_source": fp32_src,
+                    "frac_fp32_pipe": alg_flops / t_launch / 1e12 / fp32_peak,
+                    "frac_bf16_tensor_peak": alg_flops / t_launch / 1e12 / bf16,
+                    "note": "algorithmic flops of the implemented BUG step (FP32 and double-float "
+                            "multiply-adds counted once; a double-float one costs 12-15 FP32 instructions)"},
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -759,6 +923,13 @@ def main():
         line["cpu_baseline"] = {"value": cpu[0], "unit": UNIT, "cores": cpu[1], "kind": "port", "sample": cpu[2]}
     if e2e is not None:
         line["e2e"] = e2e
+    if ws == 1 and not args.no_legs:
+        # the other workloads, each timed on its own with its own clocks,
+        # accuracy, roofline and CPU sample
+        line["workloads"] = {"laplace_256": run_leg("laplace", args),
+                             "data_stream_8192x4096": run_leg("stream", args),
+                             "burgers_uq_4096x16384": run_leg("burgers", args),
+                             "adjoint_2048": run_leg("adjoint", args)}
     print(json.dumps(line), flush=True)
 
 
