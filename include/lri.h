@@ -267,6 +267,28 @@ LRI_API lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void
 LRI_API lri_status lri_stream_rank(lri_stream* s, int64_t* r_out, void* stream);
 LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
 
+/* The snapshot passes of an FP32 stream run on the tensor cores (tcgen05,
+ * operands staged by TMA; dY split into TF32 hi + lo parts, 3xTF32 products
+ * with FP32 accumulation) when n and m are multiples of 4 and at least 128;
+ * otherwise, and for FP64 streams, on the CUDA cores.  set_tensor_cores(0)
+ * selects the CUDA-core passes (LRI_ERR_UNSUPPORTED when asking for tensor
+ * cores the stream cannot use).  No counterpart in the reference. */
+LRI_API lri_status lri_stream_set_tensor_cores(lri_stream* s, int32_t enable);
+LRI_API lri_status lri_stream_uses_tensor_cores(const lri_stream* s, int32_t* out);
+
+/* One product of the data substeps (the increments left^T dY right of
+ * src/integrators/data_integrator.jl:13-16, dY = A(t+dt) - A(t) as in
+ * src/integrators/unconventional.jl:121-127) with the stream's passes:
+ *   trans = 0: out (n x ncols) = dY X,   X m x ncols (ld ldx)
+ *   trans = 1: out (m x ncols) = dY^T X, X n x ncols
+ * A_prev = A(t), A_next = A(t+dt) (n x m, column-major, the stream's
+ * dtype), 1 <= ncols <= r_max; out has leading dimension ldo (the CUDA-core
+ * passes need ldo = rows of out).  Uses the stream's workspace, so it must
+ * not overlap a step of the same stream. */
+LRI_API lri_status lri_stream_data_product(lri_stream* s, int32_t trans, const void* A_prev, const void* A_next,
+                                           const void* X, int64_t ldx, int64_t ncols, void* out, int64_t ldo,
+                                           void* stream);
+
 /* One large Burgers instance (the Burgers-UQ workload: n grid points x m
  * samples too large for the batch) on the same engine: rank-adaptive BUG
  * (rank_adaptive_unconventional.jl:194-233) for LRI_OP_BURGERS_PERIODIC with

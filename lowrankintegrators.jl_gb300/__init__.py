@@ -892,6 +892,31 @@ class DataStreamEngine:
         _native.check(self.lib.lri_stream_step(self.handle, C.c_void_p(A_prev.data_ptr()),
                                                C.c_void_p(A_next.data_ptr()), self._stream()), "lri_stream_step")
 
+    def set_tensor_cores(self, enable: bool):
+        """Selects the tensor-core (3xTF32) or CUDA-core snapshot passes."""
+        _native.check(self.lib.lri_stream_set_tensor_cores(self.handle, int(bool(enable))),
+                      "lri_stream_set_tensor_cores")
+
+    def uses_tensor_cores(self) -> bool:
+        v = C.c_int32(0)
+        _native.check(self.lib.lri_stream_uses_tensor_cores(self.handle, C.byref(v)), "lri_stream_uses_tensor_cores")
+        return bool(v.value)
+
+    def data_product(self, A_prev, A_next, X, trans: bool = False, out=None):
+        """(A_next - A_prev) @ X, or its transpose times X, with the stream's
+        passes; A_* are device snapshots (see to_device), X a device tensor
+        holding a column-major panel (rows x ncols, ncols <= rmax)."""
+        rows_x = self.n if trans else self.m
+        rows_o = self.m if trans else self.n
+        ncols = int(X.numel()) // rows_x
+        if out is None:
+            out = self.torch.empty(rows_o * self.R, dtype=self.dtype, device=self.device)
+        _native.check(self.lib.lri_stream_data_product(self.handle, int(bool(trans)), C.c_void_p(A_prev.data_ptr()),
+                                                        C.c_void_p(A_next.data_ptr()), C.c_void_p(X.data_ptr()),
+                                                        rows_x, ncols, C.c_void_p(out.data_ptr()), rows_o,
+                                                        self._stream()), "lri_stream_data_product")
+        return out
+
     def rank(self) -> int:
         r = C.c_int64(0)
         _native.check(self.lib.lri_stream_rank(self.handle, C.byref(r), self._stream()), "lri_stream_rank")

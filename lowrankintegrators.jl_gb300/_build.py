@@ -1,9 +1,9 @@
 """Builds the in-tree CUDA library ``_build/liblri_gb300.so`` for sm_103a.
 
-Seven translation units (FP32, FP64 and double-float engines, host C ABI,
+Eight translation units (FP32, FP64 and double-float engines, host C ABI,
 the allocation-free entry point, the discrete adjoint, the large-stream
-engine) compile in
-parallel with nvcc and link into one shared library.  The library is rebuilt
+engine, its tensor-core snapshot passes) compile in parallel with nvcc and
+link into one shared library.  The library is rebuilt
 when a source or the public header is newer than it.
 """
 from __future__ import annotations
@@ -19,7 +19,8 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liblri_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "lri.h")
 
-SOURCES = ["engine_f32.cu", "engine_f64.cu", "engine_df.cu", "api.cpp", "noalloc.cu", "adjoint.cu", "stream.cu"]
+SOURCES = ["engine_f32.cu", "engine_f64.cu", "engine_df.cu", "api.cpp", "noalloc.cu", "adjoint.cu", "stream.cu",
+           "tc_pass.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 

@@ -31,7 +31,8 @@ EXPORTED = [
     "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step", "lri_bug_step_noalloc",
     "lri_batch_prepare", "lri_batch_adjoint_prepare", "lri_batch_adjoint_step",
     "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
-    "lri_stream_status", "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
+    "lri_stream_status", "lri_stream_set_tensor_cores", "lri_stream_uses_tensor_cores", "lri_stream_data_product",
+    "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
 ]
 
 
@@ -103,6 +104,12 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_stream_rank.argtypes = [P, C.POINTER(C.c_int64), P]
     lib.lri_stream_status.restype = C.c_int
     lib.lri_stream_status.argtypes = [P, P]
+    lib.lri_stream_set_tensor_cores.restype = C.c_int
+    lib.lri_stream_set_tensor_cores.argtypes = [P, C.c_int32]
+    lib.lri_stream_uses_tensor_cores.restype = C.c_int
+    lib.lri_stream_uses_tensor_cores.argtypes = [P, C.POINTER(C.c_int32)]
+    lib.lri_stream_data_product.restype = C.c_int
+    lib.lri_stream_data_product.argtypes = [P, C.c_int32, P, P, P, C.c_int64, C.c_int64, P, C.c_int64, P]
     lib.lri_burgers_create.restype = C.c_int
     lib.lri_burgers_create.argtypes = [C.POINTER(P), C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                        C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double, P]

@@ -30,6 +30,7 @@ enum StatusBits : uint32_t {
   ST_SVD_NOCONV = 2u,
   ST_RANK_OVERFLOW = 4u,
   ST_BAD_SHAPE = 8u,
+  ST_TIMEOUT = 16u,  // a bounded device wait gave up
 };
 
 struct Scheme {

@@ -36,6 +36,7 @@
 
 #include "../../include/lri.h"
 #include "engine.cuh"
+#include "tc_pass.h"
 
 namespace lri {
 namespace {
@@ -1490,6 +1491,12 @@ struct lri_stream {
   void* Zp = nullptr;   // max(n, m) x 2R (dY Vhat; scratch of the orthonormalisation)
   double* part = nullptr;
   double* small = nullptr;
+  // FP32 data streams: snapshot passes on the tensor cores (tc_pass.cu)
+  bool tc_ok = false;   // shapes and device allow them
+  bool use_tc = false;  // selected (lri_stream_set_tensor_cores)
+  lri::TcPass tc;
+  void* Kd = nullptr;   // n x R: dY V0 of the step, reused as the first half of dY Vhat
+  int32_t* d_ncols = nullptr;  // column count of lri_stream_data_product on the CUDA-core passes
   // Burgers flow (lri_burgers_create): parameters and RK work panels
   bool burgers = false;
   double bh = 0.0, balpha = 0.0, bbeta = 0.0, bh_dt = 0.0;
@@ -1548,6 +1555,14 @@ struct StreamOps {
     } else {
       return mul(N, a, c, X, ldx, B, ldb, T(0), out, ldo);
     }
+  }
+  // the tensor-core passes: FP32 streams whose shapes they take, when selected
+  bool tc_selected() const { return std::is_same<T, float>::value && s->use_tc; }
+  cudaError_t tc_run(int trans, const T* A1, const T* A0, const T* X, int64_t ldx, T* out, int64_t ldo, T* kd,
+                     int ncols = -1) const {
+    if constexpr (std::is_same<T, float>::value)
+      return tc_pass_run(&s->tc, trans, A1, A0, X, ldx, s->d_rank, ncols, out, ldo, kd, s->d_status, ST_TIMEOUT, st);
+    return cudaErrorNotSupported;
   }
   using ST = typename SmallT<T>::type;
   cudaError_t pchol(int a, const double* G, double* B) const {
@@ -1866,9 +1881,16 @@ struct StreamOps {
     cudaError_t e = refresh();
     if (e != cudaSuccess) return e;
     // data passes 1 and 2: dY V0, dY^T U0
-    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_rank, A1, A0, V, m, Xk);
-    pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_rank, A1, A0, U, n, Xl);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const bool tc = tc_selected();
+    if (tc) {
+      e = tc_run(0, A1, A0, V, m, Xk, n, tp(s->Kd));
+      if (e == cudaSuccess) e = tc_run(1, A1, A0, U, n, Xl, m, nullptr);
+    } else {
+      pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_rank, A1, A0, V, m, Xk);
+      pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_rank, A1, A0, U, n, Xl);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return e;
     // Uhat = [U0 | orth((I - U0 U0^T) dY V0)], Vhat likewise
     if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
     if ((e = orth_against(m, Xl, V)) != cudaSuccess) return e;
@@ -1879,8 +1901,15 @@ struct StreamOps {
     // Mh = Uhat^T U0, Nh = Vhat^T V0 (w x R)
     if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
     if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
-    // data pass 3: Z = dY Vhat; D = Uhat^T Z
-    pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 1, s->d_rank, A1, A0, Vh, m, tp(s->Zp));
+    // data pass 3: Z = dY Vhat; D = Uhat^T Z.  On the tensor cores only
+    // dY Q_V is new (Vhat = [V0 | Q_V]): dY V0 is the copy kept by pass 1.
+    if (tc) {
+      copy_cols<T><<<304, 256, 0, st>>>(n, R, tp(s->Kd), n, tp(s->Zp), n);
+      if ((e = tc_run(0, A1, A0, Vh + (int64_t)R * m, m, tp(s->Zp) + (int64_t)R * n, n, nullptr)) != cudaSuccess)
+        return e;
+    } else {
+      pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 1, s->d_rank, A1, A0, Vh, m, tp(s->Zp));
+    }
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
     if ((e = core(w)) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
@@ -1954,6 +1983,12 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   alloc(&s->Zp, s->es * std::max(n, m) * 2 * R);
   alloc((void**)&s->part, sizeof(double) * nblk * 4 * R * R);
   alloc((void**)&s->small, sizeof(double) * kBlocksSmall * 4 * R * R);
+  alloc((void**)&s->d_ncols, sizeof(int32_t));
+  if (e == cudaSuccess && dtype == LRI_F32 && lri::tc_pass_supported(n, m, (int)R)) {
+    alloc(&s->Kd, s->es * n * R);
+    if (e == cudaSuccess) e = lri::tc_pass_init(&s->tc, n, m, (int)R);
+    s->tc_ok = s->use_tc = (e == cudaSuccess);
+  }
   const int32_t r32 = (int32_t)r0;
   if (e == cudaSuccess) e = cudaMemcpy(s->d_rank, &r32, sizeof(r32), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(uint32_t));
@@ -2058,6 +2093,9 @@ lri_status lri_stream_destroy(lri_stream* s) {
   cudaFree(s->Zp);
   cudaFree(s->part);
   cudaFree(s->small);
+  cudaFree(s->Kd);
+  cudaFree(s->d_ncols);
+  lri::tc_pass_free(&s->tc);
   delete s;
   return LRI_OK;
 }
@@ -2101,9 +2139,67 @@ lri_status lri_stream_status(lri_stream* s, void* stream) {
       cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
     return LRI_ERR_CUDA;
   if (w) cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), (cudaStream_t)stream);
+  if (w & ST_TIMEOUT) return LRI_ERR_TIMEOUT;
   if (w & ST_NONFINITE) return LRI_ERR_NONFINITE;
   if (w & ST_SVD_NOCONV) return LRI_ERR_BREAKDOWN;
   return w ? LRI_ERR_ARG : LRI_OK;
+}
+
+lri_status lri_stream_set_tensor_cores(lri_stream* s, int32_t enable) {
+  if (!s || s->burgers) return LRI_ERR_ARG;
+  if (enable && !s->tc_ok) return LRI_ERR_UNSUPPORTED;
+  s->use_tc = enable != 0;
+  return LRI_OK;
+}
+
+lri_status lri_stream_uses_tensor_cores(const lri_stream* s, int32_t* out) {
+  if (!s || !out) return LRI_ERR_ARG;
+  *out = s->use_tc ? 1 : 0;
+  return LRI_OK;
+}
+
+lri_status lri_stream_data_product(lri_stream* s, int32_t trans, const void* A_prev, const void* A_next,
+                                   const void* X, int64_t ldx, int64_t ncols, void* out, int64_t ldo, void* stream) {
+  if (!s || s->burgers || !A_prev || !A_next || !X || !out) return LRI_ERR_ARG;
+  if (trans != 0 && trans != 1) return LRI_ERR_ARG;
+  const int64_t rows_x = trans ? s->n : s->m, rows_o = trans ? s->m : s->n;
+  if (ncols < 1 || ncols > s->R || ldx < rows_x || ldo < rows_o) return LRI_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int R = (int)s->R, n = (int)s->n, m = (int)s->m;
+  cudaError_t e;
+  if (s->dtype == LRI_F32 && s->use_tc) {
+    e = StreamOps<float>{s, st}.tc_run(trans, static_cast<const float*>(A_next), static_cast<const float*>(A_prev),
+                                        static_cast<const float*>(X), ldx, static_cast<float*>(out), ldo, nullptr,
+                                        (int)ncols);
+    return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
+  }
+  // CUDA-core passes: the column count goes through a device word
+  const int32_t c32 = (int32_t)ncols;
+  if (cudaMemcpyAsync(s->d_ncols, &c32, sizeof(c32), cudaMemcpyHostToDevice, st) != cudaSuccess) return LRI_ERR_CUDA;
+  if (ldo != rows_o) return LRI_ERR_UNSUPPORTED;  // the CUDA-core passes write a packed panel
+  if (s->dtype == LRI_F32) {
+    auto A1 = static_cast<const float*>(A_next);
+    auto A0 = static_cast<const float*>(A_prev);
+    if (trans == 0)
+      pass_rows<float><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_ncols, A1, A0, static_cast<const float*>(X),
+                                                      (int)ldx, static_cast<float*>(out));
+    else
+      pass_cols<float><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_ncols, A1, A0, static_cast<const float*>(X),
+                                                      (int)ldx, static_cast<float*>(out));
+  } else {
+    auto A1 = static_cast<const double*>(A_next);
+    auto A0 = static_cast<const double*>(A_prev);
+    if (trans == 0)
+      pass_rows<double><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_ncols, A1, A0,
+                                                       static_cast<const double*>(X), (int)ldx,
+                                                       static_cast<double*>(out));
+    else
+      pass_cols<double><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_ncols, A1, A0,
+                                                       static_cast<const double*>(X), (int)ldx,
+                                                       static_cast<double*>(out));
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -1,0 +1,541 @@
+// tc_pass.cu - the snapshot passes of the data substeps on the 5th-generation
+// tensor cores.
+//
+// The data substeps (src/integrators/data_integrator.jl:13-16, driven by
+// dY = A(t+dt) - A(t), src/integrators/unconventional.jl:121-127) need the
+// products dY V0 (K step), dY^T U0 (L step) and dY Vhat (S step) of an n x m
+// snapshot increment with a tall panel of at most 128 columns.  They read
+// the two n x m FP32 snapshots once each and are bound by HBM; on the CUDA
+// cores they were bound by FP32 FMA issue instead.
+//
+// One CTA owns a 128-row tile of the output and a range of K (the
+// contraction index) in chunks of 32:
+//   warp 4   TMA producer: per chunk, the A(t+dt) and A(t) tiles (128 x 32)
+//            and the chunk's 32 rows of the split right factor (hi and lo);
+//   warps 0-3 form dY = A(t+dt) - A(t) in shared memory (exact in FP32 for
+//            nearby snapshots), split it into TF32 hi + lo parts in place,
+//            written in the K-major 128-byte-swizzled operand layout;
+//   warp 5   allocates tensor memory and issues, per 8-wide K slice,
+//            hi*hi + hi*lo + lo*hi tcgen05.mma (kind::tf32, M = 128,
+//            N = active columns rounded up to 16) into one FP32 accumulator;
+//   warps 0-3 finally read the accumulator (tcgen05.ld) and write the
+//            CTA's split-K partial; a second kernel sums the partials in a
+//            fixed order (deterministic) and writes the panel.
+// Rows of dY^T X: the snapshot tile arrives through TMA with the 128-byte
+// swizzle already in operand layout (K = rows of the snapshot are
+// contiguous), so forming and splitting dY is element-wise.  Rows of dY X:
+// the tile arrives row-contiguous and the four warps transpose it through
+// registers.  3xTF32 drops only the lo*lo term: products accurate to about
+// 2^-21 relative, summed in FP32.
+//
+// Every mbarrier wait is bounded (about two seconds of SM clock); a wait
+// that gives up sets a status bit, the CTA stops issuing work, waits (again
+// bounded) for its copies and MMAs in flight, frees its tensor memory and
+// returns.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's entry-point query)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+
+#include "engine_api.h"
+#include "tc_pass.h"
+
+namespace lri {
+namespace {
+
+constexpr int TC_BM = 128;                        // output rows per CTA (UMMA M)
+constexpr int TC_BK = 32;                         // K per pipeline stage: one 128-byte swizzle row of FP32
+constexpr int TC_THREADS = 192;                   // warps 0-3 transform/epilogue, 4 TMA, 5 MMA
+constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB snapshot tile
+constexpr int TC_MAX_STAGES = 4;
+constexpr int TC_TMEM_COLS = 128;                 // accumulator columns (N <= 128)
+constexpr int TC_SMEM_LIMIT = 232448;             // 227 KB opt-in per CTA
+constexpr int TC_CTRL_BYTES = 1024;               // barriers, tensor-memory address, abort flag
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
+
+struct TcArgs {
+  int P, R, NB, nchunks, chunks_per_split, stages, rows_mode, ncols;
+  const int32_t* rank;
+  float* part;
+  uint32_t* status;
+  uint32_t status_timeout;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Waits for the phase of `parity` to complete; gives up when another role
+// aborted or after TC_WAIT_CYCLES (then flags the abort and the status).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          const TcArgs& a, long long limit = TC_WAIT_CYCLES) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > limit) {
+      *abort_flag = 1;
+      atomicOr(a.status, a.status_timeout);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
+// 8-row groups 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B,
+// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\n"
+      "setp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// Round to the nearest TF32 value (19-bit container: sign, 8-bit exponent,
+// 10-bit mantissa; the low 13 bits of the result are zero).
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void split(float d, float& hi, float& lo) {
+  hi = tf32_rn(d);
+  lo = tf32_rn(d - hi);
+}
+
+// barrier over the 128 transform threads with an OR of `flag`
+__device__ __forceinline__ bool bar_any(bool flag) {
+  uint32_t out;
+  asm volatile(
+      "{\n.reg .pred p, q;\n"
+      "setp.ne.u32 p, %1, 0;\n"
+      "bar.red.or.pred q, 1, 128, p;\n"
+      "selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(out)
+      : "r"((uint32_t)flag)
+      : "memory");
+  return out != 0;
+}
+
+__device__ __forceinline__ int active_cols(const TcArgs& a) {
+  const int k = (a.ncols >= 0) ? a.ncols : *a.rank;
+  return max(0, min(a.R, k));
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_pass_kernel(const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmA0,
+                   const __grid_constant__ CUtensorMap tmXh, const __grid_constant__ CUtensorMap tmXl,
+                   const TcArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~static_cast<uintptr_t>(1023));
+  const int NS = a.stages;
+  const uint32_t xbytes = TC_BK * 4 * a.NB;  // one split-factor tile: NB rows of 128 bytes
+  const uint32_t stage_bytes = 2 * TC_TILE_BYTES + 2 * xbytes;
+  unsigned char* ctrl = base + NS * stage_bytes;
+  const uint32_t bar0 = smem_u32(ctrl);
+  auto full = [&](int s) { return bar0 + 8u * s; };                       // TMA bytes landed
+  auto tfull = [&](int s) { return bar0 + 8u * (TC_MAX_STAGES + s); };    // operands formed
+  auto empty = [&](int s) { return bar0 + 8u * (2 * TC_MAX_STAGES + s); };  // MMAs done with the stage
+  const uint32_t done = bar0 + 8u * (3 * TC_MAX_STAGES);                  // all MMAs done
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ctrl + 256);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(ctrl + 260);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x, sp = blockIdx.y;
+  const int kc0 = sp * a.chunks_per_split;
+  const int nk = min(a.nchunks, kc0 + a.chunks_per_split) - kc0;
+  const int ka = active_cols(a);
+  const int N = min(a.NB, max(16, (ka + 15) & ~15));
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(tfull(s), 128);
+      mbar_init(empty(s), 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int last_par[TC_MAX_STAGES];
+      for (int s = 0; s < TC_MAX_STAGES; ++s) last_par[s] = -1;
+      bool ok = true;
+      for (int it = 0; it < nk && ok; ++it) {
+        const int s = it % NS;
+        const uint32_t par = (uint32_t)(it / NS) & 1u;
+        if (!(ok = mbar_wait(empty(s), par ^ 1u, abort_flag, a))) break;
+        const int kc = kc0 + it;
+        const uint32_t st = smem_u32(base + (size_t)s * stage_bytes);
+        mbar_expect_tx(full(s), stage_bytes);
+        if (a.rows_mode) {
+          tma_load_2d(st, &tmA1, mt * TC_BM, kc * TC_BK, full(s));
+          tma_load_2d(st + TC_TILE_BYTES, &tmA0, mt * TC_BM, kc * TC_BK, full(s));
+        } else {
+          tma_load_2d(st, &tmA1, kc * TC_BK, mt * TC_BM, full(s));
+          tma_load_2d(st + TC_TILE_BYTES, &tmA0, kc * TC_BK, mt * TC_BM, full(s));
+        }
+        tma_load_2d(st + 2 * TC_TILE_BYTES, &tmXh, kc * TC_BK, 0, full(s));
+        tma_load_2d(st + 2 * TC_TILE_BYTES + xbytes, &tmXl, kc * TC_BK, 0, full(s));
+        last_par[s] = (int)par;
+      }
+      if (!ok || *abort_flag) {
+        // let the copies in flight land before the CTA's shared memory goes away
+        for (int s = 0; s < TC_MAX_STAGES; ++s)
+          if (last_par[s] >= 0) mbar_wait(full(s), (uint32_t)last_par[s], abort_flag, a, TC_WAIT_CYCLES / 4);
+      }
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_tf32(TC_BM, N);
+      for (int it = 0; it < nk; ++it) {
+        const int s = it % NS;
+        const uint32_t par = (uint32_t)(it / NS) & 1u;
+        if (!mbar_wait(full(s), par, abort_flag, a) || !mbar_wait(tfull(s), par, abort_flag, a)) break;
+        tc_fence_after();
+        const uint32_t sa1 = smem_u32(base + (size_t)s * stage_bytes);
+        const uint32_t sa0 = sa1 + TC_TILE_BYTES;
+        const uint32_t sxh = sa1 + 2 * TC_TILE_BYTES;
+        const uint32_t sxl = sxh + xbytes;
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 8; ++kk) {
+          const uint64_t ah = sw128_desc(sa1 + 32u * kk), al = sw128_desc(sa0 + 32u * kk);
+          const uint64_t bh = sw128_desc(sxh + 32u * kk), bl = sw128_desc(sxl + 32u * kk);
+          umma_tf32(tmem, ah, bh, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+          umma_tf32(tmem, ah, bl, idesc, 1u);
+          umma_tf32(tmem, al, bh, idesc, 1u);
+        }
+        umma_commit(empty(s));
+      }
+      umma_commit(done);  // arrives once every MMA issued above has completed
+      if (*abort_flag) mbar_wait(done, 0, abort_flag, a, TC_WAIT_CYCLES / 4);
+    }
+    __syncwarp();
+  } else {
+    // ---------------- form dY, split, then the epilogue (warps 0-3) ----------------
+    const int tid = threadIdx.x;
+    bool aborted = false;
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % NS;
+      const uint32_t par = (uint32_t)(it / NS) & 1u;
+      const bool ok = mbar_wait(full(s), par, abort_flag, a);
+      if (bar_any(!ok)) {
+        aborted = true;
+        break;
+      }
+      float* a1 = reinterpret_cast<float*>(base + (size_t)s * stage_bytes);
+      float* a0 = a1 + TC_BM * TC_BK;
+      if (a.rows_mode) {
+        // tile rows j (32) of 128 contiguous i; operand row i = this thread
+        float d[TC_BK];
+#pragma unroll
+        for (int j = 0; j < TC_BK; ++j) d[j] = a1[j * TC_BM + tid] - a0[j * TC_BM + tid];
+        bar_any(false);  // every thread has read its column before the tile is overwritten
+        unsigned char* h8 = reinterpret_cast<unsigned char*>(a1);
+        unsigned char* l8 = reinterpret_cast<unsigned char*>(a0);
+        const int rb = (tid >> 3) * 1024 + (tid & 7) * 128;
+#pragma unroll
+        for (int c = 0; c < TC_BK / 4; ++c) {
+          float4 h, l;
+          split(d[4 * c + 0], h.x, l.x);
+          split(d[4 * c + 1], h.y, l.y);
+          split(d[4 * c + 2], h.z, l.z);
+          split(d[4 * c + 3], h.w, l.w);
+          const int off = rb + ((c ^ (tid & 7)) << 4);
+          *reinterpret_cast<float4*>(h8 + off) = h;
+          *reinterpret_cast<float4*>(l8 + off) = l;
+        }
+      } else {
+        // the tile is already in operand layout: element-wise
+        float4* p1 = reinterpret_cast<float4*>(a1);
+        float4* p0 = reinterpret_cast<float4*>(a0);
+#pragma unroll
+        for (int u = 0; u < (TC_BM * TC_BK / 4) / 128; ++u) {
+          const int q = tid + 128 * u;
+          const float4 x1 = p1[q], x0 = p0[q];
+          float4 h, l;
+          split(x1.x - x0.x, h.x, l.x);
+          split(x1.y - x0.y, h.y, l.y);
+          split(x1.z - x0.z, h.z, l.z);
+          split(x1.w - x0.w, h.w, l.w);
+          p1[q] = h;
+          p0[q] = l;
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
+      mbar_arrive(tfull(s));
+    }
+    if (!aborted) {
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, abort_flag, a));
+      if (ok) {
+        tc_fence_after();
+        const int row = mt * TC_BM + warp * 32 + lane;
+        float* out = a.part + (size_t)sp * a.NB * a.P;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+          if (row < a.P) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) out[(size_t)(c0 + q) * a.P + row] = v[q];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 5) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+// TF32 hi / lo parts of the active columns of X (rows x R, ld ldx) into
+// xh, xl (rows x NB, ld rows); inactive and padding columns become zeros.
+__global__ void tc_split_x(int rows, int R, int NB, const int32_t* rank, int ncols, const float* __restrict__ X,
+                           int64_t ldx, float* __restrict__ xh, float* __restrict__ xl) {
+  const int ka = max(0, min(R, ncols >= 0 ? ncols : *rank));
+  const int64_t total = (int64_t)rows * NB;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(e % rows), col = (int)(e / rows);
+    const float x = (col < ka) ? X[row + (int64_t)col * ldx] : 0.0f;
+    float h, l;
+    split(x, h, l);
+    xh[e] = h;
+    xl[e] = l;
+  }
+}
+
+// out[:, c] = sum over splits (fixed order) of the partials, c < active;
+// zeros for the other columns < R
+__global__ void tc_reduce(int P, int R, int NB, int splits, const int32_t* rank, int ncols,
+                          const float* __restrict__ part, float* __restrict__ out, int64_t ldo, float* __restrict__ kd) {
+  const int ka = max(0, min(R, ncols >= 0 ? ncols : *rank));
+  const int64_t total = (int64_t)P * R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(e % P), col = (int)(e / P);
+    float v = 0.0f;
+    if (col < ka)
+      for (int s = 0; s < splits; ++s) v += part[((int64_t)s * NB + col) * P + row];
+    out[row + (int64_t)col * ldo] = v;
+    if (kd) kd[e] = v;
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encoder() {
+  static std::atomic<void*> fn{nullptr};
+  void* f = fn.load(std::memory_order_acquire);
+  if (!f) {
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f)
+      return nullptr;
+    fn.store(f, std::memory_order_release);
+  }
+  return reinterpret_cast<EncodeTiledFn>(f);
+}
+
+// 2-D FP32 tensor map of a column-major rows x cols matrix (ld = rows)
+bool encode_2d(void* out, const void* ptr, uint64_t rows, uint64_t cols, uint32_t box0, uint32_t box1, bool swizzle) {
+  EncodeTiledFn enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {rows, cols};
+  const cuuint64_t strides[1] = {rows * 4};
+  const cuuint32_t box[2] = {box0, box1};
+  const cuuint32_t es[2] = {1, 1};
+  return enc(reinterpret_cast<CUtensorMap*>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims,
+             strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct Plan {
+  int P, K, tiles, nchunks, cps, splits;
+};
+
+Plan plan(int64_t P, int64_t K, int sms) {
+  Plan p{};
+  p.P = (int)P;
+  p.K = (int)K;
+  p.tiles = (int)((P + TC_BM - 1) / TC_BM);
+  p.nchunks = (int)((K + TC_BK - 1) / TC_BK);
+  int splits = std::max(1, sms / p.tiles);
+  splits = std::min(splits, std::max(1, p.nchunks / 4));  // at least 4 chunks (one pipeline fill) per CTA
+  p.cps = (p.nchunks + splits - 1) / splits;
+  p.splits = (p.nchunks + p.cps - 1) / p.cps;
+  return p;
+}
+
+int stages_for(int NB) {
+  const int stage = 2 * (int)TC_TILE_BYTES + 2 * TC_BK * 4 * NB;
+  return std::min(TC_MAX_STAGES, (TC_SMEM_LIMIT - TC_CTRL_BYTES - 1024) / stage);
+}
+
+}  // namespace
+
+bool tc_pass_supported(int64_t n, int64_t m, int R) {
+  return n >= TC_BM && m >= TC_BM && (n % 4) == 0 && (m % 4) == 0 && R >= 1 && R <= TC_TMEM_COLS &&
+         n < (int64_t(1) << 30) && m < (int64_t(1) << 30) && encoder() != nullptr;
+}
+
+cudaError_t tc_pass_init(TcPass* t, int64_t n, int64_t m, int R) {
+  t->n = n;
+  t->m = m;
+  t->R = R;
+  t->NB = (R + 15) & ~15;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t rows = std::max(n, m);
+  const Plan pr = plan(n, m, t->sms), pc = plan(m, n, t->sms);
+  const size_t part = std::max((size_t)pr.splits * n, (size_t)pc.splits * m) * t->NB;
+  e = cudaMalloc((void**)&t->xh, sizeof(float) * rows * t->NB);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&t->xl, sizeof(float) * rows * t->NB);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&t->part, sizeof(float) * part);
+  if (e != cudaSuccess) return e;
+  const bool ok = encode_2d(t->tm_xh_m, t->xh, m, t->NB, TC_BK, t->NB, true) &&
+                  encode_2d(t->tm_xl_m, t->xl, m, t->NB, TC_BK, t->NB, true) &&
+                  encode_2d(t->tm_xh_n, t->xh, n, t->NB, TC_BK, t->NB, true) &&
+                  encode_2d(t->tm_xl_n, t->xl, n, t->NB, TC_BK, t->NB, true);
+  return ok ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+void tc_pass_free(TcPass* t) {
+  cudaFree(t->xh);
+  cudaFree(t->xl);
+  cudaFree(t->part);
+  t->xh = t->xl = t->part = nullptr;
+}
+
+cudaError_t tc_pass_run(TcPass* t, int trans, const float* A1, const float* A0, const float* X, int64_t ldx,
+                        const int32_t* rank, int ncols, float* out, int64_t ldo, float* kd, uint32_t* status,
+                        uint32_t status_timeout, cudaStream_t st) {
+  if ((reinterpret_cast<uintptr_t>(A1) | reinterpret_cast<uintptr_t>(A0)) & 15) return cudaErrorInvalidValue;
+  const int64_t n = t->n, m = t->m;
+  const bool rows_mode = (trans == 0);
+  const int64_t P = rows_mode ? n : m, K = rows_mode ? m : n;
+  alignas(64) unsigned char tm1[128], tm0[128];
+  const bool ok = rows_mode ? (encode_2d(tm1, A1, n, m, TC_BM, TC_BK, false) && encode_2d(tm0, A0, n, m, TC_BM, TC_BK, false))
+                            : (encode_2d(tm1, A1, n, m, TC_BK, TC_BM, true) && encode_2d(tm0, A0, n, m, TC_BK, TC_BM, true));
+  if (!ok) return cudaErrorInvalidValue;
+  const Plan pl = plan(P, K, t->sms);
+  const int NB = t->NB;
+  tc_split_x<<<2 * t->sms, 256, 0, st>>>((int)K, t->R, NB, rank, ncols, X, ldx, t->xh, t->xl);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int stages = stages_for(NB);
+  const size_t smem = (size_t)stages * (2 * TC_TILE_BYTES + 2 * TC_BK * 4 * NB) + TC_CTRL_BYTES + 1024;
+  static std::atomic<uint64_t> attr_done{0};  // the largest any panel width needs
+  if ((e = set_smem_limit(tc_pass_kernel, TC_SMEM_LIMIT, attr_done)) != cudaSuccess) return e;
+  TcArgs a{};
+  a.P = (int)P;
+  a.R = t->R;
+  a.NB = NB;
+  a.nchunks = pl.nchunks;
+  a.chunks_per_split = pl.cps;
+  a.stages = stages;
+  a.rows_mode = rows_mode ? 1 : 0;
+  a.ncols = ncols;
+  a.rank = rank;
+  a.part = t->part;
+  a.status = status;
+  a.status_timeout = status_timeout;
+  const CUtensorMap* xh = reinterpret_cast<const CUtensorMap*>(rows_mode ? t->tm_xh_m : t->tm_xh_n);
+  const CUtensorMap* xl = reinterpret_cast<const CUtensorMap*>(rows_mode ? t->tm_xl_m : t->tm_xl_n);
+  tc_pass_kernel<<<dim3(pl.tiles, pl.splits), TC_THREADS, smem, st>>>(
+      *reinterpret_cast<const CUtensorMap*>(tm1), *reinterpret_cast<const CUtensorMap*>(tm0), *xh, *xl, a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  tc_reduce<<<2 * t->sms, 256, 0, st>>>((int)P, t->R, NB, pl.splits, rank, ncols, t->part, out, ldo, kd);
+  return cudaGetLastError();
+}
+
+}  // namespace lri
