@@ -4,7 +4,7 @@
 // The data substeps (src/integrators/data_integrator.jl:13-16, driven by
 // dY = A(t+dt) - A(t), src/integrators/unconventional.jl:121-127) need the
 // products dY V0 (K step), dY^T U0 (L step) and dY Vhat (S step) of an n x m
-// snapshot increment with a tall panel of at most 128 columns.  They read
+// snapshot increment with a tall panel of at most 96 columns.  They read
 // the two n x m FP32 snapshots once each and are bound by HBM; on the CUDA
 // cores they were bound by FP32 FMA issue instead.
 //
@@ -16,11 +16,19 @@
 //            nearby snapshots), split it into TF32 hi + lo parts in place,
 //            written in the K-major 128-byte-swizzled operand layout;
 //   warp 5   allocates tensor memory and issues, per 8-wide K slice,
-//            hi*hi + hi*lo + lo*hi tcgen05.mma (kind::tf32, M = 128,
-//            N = active columns rounded up to 16) into one FP32 accumulator;
-//   warps 0-3 finally read the accumulator (tcgen05.ld) and write the
-//            CTA's split-K partial; a second kernel sums the partials in a
-//            fixed order (deterministic) and writes the panel.
+//            tcgen05.mma (kind::tf32, M = 128, N = active columns rounded
+//            up to 16): hi*hi into one FP32 accumulator, hi*lo + lo*hi into
+//            a second (correction) one;
+//   warps 0-3 also drain the accumulators: the tensor cores' FP32
+//            accumulation truncates, so its error grows with the number of
+//            MMAs summed into one accumulator (1.4e-5 relative over 2048
+//            terms of K).  Every TC_DRAIN chunks (128 terms) the MMAs switch
+//            to the other of two accumulator buffers while the four warps
+//            add the finished block into FP32 registers (tcgen05.ld, round
+//            to nearest) and hand the buffer back;
+//   warps 0-3 finally write the CTA's split-K partial; a second kernel sums
+//            the partials in a fixed order (deterministic) and writes the
+//            panel.
 // Rows of dY^T X: the snapshot tile arrives through TMA with the 128-byte
 // swizzle already in operand layout (K = rows of the snapshot are
 // contiguous), so forming and splitting dY is element-wise.  Rows of dY X:
@@ -51,7 +59,9 @@ constexpr int TC_BK = 32;                         // K per pipeline stage: one 1
 constexpr int TC_THREADS = 192;                   // warps 0-3 transform/epilogue, 4 TMA, 5 MMA
 constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB snapshot tile
 constexpr int TC_MAX_STAGES = 4;
-constexpr int TC_TMEM_COLS = 128;                 // accumulator columns (N <= 128)
+constexpr int TC_MAX_NB = 96;                     // panel columns (N <= 96)
+constexpr int TC_DRAIN = 4;                       // chunks accumulated in tensor memory between drains
+constexpr int TC_DRAIN_LAG = 2;                   // chunks of the next block queued before a drain
 constexpr int TC_SMEM_LIMIT = 232448;             // 227 KB opt-in per CTA
 constexpr int TC_CTRL_BYTES = 1024;               // barriers, tensor-memory address, abort flag
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
@@ -203,10 +213,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t stage_bytes = 2 * TC_TILE_BYTES + 2 * xbytes;
   unsigned char* ctrl = base + NS * stage_bytes;
   const uint32_t bar0 = smem_u32(ctrl);
-  auto full = [&](int s) { return bar0 + 8u * s; };                       // TMA bytes landed
-  auto tfull = [&](int s) { return bar0 + 8u * (TC_MAX_STAGES + s); };    // operands formed
-  auto empty = [&](int s) { return bar0 + 8u * (2 * TC_MAX_STAGES + s); };  // MMAs done with the stage
-  const uint32_t done = bar0 + 8u * (3 * TC_MAX_STAGES);                  // all MMAs done
+  auto full = [&](int s) { return bar0 + 8u * s; };                          // TMA bytes landed
+  auto tfull = [&](int s) { return bar0 + 8u * (TC_MAX_STAGES + s); };       // operands formed
+  auto empty = [&](int s) { return bar0 + 8u * (2 * TC_MAX_STAGES + s); };   // MMAs done with the stage
+  auto acc_full = [&](int b) { return bar0 + 8u * (3 * TC_MAX_STAGES + b); };       // a block's MMAs done
+  auto acc_empty = [&](int b) { return bar0 + 8u * (3 * TC_MAX_STAGES + 2 + b); };  // a block drained
+  const uint32_t done = bar0 + 8u * (3 * TC_MAX_STAGES + 4);                 // every MMA done
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ctrl + 256);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(ctrl + 260);
 
@@ -214,8 +226,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int mt = blockIdx.x, sp = blockIdx.y;
   const int kc0 = sp * a.chunks_per_split;
   const int nk = min(a.nchunks, kc0 + a.chunks_per_split) - kc0;
+  const int nblocks = (nk + TC_DRAIN - 1) / TC_DRAIN;
   const int ka = active_cols(a);
   const int N = min(a.NB, max(16, (ka + 15) & ~15));
+  // accumulator buffer b: hi*hi sums in columns [2 b NB, 2 b NB + N), the
+  // hi*lo + lo*hi corrections NB columns further
+  const uint32_t ncols_tmem = (4 * a.NB > 256) ? 512u : ((4 * a.NB > 128) ? 256u : 128u);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
@@ -223,13 +239,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(tfull(s), 128);
       mbar_init(empty(s), 1);
     }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), 128);
+    }
     mbar_init(done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 5) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TC_TMEM_COLS)
+                 "r"(ncols_tmem)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -275,30 +295,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int it = 0; it < nk; ++it) {
         const int s = it % NS;
         const uint32_t par = (uint32_t)(it / NS) & 1u;
+        const int bi = it / TC_DRAIN, b = bi & 1;
+        const bool first = (it % TC_DRAIN) == 0;
+        // the buffer's previous block (bi - 2) must have been drained
+        if (first && bi >= 2 && !mbar_wait(acc_empty(b), (uint32_t)((bi >> 1) - 1) & 1u, abort_flag, a)) break;
         if (!mbar_wait(full(s), par, abort_flag, a) || !mbar_wait(tfull(s), par, abort_flag, a)) break;
         tc_fence_after();
         const uint32_t sa1 = smem_u32(base + (size_t)s * stage_bytes);
         const uint32_t sa0 = sa1 + TC_TILE_BYTES;
         const uint32_t sxh = sa1 + 2 * TC_TILE_BYTES;
         const uint32_t sxl = sxh + xbytes;
+        const uint32_t dmain = tmem + (uint32_t)(2 * b * a.NB), dcorr = dmain + (uint32_t)a.NB;
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 8; ++kk) {
           const uint64_t ah = sw128_desc(sa1 + 32u * kk), al = sw128_desc(sa0 + 32u * kk);
           const uint64_t bh = sw128_desc(sxh + 32u * kk), bl = sw128_desc(sxl + 32u * kk);
-          umma_tf32(tmem, ah, bh, idesc, (it > 0 || kk > 0) ? 1u : 0u);
-          umma_tf32(tmem, ah, bl, idesc, 1u);
-          umma_tf32(tmem, al, bh, idesc, 1u);
+          const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
+          umma_tf32(dmain, ah, bh, idesc, acc);
+          umma_tf32(dcorr, ah, bl, idesc, acc);
+          umma_tf32(dcorr, al, bh, idesc, 1u);
         }
         umma_commit(empty(s));
+        if ((it % TC_DRAIN) == TC_DRAIN - 1 || it == nk - 1) umma_commit(acc_full(b));
       }
       umma_commit(done);  // arrives once every MMA issued above has completed
       if (*abort_flag) mbar_wait(done, 0, abort_flag, a, TC_WAIT_CYCLES / 4);
     }
     __syncwarp();
   } else {
-    // ---------------- form dY, split, then the epilogue (warps 0-3) ----------------
+    // -------- form dY, split; drain the accumulators; epilogue (warps 0-3) --------
     const int tid = threadIdx.x;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    float acc[TC_MAX_NB];
+#pragma unroll
+    for (int c = 0; c < TC_MAX_NB; ++c) acc[c] = 0.0f;
     bool aborted = false;
+    int drained = 0;
+    // adds block k's hi*hi and correction sums (FP32, round to nearest) into
+    // the registers and hands the buffer back to the MMA issuer
+    auto drain = [&](int k) {
+      const int b = k & 1;
+      const bool ok = mbar_wait(acc_full(b), (uint32_t)(k >> 1) & 1u, abort_flag, a);
+      if (bar_any(!ok)) return false;
+      tc_fence_after();
+      const uint32_t dmain = tmem + lane_base + (uint32_t)(2 * b * a.NB), dcorr = dmain + (uint32_t)a.NB;
+#pragma unroll
+      for (int c0 = 0; c0 < TC_MAX_NB; c0 += 16) {
+        if (c0 < N) {
+          float v[16], w[16];
+          tmem_ld16(dmain + (uint32_t)c0, v);
+          tmem_ld16(dcorr + (uint32_t)c0, w);
+#pragma unroll
+          for (int q = 0; q < 16; ++q) acc[c0 + q] += v[q] + w[q];
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(acc_empty(b));
+      return true;
+    };
     for (int it = 0; it < nk; ++it) {
       const int s = it % NS;
       const uint32_t par = (uint32_t)(it / NS) & 1u;
@@ -348,21 +402,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
       mbar_arrive(tfull(s));
+      // the previous block is drained once this block has a few chunks queued
+      if ((it % TC_DRAIN) == TC_DRAIN_LAG && it >= TC_DRAIN) {
+        if (!drain(drained)) {
+          aborted = true;
+          break;
+        }
+        ++drained;
+      }
+    }
+    while (!aborted && drained < nblocks) {
+      if (!drain(drained)) aborted = true;
+      ++drained;
     }
     if (!aborted) {
-      const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, abort_flag, a));
-      if (ok) {
-        tc_fence_after();
-        const int row = mt * TC_BM + warp * 32 + lane;
-        float* out = a.part + (size_t)sp * a.NB * a.P;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-          float v[16];
-          tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-          if (row < a.P) {
+      const int row = mt * TC_BM + warp * 32 + lane;
+      float* out = a.part + (size_t)sp * a.NB * a.P;
+      if (row < a.P) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) out[(size_t)(c0 + q) * a.P + row] = v[q];
-          }
-        }
+        for (int c = 0; c < TC_MAX_NB; ++c)
+          if (c < N) out[(size_t)c * a.P + row] = acc[c];
       }
     }
   }
@@ -370,7 +429,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   if (warp == 5) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem) : "memory");
   }
 }
 
@@ -462,7 +521,7 @@ int stages_for(int NB) {
 }  // namespace
 
 bool tc_pass_supported(int64_t n, int64_t m, int R) {
-  return n >= TC_BM && m >= TC_BM && (n % 4) == 0 && (m % 4) == 0 && R >= 1 && R <= TC_TMEM_COLS &&
+  return n >= TC_BM && m >= TC_BM && (n % 4) == 0 && (m % 4) == 0 && R >= 1 && R <= TC_MAX_NB &&
          n < (int64_t(1) << 30) && m < (int64_t(1) << 30) && encoder() != nullptr;
 }
 

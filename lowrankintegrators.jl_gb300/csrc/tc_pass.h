@@ -25,7 +25,7 @@ struct TcPass {
 };
 
 // Shapes the tensor-core passes take: FP32 n x m snapshots with n, m
-// multiples of 4 (16-byte TMA strides) and at least 128, panel width R <= 128.
+// multiples of 4 (16-byte TMA strides) and at least 128, panel width R <= 96.
 bool tc_pass_supported(int64_t n, int64_t m, int R);
 
 // Allocates the split buffers and partials and encodes their tensor maps.
