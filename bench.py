@@ -281,6 +281,38 @@ def leg_stream(steps, warmup):
     ms = e0.elapsed_time(e1) / K
     eng.check_status()
     rank_end = eng.rank()
+    tc_used = eng.uses_tensor_cores()
+
+    # the dominant kernel: one snapshot pass (dY X, dY^T X with 96 columns)
+    # timed alone, on the tensor cores and on the CUDA cores
+    def time_pass(trans, tc, reps=20):
+        eng.set_tensor_cores(tc)
+        X = torch.randn((n if trans else m) * R, dtype=torch.float32, device=A[0].device)
+        out = eng.data_product(A[0], A[1], X, trans=trans)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for j in range(reps):  # alternate snapshot pairs: 268 MB per pass, more than L2
+            eng.data_product(A[j % 4], A[j % 4 + 1], X, trans=trans, out=out)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        return f0.elapsed_time(f1) / reps
+    pass_ms = {}
+    if tc_used:
+        pass_ms["tensor_cores"] = {"dY_X_ms": time_pass(False, True), "dYt_X_ms": time_pass(True, True)}
+    pass_ms["cuda_cores"] = {"dY_X_ms": time_pass(False, False), "dYt_X_ms": time_pass(True, False)}
+    # the same steps with the CUDA-core passes, for comparison
+    eng.set_tensor_cores(False)
+    eng.bind(Y0)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for j in range(W, W + K):
+        eng.step(A[j], A[j + 1])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_cuda_core = e0.elapsed_time(e1) / K
+    eng.set_tensor_cores(tc_used)
+    eng.check_status()
     # e2e: next snapshot from pinned host memory every step, rank read back
     hostA = [A[j].cpu().pin_memory() for j in range(4)]
     dA = [torch.empty_like(A[0]) for _ in range(2)]
@@ -310,7 +342,13 @@ def leg_stream(steps, warmup):
     err = float(np.sqrt(max(d2, 0.0) / gram_fro(Yo, Yo)))
     hbm, bf16, src = peaks()
     alg_bytes = 2 * 2 * n * m * 4
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    pass_bytes = 2 * n * m * 4  # one pass reads both snapshots once
+    kern = pass_ms.get("tensor_cores", pass_ms["cuda_cores"])
+    t_pass = 0.5 * (kern["dY_X_ms"] + kern["dYt_X_ms"]) * 1e-3
+    achieved = pass_bytes / t_pass / 1e9
+    for v in pass_ms.values():
+        v["GB_per_s"] = pass_bytes / (0.5 * (v["dY_X_ms"] + v["dYt_X_ms"]) * 1e-3) / 1e9
+    flops_pass = 2.0 * n * m * R
     line = {"metric": "rank-adaptive BUG steps/s (8192x4096 FP32 data stream, r <= 96)", "value": 1e3 / ms,
             "unit": "steps/s", "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (device-generated stream)",
@@ -318,10 +356,18 @@ def leg_stream(steps, warmup):
                        "rank_after": rank_end, "l2": "inputs larger than L2 (134 MB per snapshot)"},
             "accuracy": {"steps": 3, "rel_fro_vs_fp64_oracle": err, "rank_gpu": Yg.S.shape[0],
                          "rank_oracle": Yo.S.shape[0]},
+            "passes": pass_ms,
+            "ms_per_step_cuda_core_passes": ms_cuda_core,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "peak_source": src, "algorithmic_bytes_per_launch": alg_bytes,
-                         "note": "algorithmic bytes = the reference formulation's two passes over the snapshot "
-                                 "pair; this engine makes three (dY V0, dY^T U0, dY Vhat)"},
+                         "traffic": None, "peak_source": src,
+                         "kernel": "tc_pass_kernel (tcgen05 + TMA, 3xTF32)" if tc_used else "pass_rows/pass_cols",
+                         "algorithmic_bytes_per_launch": pass_bytes,
+                         "tensor_tflops": flops_pass * 3 / t_pass / 1e12,
+                         "note": "one snapshot pass (both snapshots read once, 96 columns), mean of dY X and dY^T X, "
+                                 "CUDA events around the whole call (TF32 split of the panel, the pass, the "
+                                 "split-K sum); a step makes three passes (dY V0, dY^T U0, dY Q_V), "
+                                 "step-level bytes %.0f MB / %.3f ms = %.0f GB/s"
+                                 % (alg_bytes / 1e6, ms, alg_bytes / (ms * 1e-3) / 1e9)},
             "gpu_launches": None,
             "clocks": sampler.summary(),
             "cpu_baseline": {"value": 1.0 / cpu_step, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
