@@ -301,9 +301,11 @@ def leg_stream(steps, warmup):
     if tc_used:
         pass_ms["tensor_cores"] = {"dY_X_ms": time_pass(False, True), "dYt_X_ms": time_pass(True, True)}
     pass_ms["cuda_cores"] = {"dY_X_ms": time_pass(False, False), "dYt_X_ms": time_pass(True, False)}
-    # the same steps with the CUDA-core passes, for comparison
+    # the same steps with the CUDA-core passes, for comparison (same warm-up)
     eng.set_tensor_cores(False)
     eng.bind(Y0)
+    for j in range(W):
+        eng.step(A[j], A[j + 1])
     torch.cuda.synchronize()
     e0.record(stream)
     for j in range(W, W + K):
