@@ -75,8 +75,19 @@ typedef enum { LRI_F64 = 0, LRI_F32 = 1, LRI_DF = 2 } lri_dtype;
 
 /* Algorithms: UnconventionalAlgorithm (unconventional.jl:13-21),
  * RankAdaptiveUnconventionalAlgorithm (rank_adaptive_unconventional.jl:15-23),
- * ProjectorSplitting (projector_splitting.jl:27-41). */
-typedef enum { LRI_ALG_BUG = 0, LRI_ALG_RA_BUG = 1, LRI_ALG_KSL = 2 } lri_alg_kind;
+ * ProjectorSplitting (projector_splitting.jl:27-41),
+ * GreedyIntegrator (greedy_integrator.jl:17-24; fixed rank):
+ *   two_factor = 0, op DATA: SVD-like factors, U = Q of qr(X V),
+ *       V = Q of qr(X^T U), S = U^T X V (greedy_integrator.jl:96-104);
+ *   two_factor = 1, op DATA: u = U Z^T with Z in the V buffer (S unused):
+ *       Z = X^T U, U = polar factor of X Z (:84-94);
+ *   two_factor = 1, op ZERO / SYLVESTER / BURGERS: MatrixHybridProblem
+ *       (primitives.jl:36-41): Z advanced over [t, t+dt] by the L-substep
+ *       flow Z' = F(U Z^T)^T U of the operator (the reference's coefficient
+ *       ODE f(Z, U, t) for a flow map F) with the L_alg scheme, then
+ *       U = polar factor of X Z (:73-82).
+ *   X = y(t+dt) is the snapshot passed to every lri_batch_step call. */
+typedef enum { LRI_ALG_BUG = 0, LRI_ALG_RA_BUG = 1, LRI_ALG_KSL = 2, LRI_ALG_GREEDY = 3 } lri_alg_kind;
 typedef enum { LRI_KSL_PRIMAL = 0, LRI_KSL_DUAL = 1, LRI_KSL_STRANG = 2 } lri_ksl_order;
 
 /* Flow maps.  The reference accepts any Julia closure F(Y,t) evaluated by
@@ -117,7 +128,7 @@ typedef struct {
   lri_scheme K_alg, L_alg, S_alg;
   double tol;          /* rank-adaptive truncation tolerance (absolute) */
   int32_t r_min;       /* rank-adaptive lower bound (>= 1); no reference counterpart */
-  int32_t reserved;
+  int32_t two_factor;  /* GreedyIntegrator only: 1 = factors U Z^T (TwoFactorRepresentation) */
 } lri_alg_desc;
 
 typedef struct {
@@ -166,8 +177,9 @@ LRI_API lri_status lri_batch_data_layout(const lri_batch* b, int64_t* offY, int6
 LRI_API lri_status lri_batch_data_init(lri_batch* b, const void* Y0, void* stream);
 
 /* step!(integrator, alg, dt), nsteps times, starting at time t.  For DATA
- * problems nsteps must be 1 and Ynext points at A(t+dt) for every instance
- * (same packing as lri_batch_data_init); for other operators Ynext is NULL.
+ * problems and GreedyIntegrator batches nsteps must be 1 and Ynext points at
+ * A(t+dt) for every instance (same packing as lri_batch_data_init; the
+ * greedy steps need no lri_batch_data_init); for other batches Ynext is NULL.
  * Runs asynchronously on `stream` (cudaStream_t, NULL = legacy default);
  * multi-step calls run as one captured CUDA graph. */
 LRI_API lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, const void* Ynext,
@@ -306,6 +318,27 @@ LRI_API lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n
                                       double beta, const lri_scheme* scheme);
 LRI_API lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void* nu);
 LRI_API lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stream);
+
+/* Solution history (update_sol!, src/primitives.jl:82-90, which deep-copies
+ * the factors after every step).  A history owns `slots` device copies of
+ * the batch's factors and ranks and a copy stream of its own.
+ * lri_history_record queues, on `stream` after the work already queued
+ * there, a device-to-device copy of the bound U, S, V and the ranks into the
+ * next slot, then (on the history's stream) the copy of that slot into the
+ * caller's host buffers: U, S, V packed like the bound buffers in the
+ * batch's dtype (FP64 for double-float batches), ranks as int32 per
+ * instance (optional).  The host buffers should be page-locked for the copy
+ * to overlap the next steps, and must stay valid until lri_history_wait
+ * returns for the record.  When a slot comes round again, `stream` first
+ * waits for its previous host copy.  *seq receives the record's number
+ * (0, 1, ...).  lri_history_wait blocks the calling thread until record seq
+ * is on the host.  No counterpart in the reference's API. */
+typedef struct lri_history lri_history;
+LRI_API lri_status lri_history_create(lri_history** out, lri_batch* b, int32_t slots);
+LRI_API lri_status lri_history_destroy(lri_history* h);
+LRI_API lri_status lri_history_record(lri_history* h, void* hostU, void* hostS, void* hostV, int32_t* host_ranks,
+                                      void* stream, int64_t* seq);
+LRI_API lri_status lri_history_wait(lri_history* h, int64_t seq);
 
 /* Number of kernel launches a single-step lri_batch_step call makes. */
 LRI_API int32_t lri_batch_launches_per_step(const lri_batch* b);

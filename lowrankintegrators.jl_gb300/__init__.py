@@ -27,11 +27,12 @@ from . import _native
 from ._native import LriError
 
 __all__ = [
-    "SVDLikeRepresentation", "MatrixDEProblem", "MatrixDataProblem", "DLRSolution", "DLRIntegrator",
-    "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm", "ProjectorSplitting",
+    "SVDLikeRepresentation", "TwoFactorRepresentation", "MatrixDEProblem", "MatrixDataProblem",
+    "MatrixHybridProblem", "DLRSolution", "DLRIntegrator",
+    "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm", "ProjectorSplitting", "GreedyIntegrator",
     "PrimalLieTrotter", "DualLieTrotter", "Strang", "SubstepScheme", "Euler", "Heun", "Midpoint", "RK4",
     "ZeroOperator", "SylvesterTridiagOperator", "Batch", "MixedEnsemble", "init", "step", "solve",
-    "solve_ensemble", "core_condition",
+    "solve_ensemble", "core_condition", "History",
     "LriError", "n_steps",
 ]
 
@@ -60,6 +61,29 @@ class SVDLikeRepresentation:
 
     def copy(self) -> "SVDLikeRepresentation":
         return SVDLikeRepresentation(self.U.copy(), self.S.copy(), self.V.copy())
+
+
+@dataclass
+class TwoFactorRepresentation:
+    """Y = U Z^T (U n x r orthonormal, Z m x r), host arrays in float64
+    (LowRankArithmetic's TwoFactorRepresentation, used by the greedy
+    integrator, src/integrators/greedy_integrator.jl:26-32,73-94)."""
+    U: np.ndarray
+    Z: np.ndarray
+
+    @property
+    def rank(self) -> int:
+        return self.U.shape[1]
+
+    @property
+    def shape(self) -> Tuple[int, int]:
+        return (self.U.shape[0], self.Z.shape[0])
+
+    def full(self) -> np.ndarray:
+        return self.U @ self.Z.T
+
+    def copy(self) -> "TwoFactorRepresentation":
+        return TwoFactorRepresentation(self.U.copy(), self.Z.copy())
 
 
 class ZeroOperator:
@@ -137,6 +161,21 @@ class MatrixDataProblem:
             tspan = (1, len(y))
         self.tspan = tspan
         self.f = None
+
+
+class MatrixHybridProblem:
+    """Data-informed basis (src/primitives.jl:32-41): y(t) ~ U(t) Z(t)^T with
+    the coefficients following dZ/dt = f(Z, U, t) and U refitted to the data.
+    ``y`` is a callable t -> snapshot or a list of snapshots, ``u0`` a
+    TwoFactorRepresentation.  On the GPU ``f`` is one of the engine's flow
+    maps F, meaning f(Z, U, t) = F(U Z^T, t)^T U (the form the reference's
+    test uses, test/data_informed_approximation.jl:73)."""
+
+    def __init__(self, y, f, u0: "TwoFactorRepresentation", tspan):
+        self.y = y
+        self.f = f
+        self.u0 = u0
+        self.tspan = tspan
 
 
 @dataclass
@@ -244,9 +283,27 @@ class ProjectorSplitting:
         self.S_alg = self.S_alg or self.K_alg
 
 
-def _alg_desc(alg) -> _native.lri_alg_desc:
+@dataclass
+class GreedyIntegrator:
+    """Greedy basis fitting (src/integrators/greedy_integrator.jl:17-24):
+    every step refits the factors to the snapshot y(t + dt); Z_alg integrates
+    the coefficients of a MatrixHybridProblem.  Fixed rank."""
+    Z_alg: SubstepScheme = field(default_factory=RK4)
+
+    @property
+    def K_alg(self):
+        return self.Z_alg
+
+    L_alg = K_alg
+    S_alg = K_alg
+
+
+def _alg_desc(alg, two_factor: bool = False) -> _native.lri_alg_desc:
     d = _native.lri_alg_desc()
-    if isinstance(alg, UnconventionalAlgorithm):
+    if isinstance(alg, GreedyIntegrator):
+        d.kind = _native.LRI_ALG_GREEDY
+        d.two_factor = int(bool(two_factor))
+    elif isinstance(alg, UnconventionalAlgorithm):
         d.kind = _native.LRI_ALG_BUG
     elif isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
         d.kind = _native.LRI_ALG_RA_BUG
@@ -292,7 +349,7 @@ class Batch:
 
     def __init__(self, n: Sequence[int], m: Sequence[int], r: Sequence[int], alg, op_kind: int,
                  precision: str = "fp64", r_cap: Optional[Sequence[int]] = None,
-                 op_params: Optional[Tuple[float, float, float]] = None):
+                 op_params: Optional[Tuple[float, float, float]] = None, two_factor: bool = False):
         torch = _torch()
         self.torch = torch
         self.lib = _native.load()
@@ -322,7 +379,8 @@ class Batch:
         desc.r_cap = self.rcap.ctypes.data_as(I64P)
         if op_params is not None:  # Burgers (h, alpha, beta), shared by the batch
             desc.burgers_h, desc.burgers_alpha, desc.burgers_beta = (float(x) for x in op_params)
-        self._algd = _alg_desc(alg)
+        self._algd = _alg_desc(alg, two_factor)
+        self.two_factor = bool(two_factor)
         self.handle = C.c_void_p()
         _native.check(self.lib.lri_batch_create(C.byref(self.handle), C.byref(desc), C.byref(self._algd)),
                       "lri_batch_create")
@@ -343,7 +401,8 @@ class Batch:
         self.U, self.S, self.V = mk(tot[0]), mk(tot[1]), mk(tot[2])
         self.opA, self.opB = mk(tot[3]), mk(tot[4])
         self.offY = None
-        if op_kind == _native.LRI_OP_DATA:
+        self.has_data = op_kind == _native.LRI_OP_DATA or isinstance(alg, GreedyIntegrator)
+        if self.has_data:
             self.offY = np.zeros(cnt, np.int64)
             totY = np.zeros(1, np.int64)
             _native.check(self.lib.lri_batch_data_layout(self.handle, self.offY.ctypes.data_as(I64P),
@@ -437,7 +496,7 @@ class Batch:
     def step(self, t: float, dt: float, nsteps: int = 1, next_snapshots=None):
         """step!(integrator, alg, dt), ``nsteps`` times (asynchronous)."""
         yptr = None
-        if self.op_kind == _native.LRI_OP_DATA:
+        if self.has_data:
             if next_snapshots is None:
                 raise ValueError("data problems need the next snapshot")
             if isinstance(next_snapshots, np.ndarray) and next_snapshots.ndim == 1:
@@ -450,7 +509,7 @@ class Batch:
 
     def prepare(self, dt: float, nsteps: int):
         """Builds the CUDA graph of an nsteps-step call ahead of time."""
-        if nsteps > 1 and self.op_kind != _native.LRI_OP_DATA:
+        if nsteps > 1 and not self.has_data:
             _native.check(self.lib.lri_batch_prepare(self.handle, float(dt), int(nsteps)), "lri_batch_prepare")
 
     def launches_per_step(self) -> int:
@@ -474,9 +533,13 @@ class Batch:
 
     def download(self) -> List[SVDLikeRepresentation]:
         ranks = self.ranks()
-        hU = self.U.cpu().numpy().astype(np.float64)
-        hS = self.S.cpu().numpy().astype(np.float64)
-        hV = self.V.cpu().numpy().astype(np.float64)
+        return self.unpack(self.U.cpu().numpy(), self.S.cpu().numpy(), self.V.cpu().numpy(), ranks)
+
+    def unpack(self, hU, hS, hV, ranks) -> List[SVDLikeRepresentation]:
+        """Per-instance factors from host copies of the packed buffers."""
+        hU = np.asarray(hU).astype(np.float64)
+        hS = np.asarray(hS).astype(np.float64)
+        hV = np.asarray(hV).astype(np.float64)
         out = []
         for i in range(self.count):
             n, m, rc, r = int(self.n[i]), int(self.m[i]), int(self.rcap[i]), int(ranks[i])
@@ -485,6 +548,59 @@ class Batch:
             V = hV[self.offV[i]:self.offV[i] + m * rc].reshape((m, rc), order="F")[:, :r].copy()
             out.append(SVDLikeRepresentation(U, S, V))
         return out
+
+
+class History:
+    """The solution history of a batch (lri_history_*): every record is a
+    device copy of the factors into a ring slot and an asynchronous copy of
+    the slot to page-locked host memory, so the steps do not wait for the
+    transfers (the reference deep-copies after every step, update_sol!,
+    src/primitives.jl:82-90)."""
+
+    def __init__(self, batch: Batch, slots: int = 8):
+        self.b = batch
+        self.lib = batch.lib
+        self.torch = batch.torch
+        self.handle = C.c_void_p()
+        _native.check(self.lib.lri_history_create(C.byref(self.handle), batch.handle, int(slots)),
+                      "lri_history_create")
+        self.pending = []
+
+    def record(self) -> int:
+        """Queues a copy of the batch's current factors; returns its number."""
+        t, b = self.torch, self.b
+        pin = lambda k, dt: t.empty(max(int(k), 1), dtype=dt, pin_memory=True)
+        hU, hS, hV = pin(b.U.numel(), b.dtype), pin(b.S.numel(), b.dtype), pin(b.V.numel(), b.dtype)
+        hR = pin(b.count, t.int32)
+        seq = C.c_int64(0)
+        ptr = lambda x: C.c_void_p(x.data_ptr())
+        _native.check(self.lib.lri_history_record(self.handle, ptr(hU), ptr(hS), ptr(hV),
+                                                  C.cast(hR.data_ptr(), C.POINTER(C.c_int32)), b._stream(),
+                                                  C.byref(seq)), "lri_history_record")
+        self.pending.append((seq.value, hU, hS, hV, hR))
+        return seq.value
+
+    def collect(self) -> List[List[SVDLikeRepresentation]]:
+        """Waits for every queued record; their per-instance factors, in order."""
+        out = []
+        for seq, hU, hS, hV, hR in self.pending:
+            _native.check(self.lib.lri_history_wait(self.handle, seq), "lri_history_wait")
+            n = self.b
+            out.append(n.unpack(hU.numpy()[:n.U.numel()], hS.numpy()[:n.S.numel()], hV.numpy()[:n.V.numel()],
+                                hR.numpy()[:n.count]))
+        self.pending = []
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.lri_history_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------
@@ -540,9 +656,14 @@ def _op_kind(prob) -> int:
     raise LriError(2, "flow map is not one of the engine's operators (arbitrary closures are unsupported)")
 
 
+def _has_data(prob) -> bool:
+    return isinstance(prob, (MatrixDataProblem, MatrixHybridProblem))
+
+
 def _op_params(probs):
     """Batch-wide Burgers parameters (h, alpha, beta), or None."""
-    fs = [p.f for p in probs if isinstance(p, MatrixDEProblem) and isinstance(p.f, BurgersOperator)]
+    fs = [p.f for p in probs if isinstance(p, (MatrixDEProblem, MatrixHybridProblem))
+          and isinstance(p.f, BurgersOperator)]
     if not fs:
         return None
     ps = {f.params() for f in fs}
@@ -561,29 +682,43 @@ def _data_at(prob: MatrixDataProblem, t):
 
 
 def init(prob, alg, dt, precision: str = "fp64") -> DLRIntegrator:
+    """init(prob, alg, dt) (unconventional.jl:109-119, greedy_integrator.jl:54-71)."""
     t0, tf = prob.tspan
     if not tf > t0:
         raise AssertionError("Integration in reverse time direction is not supported")
     u0 = prob.u0
-    n, m = u0.U.shape[0], u0.V.shape[0]
-    r = u0.S.shape[0]
+    two = isinstance(u0, TwoFactorRepresentation)
+    if two and not isinstance(alg, GreedyIntegrator):
+        raise TypeError("two-factor (U Z^T) representations are integrated by the GreedyIntegrator")
+    if isinstance(prob, MatrixHybridProblem) and not (two and isinstance(alg, GreedyIntegrator)):
+        raise TypeError("a MatrixHybridProblem takes a TwoFactorRepresentation and the GreedyIntegrator")
+    n = u0.U.shape[0]
+    m = (u0.Z if two else u0.V).shape[0]
+    r = u0.rank
     rcap = r
     if isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
         rcap = max(r, min(alg.rmax, n // 2, m // 2))
-    b = Batch([n], [m], [r], alg, _op_kind(prob), precision, r_cap=[rcap], op_params=_op_params([prob]))
-    b.upload([u0], [prob.f] if isinstance(prob, MatrixDEProblem) else None)
-    if isinstance(prob, MatrixDataProblem):
+    packed = SVDLikeRepresentation(u0.U, np.eye(r), u0.Z) if two else u0
+    b = Batch([n], [m], [r], alg, _op_kind(prob), precision, r_cap=[rcap], op_params=_op_params([prob]),
+              two_factor=two)
+    b.upload([packed], [prob.f] if isinstance(prob, (MatrixDEProblem, MatrixHybridProblem)) else None)
+    if isinstance(prob, MatrixDataProblem) and not isinstance(alg, GreedyIntegrator):
         b.data_init([_data_at(prob, t0)])
     sol = _init_sol(dt, t0, tf, u0)
     sol.Y[0] = u0.copy()
     return DLRIntegrator(u0.copy(), t0, dt, sol, alg, b, prob, 0)
 
 
+def _download_one(b: "Batch"):
+    Y = b.download()[0]
+    return TwoFactorRepresentation(Y.U, Y.V) if b.two_factor else Y
+
+
 def step(integ: DLRIntegrator, alg=None, dt=None, sync_factors: bool = True) -> None:
     """step!(integrator, alg, dt): one step on the device."""
     dt = integ.dt if dt is None else dt
     b = integ.batch
-    if isinstance(integ.prob, MatrixDataProblem):
+    if _has_data(integ.prob):
         b.step(integ.t, dt, 1, [_data_at(integ.prob, integ.t + dt)])
     else:
         b.step(integ.t, dt, 1)
@@ -591,7 +726,7 @@ def step(integ: DLRIntegrator, alg=None, dt=None, sync_factors: bool = True) -> 
     integ.iter += 1
     if sync_factors:
         b.check_status()
-        integ.u = b.download()[0]
+        integ.u = _download_one(b)
 
 
 def _update_sol(integ: DLRIntegrator) -> None:
@@ -614,25 +749,41 @@ def solve(prob, alg, dt=None, precision: str = "fp64", save_everystep: bool = Tr
         dt = 1
     integ = init(prob, alg, dt, precision)
     T = prob.tspan[1] - prob.tspan[0]
-    if not save_everystep and not isinstance(prob, MatrixDataProblem):
+    if not save_everystep and not _has_data(prob):
         k = n_steps(prob.tspan, dt)
         integ.batch.step(integ.t, dt, k)
         for _ in range(k):
             integ.t += dt
         integ.iter = k
         integ.batch.check_status()
-        integ.u = integ.batch.download()[0]
+        integ.u = _download_one(integ.batch)
         integ.sol.Y = [integ.sol.Y[0], integ.u.copy()]
         integ.sol.t = [integ.sol.t[0], integ.t]
         integ.batch.close()
         return integ.sol
-    while (prob.tspan[1] - integ.t) / T > 1e-8:
-        step(integ, alg, dt, sync_factors=save_everystep)
-        if save_everystep:
-            _update_sol(integ)
+    if save_everystep:
+        # the history copies overlap the next steps; unpacked once at the end
+        hist = History(integ.batch)
+        times = []
+        try:
+            while (prob.tspan[1] - integ.t) / T > 1e-8:
+                step(integ, alg, dt, sync_factors=False)
+                hist.record()
+                times.append(integ.t)
+            integ.batch.check_status()
+            for k, (Y, tk) in enumerate(zip(hist.collect(), times)):
+                Y = Y[0]
+                integ.u = TwoFactorRepresentation(Y.U, Y.V) if integ.batch.two_factor else Y
+                integ.iter, integ.t = k + 1, tk
+                _update_sol(integ)
+        finally:
+            hist.close()
+    else:
+        while (prob.tspan[1] - integ.t) / T > 1e-8:
+            step(integ, alg, dt, sync_factors=False)
     if not save_everystep:
         integ.batch.check_status()
-        integ.u = integ.batch.download()[0]
+        integ.u = _download_one(integ.batch)
         integ.sol.Y = [integ.sol.Y[0], integ.u.copy()]
         integ.sol.t = [integ.sol.t[0], integ.t]
     integ.batch.close()

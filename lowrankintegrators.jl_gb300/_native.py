@@ -20,7 +20,7 @@ STATUS_NAMES = {
 }
 
 LRI_F64, LRI_F32, LRI_DF = 0, 1, 2
-LRI_ALG_BUG, LRI_ALG_RA_BUG, LRI_ALG_KSL = 0, 1, 2
+LRI_ALG_BUG, LRI_ALG_RA_BUG, LRI_ALG_KSL, LRI_ALG_GREEDY = 0, 1, 2, 3
 LRI_KSL_PRIMAL, LRI_KSL_DUAL, LRI_KSL_STRANG = 0, 1, 2
 LRI_OP_ZERO, LRI_OP_SYLVESTER_TRIDIAG, LRI_OP_BURGERS_PERIODIC, LRI_OP_DATA = 0, 1, 2, 3
 
@@ -33,6 +33,7 @@ EXPORTED = [
     "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
     "lri_stream_status", "lri_stream_set_tensor_cores", "lri_stream_uses_tensor_cores", "lri_stream_data_product",
     "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
+    "lri_history_create", "lri_history_destroy", "lri_history_record", "lri_history_wait",
 ]
 
 
@@ -50,7 +51,7 @@ class lri_scheme(C.Structure):
 class lri_alg_desc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("ksl_order", C.c_int32), ("K_alg", lri_scheme),
                 ("L_alg", lri_scheme), ("S_alg", lri_scheme), ("tol", C.c_double),
-                ("r_min", C.c_int32), ("reserved", C.c_int32)]
+                ("r_min", C.c_int32), ("two_factor", C.c_int32)]
 
 
 class lri_batch_desc(C.Structure):
@@ -110,6 +111,14 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_stream_uses_tensor_cores.argtypes = [P, C.POINTER(C.c_int32)]
     lib.lri_stream_data_product.restype = C.c_int
     lib.lri_stream_data_product.argtypes = [P, C.c_int32, P, P, P, C.c_int64, C.c_int64, P, C.c_int64, P]
+    lib.lri_history_create.restype = C.c_int
+    lib.lri_history_create.argtypes = [C.POINTER(P), P, C.c_int32]
+    lib.lri_history_destroy.restype = C.c_int
+    lib.lri_history_destroy.argtypes = [P]
+    lib.lri_history_record.restype = C.c_int
+    lib.lri_history_record.argtypes = [P, P, P, P, C.POINTER(C.c_int32), P, C.POINTER(C.c_int64)]
+    lib.lri_history_wait.restype = C.c_int
+    lib.lri_history_wait.argtypes = [P, C.c_int64]
     lib.lri_burgers_create.restype = C.c_int
     lib.lri_burgers_create.argtypes = [C.POINTER(P), C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                        C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double, P]

@@ -117,6 +117,7 @@ StepArgs<T> make_args(const lri_batch* b, double t, double dt, const void* Ynext
   g.ksl_order = b->alg.ksl_order;
   g.op = b->desc.op;
   g.r_min = b->alg.r_min;
+  g.two_factor = b->alg.two_factor;
   g.tol = b->alg.tol;
   g.sK = to_scheme(b->alg.K_alg);
   g.sL = to_scheme(b->alg.L_alg);
@@ -193,7 +194,12 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   if (desc->count < 1 || !desc->n || !desc->m || !desc->r) return LRI_ERR_ARG;
   if (desc->dtype != LRI_F32 && desc->dtype != LRI_F64 && desc->dtype != LRI_DF) return LRI_ERR_ARG;
   if (desc->op < LRI_OP_ZERO || desc->op > LRI_OP_DATA) return LRI_ERR_ARG;
-  if (alg->kind < LRI_ALG_BUG || alg->kind > LRI_ALG_KSL) return LRI_ERR_ARG;
+  if (alg->kind < LRI_ALG_BUG || alg->kind > LRI_ALG_GREEDY) return LRI_ERR_ARG;
+  if (alg->kind == LRI_ALG_GREEDY) {
+    if (alg->two_factor != 0 && alg->two_factor != 1) return LRI_ERR_ARG;
+    // SVD-like greedy fitting needs data; two factors take data or a flow (hybrid)
+    if (!alg->two_factor && desc->op != LRI_OP_DATA) return LRI_ERR_UNSUPPORTED;
+  }
   if (alg->kind == LRI_ALG_KSL && (alg->ksl_order < 0 || alg->ksl_order > 2)) return LRI_ERR_ARG;
   if (!scheme_ok(alg->K_alg) || !scheme_ok(alg->L_alg) || !scheme_ok(alg->S_alg)) return LRI_ERR_ARG;
   if (alg->kind == LRI_ALG_RA_BUG && (!(alg->tol >= 0.0) || alg->r_min < 1)) return LRI_ERR_ARG;
@@ -224,7 +230,7 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
     const int64_t w = ra ? 2 * rc : rc;
     bool ok = n >= 1 && m >= 1 && r >= 1 && rc >= r && n < (1LL << 30) && m < (1LL << 30);
     ok = ok && w <= 64 && w <= n && w <= m;
-    if (desc->op == LRI_OP_DATA) ok = ok && (n * m) < (1LL << 40);
+    if (desc->op == LRI_OP_DATA || alg->kind == LRI_ALG_GREEDY) ok = ok && (n * m) < (1LL << 40);
     if (!ok) {
       delete b;
       return (w > 64 && n >= w && m >= w && r >= 1 && rc >= r) ? LRI_ERR_UNSUPPORTED : LRI_ERR_ARG;
@@ -266,7 +272,7 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
     d.offSmall = b->totSmall;
     b->totSmall += lri::kSmallBlocks * al(w * w);  // blocks padded to 4 elements (see Inst::blk)
     d.offY = b->totY;
-    if (desc->op == LRI_OP_DATA) b->totY += n * m;
+    if (desc->op == LRI_OP_DATA || alg->kind == LRI_ALG_GREEDY) b->totY += n * m;
   }
   // longest-processing-time-first launch order: CTAs start in block order
   b->order.resize(count);
@@ -290,14 +296,14 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   alloc((void**)&b->d_status, sizeof(uint32_t));
   alloc(&b->d_work, b->esize * (size_t)b->totWork);
   alloc(&b->d_small, b->esize * (size_t)b->totSmall);
-  if (desc->op == LRI_OP_DATA) alloc(&b->d_Yprev, b->esize * (size_t)b->totY);
+  if (desc->op == LRI_OP_DATA && alg->kind != LRI_ALG_GREEDY) alloc(&b->d_Yprev, b->esize * (size_t)b->totY);
   if (desc->dtype == LRI_DF) {
     alloc(&b->iU, 8 * (size_t)b->totU);
     alloc(&b->iS, 8 * (size_t)b->totS);
     alloc(&b->iV, 8 * (size_t)b->totV);
     alloc(&b->iA, 8 * (size_t)b->totA);
     alloc(&b->iB, 8 * (size_t)b->totB);
-    if (desc->op == LRI_OP_DATA) alloc(&b->iYn, 8 * (size_t)b->totY);
+    if (b->totY > 0) alloc(&b->iYn, 8 * (size_t)b->totY);
   }
   if (e == cudaSuccess) e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_order, b->order.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice);
@@ -403,6 +409,10 @@ lri_status lri_batch_bind(lri_batch* b, void* U, void* S, void* V, const void* o
 lri_status lri_batch_data_init(lri_batch* b, const void* Y0, void* stream) {
   if (!b || !Y0) return LRI_ERR_ARG;
   if (b->desc.op != LRI_OP_DATA) return LRI_ERR_STATE;
+  if (b->alg.kind == LRI_ALG_GREEDY) {  // the greedy steps read y(t + dt) only
+    b->data_ready = true;
+    return LRI_OK;
+  }
   if (b->desc.dtype == LRI_DF) {
     LRI_CUDA(lri::convert_f64_to_df(static_cast<const double*>(Y0), b->d_Yprev, b->totY, (cudaStream_t)stream));
   } else {
@@ -418,8 +428,9 @@ lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, con
   if (!b->bound) return LRI_ERR_STATE;
   if (nsteps == 0) return LRI_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (b->desc.op == LRI_OP_DATA) {
-    if (!b->data_ready) return LRI_ERR_STATE;
+  const bool greedy = b->alg.kind == LRI_ALG_GREEDY;
+  if (b->desc.op == LRI_OP_DATA || greedy) {
+    if (!b->data_ready && !greedy) return LRI_ERR_STATE;
     if (!Ynext || nsteps != 1) return LRI_ERR_ARG;
     cudaError_t e = launch_one(b, t, dt, Ynext, st);
     if (e == cudaSuccess) e = writeback(b, st);
@@ -439,7 +450,7 @@ lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nsteps, con
 lri_status lri_batch_prepare(lri_batch* b, double dt, int32_t nsteps) {
   if (!b || nsteps < 2 || !std::isfinite(dt)) return LRI_ERR_ARG;
   if (!b->bound) return LRI_ERR_STATE;
-  if (b->desc.op == LRI_OP_DATA) return LRI_ERR_UNSUPPORTED;
+  if (b->desc.op == LRI_OP_DATA || b->alg.kind == LRI_ALG_GREEDY) return LRI_ERR_UNSUPPORTED;
   // The engine's operators are autonomous, so a captured graph depends on
   // (nsteps, dt) only and is reused across calls.
   if (b->gexec && b->g_steps == nsteps && b->g_dt == dt) return LRI_OK;
@@ -494,7 +505,7 @@ int32_t lri_batch_launches_per_step(const lri_batch* b) {
   if (!b) return 0;
   // one engine launch; double-float batches add the three write-back
   // conversions (and one snapshot conversion for data problems) per call
-  if (b->desc.dtype == LRI_DF) return 4 + (b->desc.op == LRI_OP_DATA ? 1 : 0);
+  if (b->desc.dtype == LRI_DF) return 4 + (b->totY > 0 ? 1 : 0);
   return 1;
 }
 
@@ -562,3 +573,108 @@ lri_status lri_batch_adjoint_step(lri_batch* b, double dt, const void* U0, const
       static_cast<const double*>(b->opB), b->d_adj_work, to_scheme(b->alg.K_alg), to_scheme(b->alg.L_alg),
       to_scheme(b->alg.S_alg), dt, (cudaStream_t)stream));
 }
+
+// ---------------------------------------------------------------------------
+// Solution history: the reference deep-copies the factors into its solution
+// after every step (update_sol!, src/primitives.jl:82-90).  Here every
+// record is a device-to-device copy into a ring slot on the caller's stream
+// and a copy of that slot to host memory on the history's own stream, so the
+// steps never wait for PCIe/NVLink-C2C transfers.
+// ---------------------------------------------------------------------------
+struct lri_history {
+  lri_batch* b = nullptr;
+  int slots = 0;
+  size_t bytesU = 0, bytesS = 0, bytesV = 0, bytesR = 0;
+  std::vector<void*> d;               // per slot: U | S | V | ranks (one allocation)
+  std::vector<cudaEvent_t> ready;     // the slot's device copy is done
+  std::vector<cudaEvent_t> done;      // the slot's host copy is done
+  std::vector<int64_t> slot_seq;
+  cudaStream_t copy = nullptr;
+  int64_t next = 0;
+};
+
+extern "C" {
+
+lri_status lri_history_destroy(lri_history* h) {
+  if (!h) return LRI_ERR_ARG;
+  if (h->copy) cudaStreamSynchronize(h->copy);
+  for (void* p : h->d) cudaFree(p);
+  for (cudaEvent_t e : h->ready) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->done) if (e) cudaEventDestroy(e);
+  if (h->copy) cudaStreamDestroy(h->copy);
+  delete h;
+  return LRI_OK;
+}
+
+lri_status lri_history_create(lri_history** out, lri_batch* b, int32_t slots) {
+  if (!out || !b || slots < 1 || slots > 1024) return LRI_ERR_ARG;
+  *out = nullptr;
+  lri_history* h = new lri_history();
+  h->b = b;
+  h->slots = slots;
+  const size_t es = b->desc.dtype == LRI_F32 ? 4 : 8;  // double-float batches expose FP64 factors
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  h->bytesU = es * (size_t)b->totU;
+  h->bytesS = es * (size_t)b->totS;
+  h->bytesV = es * (size_t)b->totV;
+  h->bytesR = sizeof(int32_t) * (size_t)b->desc.count;
+  const size_t per = al(h->bytesU) + al(h->bytesS) + al(h->bytesV) + al(h->bytesR);
+  h->d.assign(slots, nullptr);
+  h->ready.assign(slots, nullptr);
+  h->done.assign(slots, nullptr);
+  h->slot_seq.assign(slots, -1);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking);
+  for (int i = 0; i < slots && e == cudaSuccess; ++i) {
+    e = cudaMalloc(&h->d[i], per);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ready[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done[i], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    lri_history_destroy(h);
+    return LRI_ERR_CUDA;
+  }
+  *out = h;
+  return LRI_OK;
+}
+
+lri_status lri_history_record(lri_history* h, void* hostU, void* hostS, void* hostV, int32_t* host_ranks, void* stream,
+                              int64_t* seq) {
+  if (!h || !hostU || !hostS || !hostV) return LRI_ERR_ARG;
+  lri_batch* b = h->b;
+  if (!b->bound) return LRI_ERR_STATE;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int slot = (int)(h->next % h->slots);
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  unsigned char* base = static_cast<unsigned char*>(h->d[slot]);
+  unsigned char* sU = base;
+  unsigned char* sS = sU + al(h->bytesU);
+  unsigned char* sV = sS + al(h->bytesS);
+  unsigned char* sR = sV + al(h->bytesV);
+  // the slot's previous host copy must have finished before it is overwritten
+  if (h->slot_seq[slot] >= 0) LRI_CUDA(cudaStreamWaitEvent(st, h->done[slot], 0));
+  LRI_CUDA(cudaMemcpyAsync(sU, b->U, h->bytesU, cudaMemcpyDeviceToDevice, st));
+  LRI_CUDA(cudaMemcpyAsync(sS, b->S, h->bytesS, cudaMemcpyDeviceToDevice, st));
+  LRI_CUDA(cudaMemcpyAsync(sV, b->V, h->bytesV, cudaMemcpyDeviceToDevice, st));
+  LRI_CUDA(cudaMemcpyAsync(sR, b->d_rank, h->bytesR, cudaMemcpyDeviceToDevice, st));
+  LRI_CUDA(cudaEventRecord(h->ready[slot], st));
+  LRI_CUDA(cudaStreamWaitEvent(h->copy, h->ready[slot], 0));
+  LRI_CUDA(cudaMemcpyAsync(hostU, sU, h->bytesU, cudaMemcpyDeviceToHost, h->copy));
+  LRI_CUDA(cudaMemcpyAsync(hostS, sS, h->bytesS, cudaMemcpyDeviceToHost, h->copy));
+  LRI_CUDA(cudaMemcpyAsync(hostV, sV, h->bytesV, cudaMemcpyDeviceToHost, h->copy));
+  if (host_ranks) LRI_CUDA(cudaMemcpyAsync(host_ranks, sR, h->bytesR, cudaMemcpyDeviceToHost, h->copy));
+  LRI_CUDA(cudaEventRecord(h->done[slot], h->copy));
+  h->slot_seq[slot] = h->next;
+  if (seq) *seq = h->next;
+  ++h->next;
+  return LRI_OK;
+}
+
+lri_status lri_history_wait(lri_history* h, int64_t seq) {
+  if (!h || seq < 0 || seq >= h->next) return LRI_ERR_ARG;
+  // a later record of the same slot completes after this one (one copy stream)
+  const int slot = (int)(seq % h->slots);
+  LRI_CUDA(cudaEventSynchronize(h->done[slot]));
+  return LRI_OK;
+}
+
+}  // extern "C"

@@ -334,7 +334,7 @@ struct LoadDelta {
       if (ii < rows) {
         const int64_t idx = trans ? (int64_t)(k0 + kk) + (int64_t)(i0 + ii) * n
                                   : (int64_t)(i0 + ii) + (int64_t)(k0 + kk) * n;
-        v = Yn[idx] - Yp[idx];
+        v = Yp ? Yn[idx] - Yp[idx] : Yn[idx];  // no previous snapshot: Yn itself
       }
       xs[kk * TR + ii] = v;
     }

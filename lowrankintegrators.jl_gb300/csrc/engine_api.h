@@ -20,7 +20,7 @@ using lri_df::dfloat;
 // the double-float copies of M, N, P_U, P_V of the FP32 class.
 constexpr int kSmallBlocks = 23;
 
-enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2 };
+enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2, ALG_GREEDY = 3 };
 enum KslOrder : int32_t { KSL_PRIMAL = 0, KSL_DUAL = 1, KSL_STRANG = 2 };
 enum OpKind : int32_t { OP_ZERO = 0, OP_SYLVESTER = 1, OP_BURGERS = 2, OP_DATA = 3 };
 
@@ -66,6 +66,7 @@ struct StepArgs {
   const T* Ynext;
   double t, dt;
   int32_t alg, ksl_order, op, r_min;
+  int32_t two_factor;  // greedy: factors U Z^T (Z in V) instead of U S V^T
   double tol;
   Scheme sK, sL, sS;
   double bh, balpha, bbeta;

@@ -8,6 +8,7 @@
 //   ksl_primal    src/integrators/projector_splitting.jl:129-152
 //   ksl_dual      src/integrators/projector_splitting.jl:166-189
 //   Strang        src/integrators/projector_splitting.jl:205-211
+//   greedy_step   src/integrators/greedy_integrator.jl:73-104
 //   data substeps src/integrators/data_integrator.jl:13-16 (u += sign*left'*Δy*right)
 //   K/L/S rhs     src/integrators/unconventional.jl:52-54,62-64,72-74
 #pragma once
@@ -451,6 +452,15 @@ __device__ void check_finite(const StepArgs<T>& g, const T* S, int r, int ld) {
   __syncthreads();
 }
 
+// non-finite entries of an N x r panel (ld N) -> status
+template <typename T>
+__device__ void check_finite_panel(const StepArgs<T>& g, const T* X, int N, int r) {
+  const int64_t len = (int64_t)N * r;
+  bool bad = false;
+  for (int64_t o = threadIdx.x; o < len; o += NT) bad |= !is_finite_val(X[o]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(g.status, ST_NONFINITE);
+}
+
 // S-step of the FP32 class in double-float (Sylvester flow, orthonormal
 // bases): S0 = M S N^T from the FP32 core and the double-float basis
 // changes, then the substeps of S' = P_U S + S P_V^T in Horner form (the
@@ -772,6 +782,84 @@ __device__ __noinline__ void ksl_dual(const StepArgs<T>& g, Inst<T>& I, int r, d
 }
 
 // ---------------------------------------------------------------------------
+// Greedy basis fitting (GreedyIntegrator, src/integrators/greedy_integrator.jl)
+// ---------------------------------------------------------------------------
+// dst (N x r) = the orthonormal polar factor of X (N x r, ld N): the Q P^T of
+// svd(X) = Q Sigma P^T (greedy_integrator.jl:80-81,92-93), formed as
+// X = Q_X R (QR), R = A Sigma B^T (one-sided Jacobi), dst = Q_X (A B^T).
+// A rank-deficient X keeps directions completed by complete_left.  Uses the
+// side's QR panel and the small blocks B_RK, B_T2; X may be sd.PY.
+template <typename T>
+__device__ void polar_panel(const StepArgs<T>& g, const Inst<T>& I, const Side<T>& sd, T* X, int N, int r, T* dst,
+                            Smem<T>& sm) {
+  const int W = I.W;
+  T* R = I.blk(B_RK);
+  T* C = I.blk(B_T2);
+  orth_panel<T>(I, X, N, r, sd.PQ, R, W, sm);
+  T* a = sm.stage;
+  T* v = sm.stage + r * r;
+  int* perm = reinterpret_cast<int*>(sm.stage + 2 * r * r);
+  int* flag = perm + r + 1;
+  T* sigma = sm.vec;
+  for (int o = threadIdx.x; o < r * r; o += NT) a[o] = R[(o % r) + (int64_t)(o / r) * W];
+  __syncthreads();
+  const bool ok = jacobi_svd<T>(r, a, v, sigma, perm, flag);
+  if (threadIdx.x == 0 && !ok) atomicOr(g.status, ST_SVD_NOCONV);
+  complete_left<T>(r, r, a, sigma, perm, R);  // R is free once copied
+  // C = A B^T (the polar factor of R)
+  for (int o = threadIdx.x; o < r * r; o += NT) {
+    const int i = o % r, j = o / r;
+    T acc = T(0);
+    for (int k = 0; k < r; ++k) acc = fma_acc(a[i + perm[k] * r], v[j + perm[k] * r], acc);
+    C[i + (int64_t)j * W] = renorm(acc);
+  }
+  __syncthreads();
+  tile_gemm<T>(N, r, r, sm.stage, LoadPanel<T>{sd.PQ, N}, LoadSmall<T>{C, W, false}, EpiStore<T>{dst, N});
+}
+
+// One greedy step with the snapshot X = y(t + dt) (update_data!,
+// data_integrator.jl:22-28):
+//   SVD-like factors (greedy_integrator.jl:96-104): U = Q of qr(X V),
+//     V = Q of qr(X^T U), S = U^T X V with the new U, V;
+//   two factors u = U Z^T, Z kept in the V buffer (S unused):
+//     data problem (:84-94): Z = X^T U, U = polar(X Z);
+//     hybrid problem (:73-82): Z advanced over [t, t + dt] by the flow's
+//     L substep, Z' = F(U Z^T)^T U with U fixed (the reference's coefficient
+//     ODE f(Z, U, t) for a flow map F), then U = polar(X Z).
+template <typename T>
+__device__ __noinline__ void greedy_step(const StepArgs<T>& g, Inst<T>& I, int r, Smem<T>& sm) {
+  const int n = I.n, m = I.m, W = I.W;
+  const LoadDelta<T> Xn{I.Yn, nullptr, n, false};
+  const LoadDelta<T> Xt{I.Yn, nullptr, n, true};
+  if (!g.two_factor) {
+    tile_gemm<T>(n, m, r, sm.stage, Xn, LoadSmall<T>{I.V, m, false}, EpiStore<T>{I.k.PY, n});  // X V
+    tile_gemm<T>(m, n, r, sm.stage, Xt, LoadSmall<T>{I.U, n, false}, EpiStore<T>{I.l.PY, m});  // X^T U
+    orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
+    orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
+    copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
+    copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
+    tile_gemm<T>(n, m, r, sm.stage, Xn, LoadSmall<T>{I.V, m, false}, EpiStore<T>{I.k.PY, n});  // X V (new V)
+    T* St = I.blk(B_ST);
+    tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.U, n, r}, RowLoadPanel<T>{I.k.PY, n, r}, St, W, T(1), T(0));
+    copy_mat<T>(r, r, St, W, I.S, I.rcap);
+    check_finite<T>(g, I.S, r, I.rcap);
+    return;
+  }
+  T* Z = I.V;
+  if (g.op == OP_DATA) {
+    tile_gemm<T>(m, n, r, sm.stage, Xt, LoadSmall<T>{I.U, n, false}, EpiStore<T>{Z, m});  // Z = X^T U
+  } else {
+    T* GU = I.blk(B_GU);
+    if (g.op == OP_SYLVESTER) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    substep_side<T>(g, I, I.l, 1, Z, r, GU, I.U, g.sL, g.dt, sm);
+  }
+  tile_gemm<T>(n, m, r, sm.stage, Xn, LoadSmall<T>{Z, m, false}, EpiStore<T>{I.k.PY, n});  // X Z
+  polar_panel<T>(g, I, I.k, I.k.PY, n, r, I.U, sm);
+  check_finite_panel<T>(g, I.U, n, r);
+  check_finite_panel<T>(g, Z, m, r);
+}
+
+// ---------------------------------------------------------------------------
 // The step kernel
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -793,9 +881,11 @@ __global__ void __launch_bounds__(NT, 3) step_kernel(StepArgs<T> g) {
   I.l = Side<T>{d.m, I.V, g.opB ? g.opB + d.offB : nullptr, wl, wl + (int64_t)d.m * W,
                 wl + (int64_t)d.m * 2 * W, wl + (int64_t)d.m * (2 * W + rc), wl + (int64_t)d.m * (2 * W + 2 * rc)};
   I.small = g.small + d.offSmall;
-  I.Yp = (g.op == OP_DATA) ? g.Yprev + d.offY : nullptr;
-  I.Ypw = (g.op == OP_DATA) ? g.Yprev + d.offY : nullptr;
-  I.Yn = (g.op == OP_DATA) ? g.Ynext + d.offY : nullptr;
+  // data problems read A(t + dt) and A(t); the greedy steps read y(t + dt) only
+  const bool prev = (g.op == OP_DATA) && (g.alg != ALG_GREEDY);
+  I.Yp = prev ? g.Yprev + d.offY : nullptr;
+  I.Ypw = prev ? g.Yprev + d.offY : nullptr;
+  I.Yn = (g.op == OP_DATA || g.alg == ALG_GREEDY) ? g.Ynext + d.offY : nullptr;
   const int r = g.rank[inst];
   if (r < 1 || r > d.rcap || (g.alg == ALG_RA_BUG && (2 * r > d.wcap || 2 * r > d.n || 2 * r > d.m))) {
     if (threadIdx.x == 0) atomicOr(g.status, ST_BAD_SHAPE);
@@ -803,6 +893,8 @@ __global__ void __launch_bounds__(NT, 3) step_kernel(StepArgs<T> g) {
   }
   if (g.alg == ALG_BUG) {
     bug_step<T>(g, I, r, sm);
+  } else if (g.alg == ALG_GREEDY) {
+    greedy_step<T>(g, I, r, sm);
   } else if (g.alg == ALG_RA_BUG) {
     ra_bug_step<T>(g, I, r, sm);
   } else {
@@ -817,7 +909,7 @@ __global__ void __launch_bounds__(NT, 3) step_kernel(StepArgs<T> g) {
     check_finite<T>(g, I.S, r, I.rcap);
   }
   // data problems: yprev <- ycurr (unconventional.jl:125)
-  if (g.op == OP_DATA) {
+  if (prev) {
     const int64_t nm = (int64_t)d.n * d.m;
     for (int64_t o = threadIdx.x; o < nm; o += NT) I.Ypw[o] = I.Yn[o];
   }

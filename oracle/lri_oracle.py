@@ -41,7 +41,7 @@ import numpy as np
 
 __all__ = [
     "SVDLikeRepresentation", "TwoFactorRepresentation",
-    "MatrixDEProblem", "MatrixDataProblem",
+    "MatrixDEProblem", "MatrixDataProblem", "MatrixHybridProblem", "GreedyIntegrator",
     "DLRSolution", "DLRIntegrator",
     "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm",
     "ProjectorSplitting", "PrimalLieTrotter", "DualLieTrotter", "Strang",
@@ -88,6 +88,9 @@ class TwoFactorRepresentation:
 
     def full(self) -> np.ndarray:
         return self.U @ self.Z.T
+
+    def copy(self) -> "TwoFactorRepresentation":
+        return TwoFactorRepresentation(self.U.copy(), self.Z.copy())
 
 
 def to_dense(Y) -> np.ndarray:
@@ -149,6 +152,18 @@ class MatrixDataProblem:
             if callable(y):
                 raise ValueError("tspan is required for a data stream given as a function")
             tspan = (1, len(y))
+        self.tspan = tspan
+
+
+class MatrixHybridProblem:
+    """Data-informed basis: y(t) ~= U(t) Z(t)^T with dZ/dt = f(Z, U, t)
+    (src/primitives.jl:32-41).  ``y`` is a callable t -> snapshot, ``u0`` a
+    TwoFactorRepresentation."""
+
+    def __init__(self, y, f, u0: "TwoFactorRepresentation", tspan):
+        self.y = y
+        self.f = f
+        self.u0 = u0
         self.tspan = tspan
 
 
@@ -522,6 +537,13 @@ class ProjectorSplitting:
         self.S_alg = self.S_alg or self.K_alg
 
 
+@dataclass
+class GreedyIntegrator:
+    """Greedy basis fitting (src/integrators/greedy_integrator.jl:17-24);
+    Z_alg integrates the coefficient ODE of a MatrixHybridProblem."""
+    Z_alg: SubstepScheme = field(default_factory=RK4)
+
+
 # --------------------------------------------------------------------------
 # Data-stream bookkeeping (src/integrators/data_integrator.jl)
 # --------------------------------------------------------------------------
@@ -594,11 +616,66 @@ def init(prob, alg, dt) -> DLRIntegrator:
         raise AssertionError("Integration in reverse time direction is not supported")
     u = prob.u0.copy()
     sol = init_sol(dt, t0, tf, prob.u0)
-    cache = _Substeps(prob, alg)
-    if cache.is_data:
-        cache.data = _DataCache(prob, t0)
+    if isinstance(alg, GreedyIntegrator):
+        cache = _GreedyCache(prob)
+    else:
+        cache = _Substeps(prob, alg)
+        if cache.is_data:
+            cache.data = _DataCache(prob, t0)
     sol.Y[0] = prob.u0.copy()
     return DLRIntegrator(u, t0, dt, sol, alg, cache, prob, 0)
+
+
+class _GreedyCache:
+    """GreedyIntegrator_Cache (src/integrators/greedy_integrator.jl:1-52):
+    the data source and, for a hybrid problem, the coefficient integrator's
+    right-hand side f(Z, U, t) (its parameter is the integrator's U,
+    aliased, :41-47)."""
+
+    def __init__(self, prob):
+        self.prob = prob
+        self.hybrid = isinstance(prob, MatrixHybridProblem)
+
+    def snapshot(self, t, dt):
+        """update_data!(X, y, t, dt): X = y(t + dt) (data_integrator.jl:22-28;
+        snapshot lists are 1-indexed)."""
+        y = self.prob.y
+        if callable(y):
+            return np.array(y(t + dt), dtype=np.float64)
+        idx = int(round(t + dt))
+        if abs((t + dt) - idx) > 1e-12:
+            raise TypeError("discrete snapshot data needs an integer time step")
+        return np.array(y[idx - 1], dtype=np.float64)
+
+
+def _polar(A: np.ndarray) -> np.ndarray:
+    """Q P^T from svd(A) = Q Sigma P^T (greedy_integrator.jl:80-81,92-93)."""
+    Q, _, Pt = np.linalg.svd(A, full_matrices=False)
+    return Q @ Pt
+
+
+def greedy_step(u, cache: _GreedyCache, alg: GreedyIntegrator, t, dt) -> None:
+    """greedy_step! (src/integrators/greedy_integrator.jl:73-104)."""
+    if cache.hybrid:
+        # :73-82: advance Z over [t, t+dt] with U fixed, then U = polar(X Z)
+        U = u.U
+        f = cache.prob.f
+        u.Z = alg.Z_alg.integrate(lambda Z, tt: f(Z, U, tt), u.Z, t, dt)
+        X = cache.snapshot(t, dt)
+        u.U = _polar(X @ u.Z)
+    elif isinstance(u, TwoFactorRepresentation):
+        # :84-94
+        X = cache.snapshot(t, dt)
+        u.Z = X.T @ u.U
+        u.U = _polar(X @ u.Z)
+    else:
+        # :96-104
+        X = cache.snapshot(t, dt)
+        XV = X @ u.V
+        XU = X.T @ u.U
+        u.U, _ = _qr(XV)
+        u.V, _ = _qr(XU)
+        u.S = u.U.T @ (X @ u.V)
 
 
 def _advance_data(cache, t, dt):
@@ -690,7 +767,9 @@ def step(integ: DLRIntegrator, alg, dt) -> None:
     (unconventional.jl:159-164, rank_adaptive_unconventional.jl:171-180,
     projector_splitting.jl:191-211)."""
     u, t, cache = integ.u, integ.t, integ.cache
-    if isinstance(alg, UnconventionalAlgorithm):
+    if isinstance(alg, GreedyIntegrator):
+        greedy_step(u, cache, alg, t, dt)
+    elif isinstance(alg, UnconventionalAlgorithm):
         bug_step(u, cache, t, dt)
     elif isinstance(alg, RankAdaptiveUnconventionalAlgorithm):
         ra_bug_step(u, cache, t, dt, alg)
