@@ -102,12 +102,24 @@ typedef enum { LRI_KSL_PRIMAL = 0, LRI_KSL_DUAL = 1, LRI_KSL_STRANG = 2 } lri_ks
  *               nu per column (operator B, m values).  Evaluated tile by
  *               tile on Y = K V^T without forming the n x m matrix.
  *   DATA        MatrixDataProblem: exact substep flows driven by the snapshot
- *               increment Δy = A(t+dt) - A(t) (data_integrator.jl:13-16). */
+ *               increment Δy = A(t+dt) - A(t) (data_integrator.jl:13-16).
+ *   LOCAL_FLOW  a flow map registered in the library when it is built
+ *               (csrc/flows.cuh; stands in for the reference's user-supplied
+ *               F and K_rhs / L_rhs / S_rhs hooks, unconventional.jl:2-4,
+ *               16-21,51-79): F(Y)_ij = f(Y_{i-1,j}, Y_ij, Y_{i+1,j}, c_j;
+ *               h, p0, p1), periodic along the rows.  lri_batch_desc.flow
+ *               selects it (lri_flow_count / lri_flow_name list them),
+ *               burgers_h / _alpha / _beta carry h, p0, p1, operator B the
+ *               per-column c (m values).  Evaluated like BURGERS, tile by
+ *               tile without forming the n x m matrix.  Flow 0 is the
+ *               Burgers flow; flow 1 "reaction_diffusion" is
+ *               F = (Dxx Y) diag(c) + p0 Y + p1 Y.^3. */
 typedef enum {
   LRI_OP_ZERO = 0,
   LRI_OP_SYLVESTER_TRIDIAG = 1,
   LRI_OP_BURGERS_PERIODIC = 2,
-  LRI_OP_DATA = 3
+  LRI_OP_DATA = 3,
+  LRI_OP_LOCAL_FLOW = 4
 } lri_op_kind;
 
 /* Fixed-step explicit Runge-Kutta substep scheme with a sub-diagonal Butcher
@@ -135,12 +147,12 @@ typedef struct {
   int32_t dtype;       /* lri_dtype */
   int32_t op;          /* lri_op_kind */
   int32_t count;       /* number of instances (>= 1) */
-  int32_t reserved;
+  int32_t flow;        /* LRI_OP_LOCAL_FLOW: registered flow id; else 0 */
   const int64_t* n;      /* host [count]: rows of U */
   const int64_t* m;      /* host [count]: rows of V */
   const int64_t* r;      /* host [count]: initial rank */
   const int64_t* r_cap;  /* host [count]: capacity (rank-adaptive r_max), NULL => r */
-  double burgers_h, burgers_alpha, burgers_beta;
+  double burgers_h, burgers_alpha, burgers_beta;  /* BURGERS: h, alpha, beta; LOCAL_FLOW: h, p0, p1 */
 } lri_batch_desc;
 
 typedef struct lri_batch lri_batch;
@@ -149,6 +161,10 @@ typedef struct lri_batch lri_batch;
 LRI_API int lri_abi_version(void);
 LRI_API const char* lri_status_str(lri_status s);
 LRI_API lri_status lri_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor);
+/* The local flow maps compiled into the library (LRI_OP_LOCAL_FLOW): their
+ * count and the name of flow id (NULL beyond the count). */
+LRI_API int32_t lri_flow_count(void);
+LRI_API const char* lri_flow_name(int32_t id);
 
 /* init(prob, alg, dt): validates the shapes, plans the packed layout and
  * allocates the workspace. */

@@ -31,7 +31,8 @@ __all__ = [
     "MatrixHybridProblem", "DLRSolution", "DLRIntegrator",
     "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm", "ProjectorSplitting", "GreedyIntegrator",
     "PrimalLieTrotter", "DualLieTrotter", "Strang", "SubstepScheme", "Euler", "Heun", "Midpoint", "RK4",
-    "ZeroOperator", "SylvesterTridiagOperator", "Batch", "MixedEnsemble", "init", "step", "solve",
+    "ZeroOperator", "SylvesterTridiagOperator", "BurgersOperator", "LocalFlowOperator", "ReactionDiffusionOperator",
+    "registered_flows", "Batch", "MixedEnsemble", "init", "step", "solve",
     "solve_ensemble", "core_condition", "History",
     "LriError", "n_steps",
 ]
@@ -137,6 +138,53 @@ class BurgersOperator:
         if nu.shape != (m,):
             raise ValueError(f"nu has {nu.shape[0]} entries for {m} columns")
         return np.zeros(0), np.array(nu, dtype=np.float64)
+
+
+class LocalFlowOperator:
+    """A flow map compiled into the library (csrc/flows.cuh; the engine's
+    stand-in for a user-supplied F, src/integrators/unconventional.jl:2-4,
+    51-79): F(Y)_ij = f(Y_{i-1,j}, Y_ij, Y_{i+1,j}, c_j; h, p0, p1), periodic
+    along the rows.  ``flow`` is the registered name or id
+    (``registered_flows()``), ``c`` one value or one per column."""
+    kind = _native.LRI_OP_LOCAL_FLOW
+
+    def __init__(self, flow, h: float, c, p0: float = 0.0, p1: float = 0.0):
+        self.flow = flow
+        self.h = float(h)
+        self.c = np.asarray(c, dtype=np.float64)
+        self.p0 = float(p0)
+        self.p1 = float(p1)
+
+    def flow_id(self) -> int:
+        names = registered_flows()
+        if isinstance(self.flow, str):
+            if self.flow not in names:
+                raise ValueError(f"no flow map named {self.flow!r} in the library ({names})")
+            return names.index(self.flow)
+        if not 0 <= int(self.flow) < len(names):
+            raise ValueError(f"flow id {self.flow} outside the registry ({names})")
+        return int(self.flow)
+
+    def params(self):
+        return (self.h, self.p0, self.p1)
+
+    def packed_for(self, n: int, m: int):
+        c = np.broadcast_to(self.c, (m,)) if self.c.ndim == 0 else self.c
+        if c.shape != (m,):
+            raise ValueError(f"c has {c.shape[0]} entries for {m} columns")
+        return np.zeros(0), np.array(c, dtype=np.float64)
+
+
+def ReactionDiffusionOperator(h: float, c, p0: float = 0.0, p1: float = 0.0) -> LocalFlowOperator:
+    """F(Y) = (Dxx Y) diag(c) + p0 Y + p1 Y.^3, periodic (Allen-Cahn for
+    c = eps^2, p0 = 1, p1 = -1): the registered flow "reaction_diffusion"."""
+    return LocalFlowOperator("reaction_diffusion", h, c, p0, p1)
+
+
+def registered_flows() -> List[str]:
+    """Names of the flow maps compiled into the library, by id."""
+    lib = _native.load()
+    return [lib.lri_flow_name(i).decode() for i in range(int(lib.lri_flow_count()))]
 
 
 @dataclass
@@ -377,8 +425,10 @@ class Batch:
         desc.m = self.m.ctypes.data_as(I64P)
         desc.r = self.r0.ctypes.data_as(I64P)
         desc.r_cap = self.rcap.ctypes.data_as(I64P)
-        if op_params is not None:  # Burgers (h, alpha, beta), shared by the batch
-            desc.burgers_h, desc.burgers_alpha, desc.burgers_beta = (float(x) for x in op_params)
+        if op_params is not None:  # Burgers (h, alpha, beta) or a local flow (h, p0, p1, id), shared by the batch
+            desc.burgers_h, desc.burgers_alpha, desc.burgers_beta = (float(x) for x in op_params[:3])
+            if len(op_params) > 3:
+                desc.flow = int(op_params[3])
         self._algd = _alg_desc(alg, two_factor)
         self.two_factor = bool(two_factor)
         self.handle = C.c_void_p()
@@ -464,7 +514,7 @@ class Batch:
                 hB[self.offB[i]:self.offB[i] + len(b)] = b
             self.opA.copy_(t.from_numpy(hA))
             self.opB.copy_(t.from_numpy(hB))
-        if operators is not None and self.op_kind == _native.LRI_OP_BURGERS_PERIODIC:
+        if operators is not None and self.op_kind in (_native.LRI_OP_BURGERS_PERIODIC, _native.LRI_OP_LOCAL_FLOW):
             hB = np.zeros(int(self.opB.numel()), self.np_dtype)
             for i, op in enumerate(operators):
                 _, b = op.packed_for(int(self.n[i]), int(self.m[i]))
@@ -653,6 +703,8 @@ def _op_kind(prob) -> int:
         return _native.LRI_OP_SYLVESTER_TRIDIAG
     if isinstance(f, BurgersOperator):
         return _native.LRI_OP_BURGERS_PERIODIC
+    if isinstance(f, LocalFlowOperator):
+        return _native.LRI_OP_LOCAL_FLOW
     raise LriError(2, "flow map is not one of the engine's operators (arbitrary closures are unsupported)")
 
 
@@ -663,12 +715,12 @@ def _has_data(prob) -> bool:
 def _op_params(probs):
     """Batch-wide Burgers parameters (h, alpha, beta), or None."""
     fs = [p.f for p in probs if isinstance(p, (MatrixDEProblem, MatrixHybridProblem))
-          and isinstance(p.f, BurgersOperator)]
+          and isinstance(p.f, (BurgersOperator, LocalFlowOperator))]
     if not fs:
         return None
-    ps = {f.params() for f in fs}
+    ps = {f.params() + ((f.flow_id(),) if isinstance(f, LocalFlowOperator) else ()) for f in fs}
     if len(ps) != 1:
-        raise ValueError("Burgers instances of one batch must share h, alpha and beta")
+        raise ValueError("the flow-map instances of one batch must share the flow, h and its two scalars")
     return ps.pop()
 
 
@@ -817,7 +869,7 @@ class MixedEnsemble:
     def __init__(self, factors: Sequence[SVDLikeRepresentation], operators, alg, op_kind: int,
                  kappa_max: float = MIXED_KAPPA_MAX, r_cap=None):
         op_params = None
-        if op_kind == _native.LRI_OP_BURGERS_PERIODIC:
+        if op_kind in (_native.LRI_OP_BURGERS_PERIODIC, _native.LRI_OP_LOCAL_FLOW):
             op_params = _op_params([MatrixDEProblem(f, Y, (0.0, 1.0)) for f, Y in zip(operators, factors)])
         torch = _torch()
         self.torch = torch

@@ -22,11 +22,11 @@ STATUS_NAMES = {
 LRI_F64, LRI_F32, LRI_DF = 0, 1, 2
 LRI_ALG_BUG, LRI_ALG_RA_BUG, LRI_ALG_KSL, LRI_ALG_GREEDY = 0, 1, 2, 3
 LRI_KSL_PRIMAL, LRI_KSL_DUAL, LRI_KSL_STRANG = 0, 1, 2
-LRI_OP_ZERO, LRI_OP_SYLVESTER_TRIDIAG, LRI_OP_BURGERS_PERIODIC, LRI_OP_DATA = 0, 1, 2, 3
+LRI_OP_ZERO, LRI_OP_SYLVESTER_TRIDIAG, LRI_OP_BURGERS_PERIODIC, LRI_OP_DATA, LRI_OP_LOCAL_FLOW = 0, 1, 2, 3, 4
 
 # Every symbol include/lri.h declares (checked by the CPU test suite).
 EXPORTED = [
-    "lri_abi_version", "lri_status_str", "lri_device_info", "lri_batch_create", "lri_batch_destroy",
+    "lri_abi_version", "lri_status_str", "lri_device_info", "lri_flow_count", "lri_flow_name", "lri_batch_create", "lri_batch_destroy",
     "lri_batch_layout", "lri_batch_bind", "lri_batch_data_layout", "lri_batch_data_init", "lri_batch_step",
     "lri_batch_ranks", "lri_batch_status", "lri_batch_launches_per_step", "lri_bug_step_noalloc",
     "lri_batch_prepare", "lri_batch_adjoint_prepare", "lri_batch_adjoint_step",
@@ -55,7 +55,7 @@ class lri_alg_desc(C.Structure):
 
 
 class lri_batch_desc(C.Structure):
-    _fields_ = [("dtype", C.c_int32), ("op", C.c_int32), ("count", C.c_int32), ("reserved", C.c_int32),
+    _fields_ = [("dtype", C.c_int32), ("op", C.c_int32), ("count", C.c_int32), ("flow", C.c_int32),
                 ("n", C.POINTER(C.c_int64)), ("m", C.POINTER(C.c_int64)), ("r", C.POINTER(C.c_int64)),
                 ("r_cap", C.POINTER(C.c_int64)), ("burgers_h", C.c_double), ("burgers_alpha", C.c_double),
                 ("burgers_beta", C.c_double)]
@@ -70,6 +70,9 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_abi_version.restype = C.c_int
     lib.lri_status_str.restype = C.c_char_p
     lib.lri_status_str.argtypes = [C.c_int]
+    lib.lri_flow_count.restype = C.c_int32
+    lib.lri_flow_name.restype = C.c_char_p
+    lib.lri_flow_name.argtypes = [C.c_int32]
     lib.lri_device_info.restype = C.c_int
     lib.lri_device_info.argtypes = [C.POINTER(C.c_int)] * 4
     lib.lri_batch_create.restype = C.c_int

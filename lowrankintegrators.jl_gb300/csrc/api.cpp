@@ -122,6 +122,7 @@ StepArgs<T> make_args(const lri_batch* b, double t, double dt, const void* Ynext
   g.sK = to_scheme(b->alg.K_alg);
   g.sL = to_scheme(b->alg.L_alg);
   g.sS = to_scheme(b->alg.S_alg);
+  g.flow = b->desc.flow;
   g.bh = b->desc.burgers_h;
   g.balpha = b->desc.burgers_alpha;
   g.bbeta = b->desc.burgers_beta;
@@ -176,6 +177,10 @@ const char* lri_status_str(lri_status s) {
   return "unknown status";
 }
 
+int32_t lri_flow_count(void) { return lri::local_flow_count(); }
+
+const char* lri_flow_name(int32_t id) { return lri::local_flow_name(id); }
+
 lri_status lri_device_info(int* device, int* sm_count, int* cc_major, int* cc_minor) {
   int dev = 0;
   LRI_CUDA(cudaGetDevice(&dev));
@@ -193,7 +198,9 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   *out = nullptr;
   if (desc->count < 1 || !desc->n || !desc->m || !desc->r) return LRI_ERR_ARG;
   if (desc->dtype != LRI_F32 && desc->dtype != LRI_F64 && desc->dtype != LRI_DF) return LRI_ERR_ARG;
-  if (desc->op < LRI_OP_ZERO || desc->op > LRI_OP_DATA) return LRI_ERR_ARG;
+  if (desc->op < LRI_OP_ZERO || desc->op > LRI_OP_LOCAL_FLOW) return LRI_ERR_ARG;
+  if (desc->op == LRI_OP_LOCAL_FLOW && (desc->flow < 0 || desc->flow >= lri::local_flow_count()))
+    return LRI_ERR_ARG;
   if (alg->kind < LRI_ALG_BUG || alg->kind > LRI_ALG_GREEDY) return LRI_ERR_ARG;
   if (alg->kind == LRI_ALG_GREEDY) {
     if (alg->two_factor != 0 && alg->two_factor != 1) return LRI_ERR_ARG;
@@ -203,7 +210,7 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
   if (alg->kind == LRI_ALG_KSL && (alg->ksl_order < 0 || alg->ksl_order > 2)) return LRI_ERR_ARG;
   if (!scheme_ok(alg->K_alg) || !scheme_ok(alg->L_alg) || !scheme_ok(alg->S_alg)) return LRI_ERR_ARG;
   if (alg->kind == LRI_ALG_RA_BUG && (!(alg->tol >= 0.0) || alg->r_min < 1)) return LRI_ERR_ARG;
-  if (desc->op == LRI_OP_BURGERS_PERIODIC &&
+  if ((desc->op == LRI_OP_BURGERS_PERIODIC || desc->op == LRI_OP_LOCAL_FLOW) &&
       !(desc->burgers_h > 0.0 && std::isfinite(desc->burgers_h) && std::isfinite(desc->burgers_alpha) &&
         std::isfinite(desc->burgers_beta)))
     return LRI_ERR_ARG;
@@ -260,8 +267,8 @@ lri_status lri_batch_create(lri_batch** out, const lri_batch_desc* desc, const l
     if (desc->op == LRI_OP_SYLVESTER_TRIDIAG) {
       b->totA += 3 * n;
       b->totB += 3 * m;
-    } else if (desc->op == LRI_OP_BURGERS_PERIODIC) {
-      b->totB += m;  // per-column viscosity
+    } else if (desc->op == LRI_OP_BURGERS_PERIODIC || desc->op == LRI_OP_LOCAL_FLOW) {
+      b->totB += m;  // per-column parameter (Burgers: viscosity)
     }
     // side workspaces: PY, PQ (N x W) + PA, PZ0, PZ1 (N x rcap); keep 16-byte alignment
     auto al = [](int64_t x) { return (x + 3) & ~int64_t(3); };

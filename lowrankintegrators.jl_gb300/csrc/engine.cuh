@@ -15,6 +15,7 @@
 
 #include "dfloat.cuh"
 #include "engine_api.h"
+#include "flows.cuh"
 
 namespace lri {
 
@@ -342,8 +343,10 @@ struct LoadDelta {
 };
 
 // ---------------------------------------------------------------------------
-// Periodic Burgers flow map contracted with low-rank factors (one CTA):
+// Local flow map (flows.cuh) contracted with low-rank factors (one CTA):
 //   Y = XL ZR^T (N x M: rows = grid points, columns = samples),
+//   F(Y)_ij = Flow::eval(Y_{i-1,j}, Y_ij, Y_{i+1,j}, nu_j; h, alpha, beta),
+//   rows periodic; e.g. the Burgers flow
 //   F(Y) = (Dxx Y) diag(nu) + alpha (Dx Y).*Y + beta Dx(Y.*Y),
 //   Dxx = tridiag(1,-2,1)/h^2, Dx = tridiag(-1,0,1)/(2h), both periodic;
 //   BURG_K: out (N x k, ld ldo) = F ZR
@@ -356,8 +359,8 @@ struct LoadDelta {
 // ---------------------------------------------------------------------------
 enum : int { BURG_K = 0, BURG_L = 1, BURG_S = 2 };
 
-template <typename T>
-__device__ __noinline__ void burgers_contract(int mode, int N, int M, int k, const T* XL, const T* ZR, const T* CL,
+template <typename T, typename Flow>
+__device__ __noinline__ void flow_contract(int mode, int N, int M, int k, const T* XL, const T* ZR, const T* CL,
                                               int p, const T* nu, double h, double alpha, double beta, T sgn, T* out,
                                               int ldo, T* stage) {
   const int tid = threadIdx.x;
@@ -408,10 +411,7 @@ __device__ __noinline__ void burgers_contract(int mode, int N, int M, int k, con
     for (int o = tid; o < rows * TCb; o += NT) {
       const int ii = o / TCb, jj = o - (o / TCb) * TCb;
       const T ym = ys[ii * TCb + jj], y0 = ys[(ii + 1) * TCb + jj], yp = ys[(ii + 2) * TCb + jj];
-      T f = nus[jj] * (((ym + yp) - (y0 + y0)) * ih2);
-      f = fma(al * ((yp - ym) * ihx), y0, f);
-      f = fma(be, (yp * yp - ym * ym) * ihx, f);
-      fs[ii * ldf + jj] = f;
+      fs[ii * ldf + jj] = Flow::template eval<T>(ym, y0, yp, nus[jj], ih2, ihx, al, be);
     }
     __syncthreads();
   };

@@ -22,7 +22,7 @@ constexpr int kSmallBlocks = 23;
 
 enum AlgKind : int32_t { ALG_BUG = 0, ALG_RA_BUG = 1, ALG_KSL = 2, ALG_GREEDY = 3 };
 enum KslOrder : int32_t { KSL_PRIMAL = 0, KSL_DUAL = 1, KSL_STRANG = 2 };
-enum OpKind : int32_t { OP_ZERO = 0, OP_SYLVESTER = 1, OP_BURGERS = 2, OP_DATA = 3 };
+enum OpKind : int32_t { OP_ZERO = 0, OP_SYLVESTER = 1, OP_BURGERS = 2, OP_DATA = 3, OP_LOCAL = 4 };
 
 // Device status bits (OR-ed into the batch status word).
 enum StatusBits : uint32_t {
@@ -67,10 +67,15 @@ struct StepArgs {
   double t, dt;
   int32_t alg, ksl_order, op, r_min;
   int32_t two_factor;  // greedy: factors U Z^T (Z in V) instead of U S V^T
+  int32_t flow;        // OP_LOCAL: registered flow id (flows.cuh)
   double tol;
   Scheme sK, sL, sS;
-  double bh, balpha, bbeta;
+  double bh, balpha, bbeta;  // local flows: h, p0, p1 (Burgers: h, alpha, beta)
 };
+
+// Registered local flow maps (flows.cuh): count and names.
+int local_flow_count();
+const char* local_flow_name(int id);
 
 // Raises a kernel's dynamic shared-memory limit on the current device.  The
 // attribute is per device, so `done` keeps one bit per device ordinal (< 64;

@@ -35,4 +35,18 @@ cudaError_t convert_df_to_f64(const void* in, double* out, int64_t n, cudaStream
   return cudaGetLastError();
 }
 
+int local_flow_count() { return kLocalFlowCount; }
+
+const char* local_flow_name(int id) {
+  switch (id) {
+#define LRI_FLOW_NAME(ID, TYPE, NAME) \
+  case ID:                            \
+    return NAME;
+    LRI_LOCAL_FLOWS(LRI_FLOW_NAME)
+#undef LRI_FLOW_NAME
+    default:
+      return nullptr;
+  }
+}
+
 }  // namespace lri

@@ -181,10 +181,16 @@ __device__ __noinline__ void orth_panel(const Inst<T>& I, T* Kp, int N, int W, T
   qr_panel<T>(Kp, N, W, Qdst, R, ldr, sm);
 }
 
-// Burgers K (side 0) or L (side 1) substep on the panel Y (N x r, ld N):
+// The registered local flow of the batch: the Burgers operator is flow 0.
+template <typename T>
+__device__ __forceinline__ int flow_id(const StepArgs<T>& g) {
+  return g.op == OP_BURGERS ? 0 : g.flow;
+}
+
+// Local-flow (Burgers or registered) K (side 0) or L (side 1) substep on the panel Y (N x r, ld N):
 // the scheme's stages one by one (the flow is nonlinear), each stage
 // derivative k_s = F(Z_s V^T) V (K) or F(U Z_s^T)^T U (L) formed by
-// burgers_contract into the free QR panel; Xo is the other side's basis.
+// flow_contract into the free QR panel; Xo is the other side's basis.
 template <typename T>
 __device__ __noinline__ void burgers_panel_rk(const StepArgs<T>& g, const Inst<T>& I, const Side<T>& sd, int side,
                                               T* Y, int r, const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
@@ -199,12 +205,15 @@ __device__ __noinline__ void burgers_panel_rk(const StepArgs<T>& g, const Inst<T
   for (int sub = 0; sub < sc.nsub; ++sub) {
     for (int s = 0; s < ns; ++s) {
       const T* Z = (s == 0) ? Y : Zb[(s - 1) & 1];
-      if (side == 0)
-        burgers_contract<T>(BURG_K, I.n, I.m, r, Z, Xo, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst, N,
-                            sm.stage);
-      else
-        burgers_contract<T>(BURG_L, I.n, I.m, r, Xo, Z, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst, N,
-                            sm.stage);
+      with_local_flow(flow_id(g), [&](auto flow) {
+        using Flow = decltype(flow);
+        if (side == 0)
+          flow_contract<T, Flow>(BURG_K, I.n, I.m, r, Z, Xo, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst,
+                                 N, sm.stage);
+        else
+          flow_contract<T, Flow>(BURG_L, I.n, I.m, r, Xo, Z, nullptr, 0, nu, g.bh, g.balpha, g.bbeta, T(1), Kst,
+                                 N, sm.stage);
+      });
       const T bs = T(sc.b[s]);
       const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
       T* Zout = Zb[s & 1];
@@ -237,7 +246,7 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
                              const T* Gp, const T* Xo, const Scheme& sc, double dt, Smem<T>& sm) {
   const int N = sd.N;
   if (g.op == OP_ZERO) return;
-  if (g.op == OP_BURGERS) {
+  if (g.op == OP_BURGERS || g.op == OP_LOCAL) {
     burgers_panel_rk<T>(g, I, sd, side, Y, r, Xo, sc, dt, sm);
     return;
   }
@@ -301,7 +310,7 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
     tile_gram<T>(n, p, q, sm.stage, RowLoadPanel<T>{Ub, n, p}, RowLoadPanel<T>{Z, n, q}, St, W, sign, T(1));
     return;
   }
-  if (g.op == OP_BURGERS) {
+  if (g.op == OP_BURGERS || g.op == OP_LOCAL) {
     // k_s = sign * U^T F(U Z_s V^T) V with U Z_s formed in the free K-side
     // QR panel (n x q), stages one by one
     T* XLp = I.k.PY;
@@ -314,8 +323,10 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
       for (int s = 0; s < ns; ++s) {
         const T* Z = (s == 0) ? St : SZb[(s - 1) & 1];
         tile_gemm<T>(I.n, p, q, sm.stage, LoadPanel<T>{Ub, I.n}, LoadSmall<T>{Z, W, false}, EpiStore<T>{XLp, I.n});
-        burgers_contract<T>(BURG_S, I.n, I.m, q, XLp, Vb, Ub, p, I.l.tri, g.bh, g.balpha, g.bbeta, sign, SKb, W,
-                            sm.stage);
+        with_local_flow(flow_id(g), [&](auto flow) {
+          flow_contract<T, decltype(flow)>(BURG_S, I.n, I.m, q, XLp, Vb, Ub, p, I.l.tri, g.bh, g.balpha, g.bbeta,
+                                           sign, SKb, W, sm.stage);
+        });
         const T bs = T(sc.b[s]);
         const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
         T* Zout = SZb[s & 1];

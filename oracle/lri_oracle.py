@@ -46,7 +46,7 @@ __all__ = [
     "UnconventionalAlgorithm", "RankAdaptiveUnconventionalAlgorithm",
     "ProjectorSplitting", "PrimalLieTrotter", "DualLieTrotter", "Strang",
     "SubstepScheme", "Euler", "Heun", "Midpoint", "RK4",
-    "SylvesterTridiagOp", "BurgersOp", "DenseOp", "ZeroOp",
+    "SylvesterTridiagOp", "BurgersOp", "ReactionDiffusionOp", "DenseOp", "ZeroOp",
     "solve", "init", "step", "truncate_to_tolerance", "truncated_svd",
     "rel_fro_err", "to_dense",
 ]
@@ -424,6 +424,25 @@ class BurgersOp(Operator):
         if self.beta != 0.0:
             out += self.beta * self._dx(X * X)
         return out
+
+
+class ReactionDiffusionOp(BurgersOp):
+    """Periodic reaction-diffusion flow map, column j = sample j:
+
+        F(X) = (Dxx X) diag(c) + p0 X + p1 X.^3
+
+    (Allen-Cahn for c = eps^2, p0 = 1, p1 = -1).  The dense restatement of
+    the library's registered local flow "reaction_diffusion": a flow map the
+    reference would take as a user closure F (unconventional.jl:51-79)."""
+
+    def __init__(self, n: int, h: float, c, p0: float = 0.0, p1: float = 0.0):
+        super().__init__(n, h, c, 0.0, 0.0)
+        self.p0 = float(p0)
+        self.p1 = float(p1)
+
+    def __call__(self, X, t):
+        c = self.nu if self.nu.ndim else np.full(X.shape[1], float(self.nu))
+        return self._dxx(X) * c[None, :] + self.p0 * X + self.p1 * X ** 3
 
 
 # --------------------------------------------------------------------------
