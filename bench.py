@@ -282,6 +282,7 @@ def leg_stream(steps, warmup):
     eng.check_status()
     rank_end = eng.rank()
     tc_used = eng.uses_tensor_cores()
+    eng_tiles = eng.tuning or {"shape": None, "note": "automatic: K splits filling the SMs, as many stages as fit"}
 
     # the dominant kernel: one snapshot pass (dY X, dY^T X with 96 columns)
     # timed alone, on the tensor cores and on the CUDA cores
@@ -359,6 +360,7 @@ def leg_stream(steps, warmup):
             "accuracy": {"steps": 3, "rel_fro_vs_fp64_oracle": err, "rank_gpu": Yg.S.shape[0],
                          "rank_oracle": Yo.S.shape[0]},
             "passes": pass_ms,
+            "pass_tiles": eng_tiles,
             "ms_per_step_cuda_core_passes": ms_cuda_core,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "peak_source": src,
@@ -828,6 +830,14 @@ def main():
     value = weak_value(ws, K, ms_max * 1e-3)
     kap = np.array([lri.core_condition(Y.S) for Y in factors])
     n_fp32 = int((kap <= lri.MIXED_KAPPA_MAX).sum())
+    # the autotuned register budget of each precision class (tuning.json)
+    ensemble_tiles = {}
+    for prec, sel in (("fp32", np.flatnonzero(kap <= lri.MIXED_KAPPA_MAX)),
+                      ("df", np.flatnonzero(kap > lri.MIXED_KAPPA_MAX))):
+        c, bucket = lri._tuning.ensemble_occupancy(prec, [shapes[0][i] for i in sel], [shapes[1][i] for i in sel],
+                                                   [shapes[2][i] for i in sel])
+        ensemble_tiles[prec] = {"ctas_per_sm": c, "tuned_bucket": bucket,
+                                "micro_tile": "4x4 per thread, rows per tile 4*256/ceil(c/4) (c = panel columns)"}
     # pure FP32 form and plain FP64 form, same steps
     ms32, y32, _, _ = timed_run(lambda: Single("fp32"), K, K)
     k64 = K if args.fp64_steps is None else min(K, args.fp64_steps)
@@ -937,6 +947,7 @@ def main():
                    "precision": "mixed: FP32 for kappa(S0) <= %.0e (%d instances), double-float for the other %d"
                                 % (lri.MIXED_KAPPA_MAX, n_fp32, args.count - n_fp32),
                    "instance_steps_per_s": value * args.count,
+                   "tiles": ensemble_tiles,
                    "l2": "inputs larger than L2: factors %.0f MB + operators + workspace > 129 MB"
                          % (alg_bytes / 2e6)},
         "accuracy": {"mixed_vs_fp64_gpu_rel_fro_max": float(err_mix.max()),

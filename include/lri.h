@@ -206,6 +206,12 @@ LRI_API lri_status lri_batch_step(lri_batch* b, double t, double dt, int32_t nst
  * capture.  No counterpart in the reference. */
 LRI_API lri_status lri_batch_prepare(lri_batch* b, double dt, int32_t nsteps);
 
+/* Register budget of the batch's step kernel, the autotuner's knob for the
+ * instance engine: 3 CTAs per SM (at most 80 registers per thread; the
+ * default) or 2 (at most 128 registers: fewer spills, less latency hiding).
+ * FP64 batches take 3 only.  No counterpart in the reference. */
+LRI_API lri_status lri_batch_set_occupancy(lri_batch* b, int32_t ctas_per_sm);
+
 /* Current ranks (host array of length count; synchronises the stream). */
 LRI_API lri_status lri_batch_ranks(lri_batch* b, int64_t* r_out, void* stream);
 
@@ -303,6 +309,12 @@ LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
  * cores the stream cannot use).  No counterpart in the reference. */
 LRI_API lri_status lri_stream_set_tensor_cores(lri_stream* s, int32_t enable);
 LRI_API lri_status lri_stream_uses_tensor_cores(const lri_stream* s, int32_t* out);
+/* Tile choices of the tensor-core passes (the autotuner's knobs): K splits
+ * per 128-row output tile of dY X (splits_rows) and of dY^T X (splits_cols),
+ * and pipeline stages (2 .. what fits in shared memory); 0 keeps the
+ * automatic choice (splits filling the SMs, as many stages as fit).  No
+ * counterpart in the reference. */
+LRI_API lri_status lri_stream_set_pass_tiles(lri_stream* s, int32_t splits_rows, int32_t splits_cols, int32_t stages);
 
 /* One product of the data substeps (the increments left^T dY right of
  * src/integrators/data_integrator.jl:13-16, dY = A(t+dt) - A(t) as in

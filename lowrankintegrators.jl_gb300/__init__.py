@@ -23,7 +23,7 @@ from typing import Callable, List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 
-from . import _native
+from . import _native, _tuning
 from ._native import LriError
 
 __all__ = [
@@ -562,6 +562,19 @@ class Batch:
         if nsteps > 1 and not self.has_data:
             _native.check(self.lib.lri_batch_prepare(self.handle, float(dt), int(nsteps)), "lri_batch_prepare")
 
+    def set_occupancy(self, ctas_per_sm: int):
+        """Register budget of the step kernel: 3 (default) or 2 CTAs per SM."""
+        _native.check(self.lib.lri_batch_set_occupancy(self.handle, int(ctas_per_sm)), "lri_batch_set_occupancy")
+        self.ctas_per_sm = int(ctas_per_sm)
+
+    def apply_tuning(self, table=None):
+        """Takes the tuned register budget of this batch's precision and
+        dominant rank bucket (``tuning.json``); returns what was chosen."""
+        ctas, bucket = _tuning.ensemble_occupancy(self.precision, self.n, self.m, self.rcap, table)
+        if self.precision != "fp64":
+            self.set_occupancy(ctas)
+        return {"ctas_per_sm": getattr(self, "ctas_per_sm", 3), "bucket": bucket}
+
     def launches_per_step(self) -> int:
         return int(self.lib.lri_batch_launches_per_step(self.handle))
 
@@ -867,8 +880,9 @@ class MixedEnsemble:
     double-float batch, stepped concurrently on two CUDA streams."""
 
     def __init__(self, factors: Sequence[SVDLikeRepresentation], operators, alg, op_kind: int,
-                 kappa_max: float = MIXED_KAPPA_MAX, r_cap=None):
+                 kappa_max: float = MIXED_KAPPA_MAX, r_cap=None, tuned: bool = True):
         op_params = None
+        self.tuning = {}
         if op_kind in (_native.LRI_OP_BURGERS_PERIODIC, _native.LRI_OP_LOCAL_FLOW):
             op_params = _op_params([MatrixDEProblem(f, Y, (0.0, 1.0)) for f, Y in zip(operators, factors)])
         torch = _torch()
@@ -886,6 +900,7 @@ class MixedEnsemble:
             b = Batch([Y.U.shape[0] for Y in fs], [Y.V.shape[0] for Y in fs], [Y.S.shape[0] for Y in fs], alg,
                       op_kind, prec, r_cap=rc, op_params=op_params)
             b.upload(fs, ops)
+            self.tuning[prec] = b.apply_tuning() if tuned else {"ctas_per_sm": 3, "bucket": None}
             self.parts.append((prec, sel, b, torch.cuda.Stream()))
 
     def step(self, t: float, dt: float, nsteps: int = 1):
@@ -1067,6 +1082,12 @@ class DataStreamEngine:
                                                  float(tol), int(rmin)), "lri_stream_create")
         dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
+        self.tuning = None
+        if type(self) is DataStreamEngine and self.uses_tensor_cores():
+            sr, sc, st, key = _tuning.stream_pass_tiles(self.n, self.m, self.R)
+            if key is not None:
+                self.set_pass_tiles(sr, sc, st)
+                self.tuning = {"shape": key, "splits_rows": sr, "splits_cols": sc, "stages": st}
         self.U = torch.zeros(self.n * self.R, dtype=self.dtype, device=dev)
         self.S = torch.zeros(self.R * self.R, dtype=self.dtype, device=dev)
         self.V = torch.zeros(self.m * self.R, dtype=self.dtype, device=dev)
@@ -1099,6 +1120,11 @@ class DataStreamEngine:
         """Selects the tensor-core (3xTF32) or CUDA-core snapshot passes."""
         _native.check(self.lib.lri_stream_set_tensor_cores(self.handle, int(bool(enable))),
                       "lri_stream_set_tensor_cores")
+
+    def set_pass_tiles(self, splits_rows: int = 0, splits_cols: int = 0, stages: int = 0):
+        """Tile choices of the tensor-core passes (0 = automatic)."""
+        _native.check(self.lib.lri_stream_set_pass_tiles(self.handle, int(splits_rows), int(splits_cols), int(stages)),
+                      "lri_stream_set_pass_tiles")
 
     def uses_tensor_cores(self) -> bool:
         v = C.c_int32(0)

@@ -53,6 +53,7 @@ struct lri_batch {
   const void* opB = nullptr;
   bool bound = false;
   bool data_ready = false;
+  int32_t ctas_per_sm = 3;  // register budget of the step kernel (lri_batch_set_occupancy)
   // discrete adjoint (allocated by lri_batch_adjoint_prepare)
   double* d_adj_work = nullptr;
   int64_t* d_adj_off = nullptr;
@@ -131,12 +132,13 @@ StepArgs<T> make_args(const lri_batch* b, double t, double dt, const void* Ynext
 
 cudaError_t launch_one(const lri_batch* b, double t, double dt, const void* Ynext, cudaStream_t st) {
   const int count = b->desc.count;
-  if (b->desc.dtype == LRI_F32) return lri::launch_step<float>(make_args<float>(b, t, dt, Ynext), count, st);
+  if (b->desc.dtype == LRI_F32)
+    return lri::launch_step<float>(make_args<float>(b, t, dt, Ynext), count, st, b->ctas_per_sm);
   if (b->desc.dtype == LRI_DF) {
     cudaError_t e = cudaSuccess;
     if (Ynext) e = lri::convert_f64_to_df(static_cast<const double*>(Ynext), b->iYn, b->totY, st);
     if (e != cudaSuccess) return e;
-    return lri::launch_step<lri::dfloat>(make_args<lri::dfloat>(b, t, dt, Ynext), count, st);
+    return lri::launch_step<lri::dfloat>(make_args<lri::dfloat>(b, t, dt, Ynext), count, st, b->ctas_per_sm);
   }
   return lri::launch_step<double>(make_args<double>(b, t, dt, Ynext), count, st);
 }
@@ -505,6 +507,14 @@ lri_status lri_batch_status(lri_batch* b, void* stream) {
   if (s & lri::ST_NONFINITE) return LRI_ERR_NONFINITE;
   if (s & lri::ST_SVD_NOCONV) return LRI_ERR_BREAKDOWN;
   if (s & lri::ST_RANK_OVERFLOW) return LRI_ERR_RANK_OVERFLOW;
+  return LRI_OK;
+}
+
+lri_status lri_batch_set_occupancy(lri_batch* b, int32_t ctas_per_sm) {
+  if (!b || (ctas_per_sm != 2 && ctas_per_sm != 3)) return LRI_ERR_ARG;
+  if (b->desc.dtype == LRI_F64 && ctas_per_sm != 3) return LRI_ERR_UNSUPPORTED;
+  if (b->ctas_per_sm != ctas_per_sm) free_graph(b);  // the captured graph holds the other kernel
+  b->ctas_per_sm = ctas_per_sm;
   return LRI_OK;
 }
 

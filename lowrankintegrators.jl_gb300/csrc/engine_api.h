@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <type_traits>
 
 namespace lri_df {
 struct dfloat;  // double-float value (dfloat.cuh); the host only passes pointers to it
@@ -94,8 +95,20 @@ inline cudaError_t set_smem_limit(F* func, int bytes, std::atomic<uint64_t>& don
   return e;
 }
 
+template <typename T, int MINB>
+cudaError_t launch_step_occ(const StepArgs<T>& g, int count, cudaStream_t stream);
+
+// One launch of the step kernel for `count` instances.  ctas_per_sm selects
+// the register budget: 3 CTAs per SM (at most 80 registers per thread, the
+// default) or 2 (at most 128); FP64 batches have the default only.
 template <typename T>
-cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream);
+inline cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream, int ctas_per_sm = 3) {
+  if constexpr (std::is_same<T, double>::value) {
+    return launch_step_occ<T, 3>(g, count, stream);
+  } else {
+    return ctas_per_sm == 2 ? launch_step_occ<T, 2>(g, count, stream) : launch_step_occ<T, 3>(g, count, stream);
+  }
+}
 
 // double <-> double-float conversions of n elements (dfloat storage is a
 // pair of floats, 8 bytes per element)

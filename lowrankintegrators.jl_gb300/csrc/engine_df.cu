@@ -4,7 +4,7 @@
 
 namespace lri {
 
-template cudaError_t launch_step<dfloat>(const StepArgs<dfloat>&, int, cudaStream_t);
+template cudaError_t launch_step_occ<dfloat, 3>(const StepArgs<dfloat>&, int, cudaStream_t);
 template size_t step_smem_bytes<dfloat>();
 
 __global__ void f64_to_df_kernel(const double* __restrict__ in, dfloat* __restrict__ out, int64_t n) {

@@ -3,6 +3,6 @@
 #include "engine_impl.cuh"
 
 namespace lri {
-template cudaError_t launch_step<float>(const StepArgs<float>&, int, cudaStream_t);
+template cudaError_t launch_step_occ<float, 3>(const StepArgs<float>&, int, cudaStream_t);
 template size_t step_smem_bytes<float>();
 }  // namespace lri

@@ -3,6 +3,6 @@
 #include "engine_impl.cuh"
 
 namespace lri {
-template cudaError_t launch_step<double>(const StepArgs<double>&, int, cudaStream_t);
+template cudaError_t launch_step_occ<double, 3>(const StepArgs<double>&, int, cudaStream_t);
 template size_t step_smem_bytes<double>();
 }  // namespace lri

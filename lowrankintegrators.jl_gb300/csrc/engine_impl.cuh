@@ -873,8 +873,10 @@ __device__ __noinline__ void greedy_step(const StepArgs<T>& g, Inst<T>& I, int r
 // ---------------------------------------------------------------------------
 // The step kernel
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(NT, 3) step_kernel(StepArgs<T> g) {
+// MINB: CTAs per SM the register allocation is sized for (3: at most 80
+// registers per thread; 2: at most 128); the autotuner picks per precision.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(NT, MINB) step_kernel(StepArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem<T>& sm = *reinterpret_cast<Smem<T>*>(smem_raw);
   const int inst = g.order[blockIdx.x];
@@ -931,13 +933,13 @@ size_t step_smem_bytes() {
   return sizeof(Smem<T>);
 }
 
-template <typename T>
-cudaError_t launch_step(const StepArgs<T>& g, int count, cudaStream_t stream) {
+template <typename T, int MINB>
+cudaError_t launch_step_occ(const StepArgs<T>& g, int count, cudaStream_t stream) {
   const size_t smem = sizeof(Smem<T>);
   static std::atomic<uint64_t> attr_done{0};
-  cudaError_t e = set_smem_limit(step_kernel<T>, (int)smem, attr_done);
+  cudaError_t e = set_smem_limit(step_kernel<T, MINB>, (int)smem, attr_done);
   if (e != cudaSuccess) return e;
-  step_kernel<T><<<count, NT, smem, stream>>>(g);
+  step_kernel<T, MINB><<<count, NT, smem, stream>>>(g);
   return cudaGetLastError();
 }
 

@@ -2152,6 +2152,14 @@ lri_status lri_stream_set_tensor_cores(lri_stream* s, int32_t enable) {
   return LRI_OK;
 }
 
+lri_status lri_stream_set_pass_tiles(lri_stream* s, int32_t splits_rows, int32_t splits_cols, int32_t stages) {
+  if (!s || s->burgers) return LRI_ERR_ARG;
+  if (!s->tc_ok) return LRI_ERR_UNSUPPORTED;
+  const cudaError_t e = lri::tc_pass_set_tiles(&s->tc, splits_rows, splits_cols, stages);
+  if (e == cudaErrorInvalidValue) return LRI_ERR_ARG;
+  return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
+}
+
 lri_status lri_stream_uses_tensor_cores(const lri_stream* s, int32_t* out) {
   if (!s || !out) return LRI_ERR_ARG;
   *out = s->use_tc ? 1 : 0;

@@ -500,7 +500,7 @@ struct Plan {
   int P, K, tiles, nchunks, cps, splits;
 };
 
-Plan plan(int64_t P, int64_t K, int sms) {
+Plan plan(int64_t P, int64_t K, int sms, int forced_splits = 0) {
   Plan p{};
   p.P = (int)P;
   p.K = (int)K;
@@ -508,6 +508,7 @@ Plan plan(int64_t P, int64_t K, int sms) {
   p.nchunks = (int)((K + TC_BK - 1) / TC_BK);
   int splits = std::max(1, sms / p.tiles);
   splits = std::min(splits, std::max(1, p.nchunks / 4));  // at least 4 chunks (one pipeline fill) per CTA
+  if (forced_splits > 0) splits = std::min(forced_splits, p.nchunks);
   p.cps = (p.nchunks + splits - 1) / splits;
   p.splits = (p.nchunks + p.cps - 1) / p.cps;
   return p;
@@ -540,12 +541,32 @@ cudaError_t tc_pass_init(TcPass* t, int64_t n, int64_t m, int R) {
   e = cudaMalloc((void**)&t->xh, sizeof(float) * rows * t->NB);
   if (e == cudaSuccess) e = cudaMalloc((void**)&t->xl, sizeof(float) * rows * t->NB);
   if (e == cudaSuccess) e = cudaMalloc((void**)&t->part, sizeof(float) * part);
+  t->part_elems = part;
   if (e != cudaSuccess) return e;
   const bool ok = encode_2d(t->tm_xh_m, t->xh, m, t->NB, TC_BK, t->NB, true) &&
                   encode_2d(t->tm_xl_m, t->xl, m, t->NB, TC_BK, t->NB, true) &&
                   encode_2d(t->tm_xh_n, t->xh, n, t->NB, TC_BK, t->NB, true) &&
                   encode_2d(t->tm_xl_n, t->xl, n, t->NB, TC_BK, t->NB, true);
   return ok ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t tc_pass_set_tiles(TcPass* t, int splits_rows, int splits_cols, int stages) {
+  if (splits_rows < 0 || splits_cols < 0 || stages < 0 || (stages > 0 && stages < 2)) return cudaErrorInvalidValue;
+  if (stages > stages_for(t->NB)) return cudaErrorInvalidValue;
+  const Plan pr = plan(t->n, t->m, t->sms, splits_rows), pc = plan(t->m, t->n, t->sms, splits_cols);
+  const size_t need = std::max((size_t)pr.splits * t->n, (size_t)pc.splits * t->m) * t->NB;
+  if (need > t->part_elems) {
+    float* p = nullptr;
+    cudaError_t e = cudaMalloc((void**)&p, sizeof(float) * need);
+    if (e != cudaSuccess) return e;
+    cudaFree(t->part);  // cudaFree waits for the device: no pass still reads the old buffer
+    t->part = p;
+    t->part_elems = need;
+  }
+  t->ov_splits[0] = splits_rows;
+  t->ov_splits[1] = splits_cols;
+  t->ov_stages = stages;
+  return cudaSuccess;
 }
 
 void tc_pass_free(TcPass* t) {
@@ -566,12 +587,12 @@ cudaError_t tc_pass_run(TcPass* t, int trans, const float* A1, const float* A0, 
   const bool ok = rows_mode ? (encode_2d(tm1, A1, n, m, TC_BM, TC_BK, false) && encode_2d(tm0, A0, n, m, TC_BM, TC_BK, false))
                             : (encode_2d(tm1, A1, n, m, TC_BK, TC_BM, true) && encode_2d(tm0, A0, n, m, TC_BK, TC_BM, true));
   if (!ok) return cudaErrorInvalidValue;
-  const Plan pl = plan(P, K, t->sms);
+  const Plan pl = plan(P, K, t->sms, t->ov_splits[rows_mode ? 0 : 1]);
   const int NB = t->NB;
   tc_split_x<<<2 * t->sms, 256, 0, st>>>((int)K, t->R, NB, rank, ncols, X, ldx, t->xh, t->xl);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int stages = stages_for(NB);
+  const int stages = t->ov_stages > 0 ? t->ov_stages : stages_for(NB);
   const size_t smem = (size_t)stages * (2 * TC_TILE_BYTES + 2 * TC_BK * 4 * NB) + TC_CTRL_BYTES + 1024;
   static std::atomic<uint64_t> attr_done{0};  // the largest any panel width needs
   if ((e = set_smem_limit(tc_pass_kernel, TC_SMEM_LIMIT, attr_done)) != cudaSuccess) return e;

@@ -18,6 +18,9 @@ struct TcPass {
   float* xh = nullptr;    // max(n, m) x NB: TF32 hi part of the right factor
   float* xl = nullptr;    // max(n, m) x NB: TF32 lo part
   float* part = nullptr;  // split-K partials
+  size_t part_elems = 0;
+  int ov_splits[2] = {0, 0};  // split-K factor override per mode (0 = automatic)
+  int ov_stages = 0;          // pipeline stage override (0 = as many as fit)
   alignas(64) unsigned char tm_xh_m[128];
   alignas(64) unsigned char tm_xl_m[128];
   alignas(64) unsigned char tm_xh_n[128];
@@ -31,6 +34,12 @@ bool tc_pass_supported(int64_t n, int64_t m, int R);
 // Allocates the split buffers and partials and encodes their tensor maps.
 cudaError_t tc_pass_init(TcPass* t, int64_t n, int64_t m, int R);
 void tc_pass_free(TcPass* t);
+
+// Tile overrides of the autotuner: K splits per 128-row output tile for
+// dY X (splits_rows) and dY^T X (splits_cols), pipeline stages (2 up to what
+// fits); 0 restores the automatic choice.  Grows the partial buffer when
+// needed.
+cudaError_t tc_pass_set_tiles(TcPass* t, int splits_rows, int splits_cols, int stages);
 
 // out (P x R, ld ldo) = dY X (trans = 0: P = n, X is m x R with ld ldx) or
 // dY^T X (trans = 1: P = m, X is n x R), dY = A1 - A0 (n x m, column-major,
