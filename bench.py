@@ -157,6 +157,23 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
+def _oracle_finals(args):
+    """The oracle's factors (dense) after `steps` steps of each instance."""
+    idx, steps = args
+    import workloads
+    from oracle import lri_oracle as O
+    out = []
+    for i in idx:
+        e = workloads.lyapunov_ensemble(first=i, limit=1)[0]
+        p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
+                              (0.0, DT * steps))
+        integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
+        for _ in range(steps):
+            O.step(integ, integ.alg, DT)
+        out.append((i, integ.u.full()))
+    return out
+
+
 def cpu_baseline(count, sample_every, steps, warmup=0, cores=None):
     """The oracle on every `sample_every`-th instance of the ensemble, one
     process per host core: `warmup` untimed steps, then `steps` timed steps
@@ -703,6 +720,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=None, help="plain FP64 steps timed (default: all)")
     ap.add_argument("--cpu-sample-every", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--oracle-sample", type=int, default=64, help="ensemble instances checked against the oracle")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--adjoint", action="store_true",
                     help="instead of the ensemble: the adjoint workload (loss + gradient, FD check)")
@@ -857,19 +875,23 @@ def main():
     # ---------------- accuracy vs the CPU oracle on a sample -----------------
     oracle_err = None
     if rank == 0:
+        # every 64th instance (64 of 4096), the oracle's full trajectory of
+        # W + K steps, one spawned process per host core
+        sample = list(range(0, args.count, max(1, args.count // args.oracle_sample)))[:args.oracle_sample]
+        cores = os.cpu_count() or 1
+        chunks = [c for c in (sample[k::cores] for k in range(cores)) if c]
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(len(chunks), initializer=_pool_init) as pool:
+            finals = pool.map(_oracle_finals, [(c, W + K) for c in chunks])
+        wall = time.perf_counter() - t0
+        ref = {i: Y for part in finals for i, Y in part}
         from oracle import lri_oracle as O
-        sample = list(range(0, args.count, max(1, args.count // 8)))[:8]
-        em, e64 = [], []
-        for i in sample:
-            e = insts[i]
-            p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
-                                  (0.0, DT * (W + K)))
-            integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
-            for _ in range(W + K):
-                O.step(integ, integ.alg, DT)
-            em.append(O.rel_fro_err(ymix[i].full(), integ.u.full()))
-            e64.append(O.rel_fro_err(y64[i].full(), integ.u.full()))
-        oracle_err = {"instances": sample, "mixed_max": float(max(em)), "fp64_max": float(max(e64))}
+        em = [O.rel_fro_err(ymix[i].full(), ref[i]) for i in sample]
+        e64 = [O.rel_fro_err(y64[i].full(), ref[i]) for i in sample]
+        oracle_err = {"instances": len(sample), "every": max(1, args.count // args.oracle_sample),
+                      "mixed_max": float(max(em)), "mixed_median": float(np.median(em)),
+                      "mixed_above_1e-5": int(sum(e > 1e-5 for e in em)), "fp64_max": float(max(e64)),
+                      "oracle_wall_s": wall}
 
     # ---------------- e2e through the public API with host buffers -----------------
     e2e = None

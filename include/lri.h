@@ -298,6 +298,12 @@ LRI_API lri_status lri_stream_bind(lri_stream* s, void* U, void* S, void* V);
 /* One step from snapshot A_prev = A(t) to A_next = A(t+dt) (device, n x m,
  * column-major, dtype of the stream). */
 LRI_API lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void* A_next, void* stream);
+/* GreedyIntegrator step on the stream's bound SVD-like factors
+ * (greedy_integrator.jl:96-104): with X = A_next = y(t+dt) (n x m, the
+ * stream's dtype), U = orthonormal basis of X V, V = orthonormal basis of
+ * X^T U, S = U^T X V with the new bases; the rank stays.  Three passes over
+ * the single snapshot (tensor cores for FP32 streams as above). */
+LRI_API lri_status lri_stream_greedy_step(lri_stream* s, const void* A_next, void* stream);
 LRI_API lri_status lri_stream_rank(lri_stream* s, int64_t* r_out, void* stream);
 LRI_API lri_status lri_stream_status(lri_stream* s, void* stream);
 

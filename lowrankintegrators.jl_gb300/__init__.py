@@ -1116,6 +1116,11 @@ class DataStreamEngine:
         _native.check(self.lib.lri_stream_step(self.handle, C.c_void_p(A_prev.data_ptr()),
                                                C.c_void_p(A_next.data_ptr()), self._stream()), "lri_stream_step")
 
+    def greedy_step(self, A_next):
+        """GreedyIntegrator step to the snapshot A_next (fixed rank)."""
+        _native.check(self.lib.lri_stream_greedy_step(self.handle, C.c_void_p(A_next.data_ptr()), self._stream()),
+                      "lri_stream_greedy_step")
+
     def set_tensor_cores(self, enable: bool):
         """Selects the tensor-core (3xTF32) or CUDA-core snapshot passes."""
         _native.check(self.lib.lri_stream_set_tensor_cores(self.handle, int(bool(enable))),
@@ -1173,23 +1178,31 @@ class DataStreamEngine:
             pass
 
 
-def solve_stream(prob: MatrixDataProblem, alg: RankAdaptiveUnconventionalAlgorithm, precision: str = "fp32",
+def solve_stream(prob: MatrixDataProblem, alg, precision: str = "fp32",
                  save_everystep: bool = True) -> DLRSolution:
     """solve(prob, alg) (src/primitives.jl:68-80) for a MatrixDataProblem given
     as a list of snapshots, on the large-stream engine: rank-adaptive BUG,
-    one step per consecutive pair of snapshots."""
+    one step per consecutive pair of snapshots, or the GreedyIntegrator
+    (fixed rank, one refit per snapshot)."""
     if callable(prob.y):
         raise ValueError("the stream engine takes a list of snapshots")
     u0 = prob.u0
     n, m = u0.U.shape[0], u0.V.shape[0]
-    eng = DataStreamEngine(n, m, u0.S.shape[0], min(alg.rmax, 96), alg.tol, alg.rmin, precision)
+    greedy = isinstance(alg, GreedyIntegrator)
+    if greedy:
+        eng = DataStreamEngine(n, m, u0.S.shape[0], u0.S.shape[0], 0.0, 1, precision)
+    else:
+        eng = DataStreamEngine(n, m, u0.S.shape[0], min(alg.rmax, 96), alg.tol, alg.rmin, precision)
     try:
         eng.bind(u0)
         sol = DLRSolution([u0.copy()], [float(prob.tspan[0])])
         prev = eng.to_device(prob.y[0])
         for k in range(1, len(prob.y)):
             nxt = eng.to_device(prob.y[k])
-            eng.step(prev, nxt)
+            if greedy:
+                eng.greedy_step(nxt)
+            else:
+                eng.step(prev, nxt)
             prev = nxt
             if save_everystep:
                 eng.check_status()

@@ -32,7 +32,7 @@ EXPORTED = [
     "lri_batch_prepare", "lri_batch_adjoint_prepare", "lri_batch_adjoint_step",
     "lri_stream_create", "lri_stream_destroy", "lri_stream_bind", "lri_stream_step", "lri_stream_rank",
     "lri_stream_status", "lri_stream_set_tensor_cores", "lri_stream_uses_tensor_cores", "lri_stream_data_product",
-    "lri_stream_set_pass_tiles", "lri_batch_set_occupancy",
+    "lri_stream_set_pass_tiles", "lri_batch_set_occupancy", "lri_stream_greedy_step",
     "lri_burgers_create", "lri_burgers_bind", "lri_burgers_step",
     "lri_history_create", "lri_history_destroy", "lri_history_record", "lri_history_wait",
 ]
@@ -111,6 +111,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.lri_stream_status.argtypes = [P, P]
     lib.lri_stream_set_tensor_cores.restype = C.c_int
     lib.lri_stream_set_tensor_cores.argtypes = [P, C.c_int32]
+    lib.lri_stream_greedy_step.restype = C.c_int
+    lib.lri_stream_greedy_step.argtypes = [P, P, P]
     lib.lri_stream_set_pass_tiles.restype = C.c_int
     lib.lri_stream_set_pass_tiles.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.lri_batch_set_occupancy.restype = C.c_int

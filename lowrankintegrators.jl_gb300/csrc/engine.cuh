@@ -1689,9 +1689,13 @@ __device__ void extract_r(const T* A, int lda, int W, T* R, int ldr) {
 // iteration also ends after a sweep with delta <= conv_delta (default
 // sqrt(eps): P delta^2 is then the rotation threshold itself) instead of
 // spending one more sweep to find nothing to rotate.
-// tiny_abs raises the noise level below which columns are left alone to an
-// absolute squared norm (the caller's truncation level: columns that
-// truncation drops whatever their directions).
+// tiny_abs (the caller's truncation level, an absolute squared norm): a pair
+// whose columns are BOTH below it is left alone -- together they hold less
+// than the truncation drops, and the SVD of the rest is unaffected.  (A rule
+// that skipped pairs with EITHER column below it would let a column that
+// shrank below the level keep content the exact SVD rotates into the kept
+// columns: the truncated result could then differ from the truncated exact
+// SVD by up to tol / 2.)
 template <typename T, int NTH = NT>
 __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, int* flag, int max_sweeps = 40,
                                         bool skip_noise = true, double conv_delta = -1.0, double tiny_abs = 0.0) {
@@ -1716,8 +1720,8 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
   fro2 = T(0);
   for (int wv = 0; wv < NWJ; ++wv) fro2 += red[wv];
   __syncthreads();
-  T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
-  if (T(tiny_abs) > tiny) tiny = T(tiny_abs);
+  const T tiny = T(Prec<T>::eps) * T(Prec<T>::eps) * fro2;
+  const T reach = T(tiny_abs);  // truncation level: a pair is left alone only when both columns are below it
   const int Pe = P + (P & 1);  // even number of players (a dummy when P is odd)
   // lanes per pair G (32, 16, 8 or 4): enough pairs per pass for every warp,
   // so the per-pair reductions and rotation arithmetic are shared by a warp's
@@ -1762,7 +1766,8 @@ __device__ __noinline__ bool jacobi_svd(int P, T* a, T* v, T* sigma, int* perm, 
           ga += shfl_xor(ga, o);
         }
         // (sqrt(al) * sqrt(be): al * be can leave the FP32 exponent range)
-        const bool live = valid && (skip_noise ? (al > tiny && be > tiny) : (al > tiny || be > tiny));
+        const bool live = valid && (skip_noise ? (al > tiny && be > tiny && (al > reach || be > reach))
+                                               : (al > tiny || be > tiny));
         if (live && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
           const T zeta = (be - al) / (T(2) * ga);
           // for large |zeta| use tan = 1/(2 zeta): zeta^2 would leave the FP32

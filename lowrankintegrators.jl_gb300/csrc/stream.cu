@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) pass_rows(int n, int m, int R, int aug, c
       T v = T(0);
       if (i < n && j < m) {
         const int64_t o = (int64_t)i + (int64_t)j * n;
-        v = A1[o] - A0[o];
+        v = A0 ? A1[o] - A0[o] : A1[o];  // no A0: the snapshot itself
       }
       ds[jj][ii] = v;
     }
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256) pass_cols(int n, int m, int R, const int3
       T v = T(0);
       if (i < n && j < m) {
         const int64_t o = (int64_t)i + (int64_t)j * n;
-        v = A1[o] - A0[o];
+        v = A0 ? A1[o] - A0[o] : A1[o];  // no A0: the snapshot itself
       }
       ds[jj][ii] = v;
     }
@@ -741,14 +741,11 @@ __global__ void __launch_bounds__(NTS) core_step(int R, const double* __restrict
   ST* v = vg;  // wa x wa
   for (int o = tid; o < wa * wa; o += NTS) a[o] = ST(F[o]);
   __syncthreads();
-  // FP32 panels: the sweeps leave pairs with a column of squared norm <= tol^2
-  // / (4 wa) alone.  Such columns together hold less than tol^2 / 4, so the
-  // truncated result stays within tol / 2 of S~; but a column can shrink
-  // below that level while still holding content the exact SVD would rotate
-  // into the kept columns, so the result then differs from the truncated
-  // exact SVD by up to tol / 2 (measured 4e-7 relative on a rank-90 stream,
-  // inside the FP32 step's accuracy).  FP64 panels exist for parity with the
-  // reference: exact rules there.
+  // FP32 panels: the sweeps leave alone pairs whose columns both have squared
+  // norm <= tol^2 / (4 wa).  Such columns together hold less than tol^2 / 4
+  // and are rotated against every larger column, so the kept singular
+  // directions are those of the exact SVD.  FP64 panels exist for parity with
+  // the reference: no truncation-level skip there.
   const double tiny_abs = std::is_same<ST, double>::value ? 0.0 : tol * tol / (4.0 * wa);
   bool ok;
   if constexpr (sizeof(ST) == 8 && !std::is_same<ST, double>::value) {
@@ -1396,6 +1393,16 @@ __global__ void small_to_f64(int R, const T* __restrict__ X, int trans, double* 
 }
 
 // S~0 (w x w) = Mh S0 Nh^T with Mh, Nh (w x R), S0 (R x R, FP64)
+// S (R x R, T) = the active r x r block of B (FP64, ld R), zeros elsewhere
+template <typename T>
+__global__ void store_core(int R, const int32_t* __restrict__ rank, const double* __restrict__ B, T* __restrict__ S) {
+  const int r = min(R, (int)*rank);
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < R * R; o += gridDim.x * blockDim.x) {
+    const int i = o % R, j = o / R;
+    S[o] = (i < r && j < r) ? T(B[o]) : T(0);
+  }
+}
+
 __global__ void small_msn(int w, int R, const double* __restrict__ Mh, const double* __restrict__ S0,
                           const double* __restrict__ Nh, double* __restrict__ tmp, double* __restrict__ out) {
   for (int o = threadIdx.x; o < R * w; o += blockDim.x) {
@@ -1606,13 +1613,14 @@ struct StreamOps {
   // panels two Newton-Schulz steps X <- X (3I - X^T X) / 2 (E -> ~E^2, below
   // FP32 rounding after two; whole-GPU Grams and products only), for FP64
   // panels one CholeskyQR pass.  Zero columns stay zero either way.
+  // (Y0 null: a plain orthonormal basis of X, no projections)
   cudaError_t orth_against(int N, T* X, const T* Y0) const {
     const int R = (int)s->R;
-    cudaError_t e = project_out(N, X, Y0);
-    if (e == cudaSuccess) e = project_out(N, X, Y0);
+    cudaError_t e = Y0 ? project_out(N, X, Y0) : cudaSuccess;
+    if (e == cudaSuccess && Y0) e = project_out(N, X, Y0);
     const int npass = std::is_same<T, float>::value ? 3 : 2;
     for (int pass = 0; pass < npass && e == cudaSuccess; ++pass) {
-      if (pass == 1) e = project_out(N, X, Y0);
+      if (pass == 1 && Y0) e = project_out(N, X, Y0);
       if (e == cudaSuccess) e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);         // G = X^T X
       if (e == cudaSuccess) {
         if (pass == 0) e = pchol(R, blk(1), blk(2));
@@ -1869,6 +1877,38 @@ struct StreamOps {
     return cudaGetLastError();
   }
 
+  // GreedyIntegrator on the snapshot A = y(t + dt) (greedy_integrator.jl:
+  // 96-104): U = orth(A V), V = orth(A^T U), S = U^T A V with the new bases;
+  // three single-snapshot passes, the rank is kept.
+  cudaError_t greedy_step(const T* A) const {
+    const int n = (int)s->n, m = (int)s->m, R = (int)s->R;
+    T* U = tp(s->U);
+    T* V = tp(s->V);
+    T* Xk = tp(s->Xk);
+    T* Xl = tp(s->Xl);
+    T* Z = tp(s->Zp);
+    const bool tc = tc_selected();
+    cudaError_t e = cudaSuccess;
+    auto prod = [&](int trans, const T* X, T* out) {
+      if (tc) return tc_run(trans, A, nullptr, X, trans ? n : m, out, trans ? m : n, nullptr);
+      if (trans)
+        pass_cols<T><<<(m + 15) / 16, 256, 0, st>>>(n, m, R, s->d_rank, A, nullptr, X, n, out);
+      else
+        pass_rows<T><<<(n + 31) / 32, 256, 0, st>>>(n, m, R, 0, s->d_rank, A, nullptr, X, m, out);
+      return cudaGetLastError();
+    };
+    if ((e = prod(0, V, Xk)) != cudaSuccess) return e;   // A V
+    if ((e = prod(1, U, Xl)) != cudaSuccess) return e;   // A^T U
+    if ((e = orth_against(n, Xk, nullptr)) != cudaSuccess) return e;
+    if ((e = orth_against(m, Xl, nullptr)) != cudaSuccess) return e;
+    copy_cols<T><<<304, 256, 0, st>>>(n, R, Xk, n, U, n);
+    copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, V, m);
+    if ((e = prod(0, V, Z)) != cudaSuccess) return e;    // A V with the new V
+    if ((e = gram(n, R, R, U, n, Z, n, 1.0, 0.0, blk(0), R)) != cudaSuccess) return e;
+    store_core<T><<<16, 256, 0, st>>>(R, s->d_rank, blk(0), tp(s->S));
+    return cudaGetLastError();
+  }
+
   cudaError_t step(const T* A0, const T* A1) const {
     const int n = (int)s->n, m = (int)s->m, R = (int)s->R, w = 2 * R;
     T* U = tp(s->U);
@@ -2119,6 +2159,18 @@ lri_status lri_stream_step(lri_stream* s, const void* A_prev, const void* A_next
     e = StreamOps<float>{s, st}.step(static_cast<const float*>(A_prev), static_cast<const float*>(A_next));
   else
     e = StreamOps<double>{s, st}.step(static_cast<const double*>(A_prev), static_cast<const double*>(A_next));
+  return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
+}
+
+lri_status lri_stream_greedy_step(lri_stream* s, const void* A_next, void* stream) {
+  if (!s || s->burgers || !A_next) return LRI_ERR_ARG;
+  if (!s->bound) return LRI_ERR_STATE;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (s->dtype == LRI_F32)
+    e = StreamOps<float>{s, st}.greedy_step(static_cast<const float*>(A_next));
+  else
+    e = StreamOps<double>{s, st}.greedy_step(static_cast<const double*>(A_next));
   return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
 }
 

@@ -68,6 +68,7 @@ constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
 
 struct TcArgs {
   int P, R, NB, nchunks, chunks_per_split, stages, rows_mode, ncols;
+  int has_a0;  // 0: the product of the snapshot A1 itself (no A0 tile is loaded)
   const int32_t* rank;
   float* part;
   uint32_t* status;
@@ -270,13 +271,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (!(ok = mbar_wait(empty(s), par ^ 1u, abort_flag, a))) break;
         const int kc = kc0 + it;
         const uint32_t st = smem_u32(base + (size_t)s * stage_bytes);
-        mbar_expect_tx(full(s), stage_bytes);
+        mbar_expect_tx(full(s), a.has_a0 ? stage_bytes : stage_bytes - TC_TILE_BYTES);
         if (a.rows_mode) {
           tma_load_2d(st, &tmA1, mt * TC_BM, kc * TC_BK, full(s));
-          tma_load_2d(st + TC_TILE_BYTES, &tmA0, mt * TC_BM, kc * TC_BK, full(s));
+          if (a.has_a0) tma_load_2d(st + TC_TILE_BYTES, &tmA0, mt * TC_BM, kc * TC_BK, full(s));
         } else {
           tma_load_2d(st, &tmA1, kc * TC_BK, mt * TC_BM, full(s));
-          tma_load_2d(st + TC_TILE_BYTES, &tmA0, kc * TC_BK, mt * TC_BM, full(s));
+          if (a.has_a0) tma_load_2d(st + TC_TILE_BYTES, &tmA0, kc * TC_BK, mt * TC_BM, full(s));
         }
         tma_load_2d(st + 2 * TC_TILE_BYTES, &tmXh, kc * TC_BK, 0, full(s));
         tma_load_2d(st + 2 * TC_TILE_BYTES + xbytes, &tmXl, kc * TC_BK, 0, full(s));
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // tile rows j (32) of 128 contiguous i; operand row i = this thread
         float d[TC_BK];
 #pragma unroll
-        for (int j = 0; j < TC_BK; ++j) d[j] = a1[j * TC_BM + tid] - a0[j * TC_BM + tid];
+        for (int j = 0; j < TC_BK; ++j) d[j] = a.has_a0 ? a1[j * TC_BM + tid] - a0[j * TC_BM + tid] : a1[j * TC_BM + tid];
         bar_any(false);  // every thread has read its column before the tile is overwritten
         unsigned char* h8 = reinterpret_cast<unsigned char*>(a1);
         unsigned char* l8 = reinterpret_cast<unsigned char*>(a0);
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int u = 0; u < (TC_BM * TC_BK / 4) / 128; ++u) {
           const int q = tid + 128 * u;
-          const float4 x1 = p1[q], x0 = p0[q];
+          const float4 x1 = p1[q], x0 = a.has_a0 ? p0[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
           float4 h, l;
           split(x1.x - x0.x, h.x, l.x);
           split(x1.y - x0.y, h.y, l.y);
@@ -580,6 +581,8 @@ cudaError_t tc_pass_run(TcPass* t, int trans, const float* A1, const float* A0, 
                         const int32_t* rank, int ncols, float* out, int64_t ldo, float* kd, uint32_t* status,
                         uint32_t status_timeout, cudaStream_t st) {
   if ((reinterpret_cast<uintptr_t>(A1) | reinterpret_cast<uintptr_t>(A0)) & 15) return cudaErrorInvalidValue;
+  const bool has_a0 = A0 != nullptr;
+  if (!has_a0) A0 = A1;  // a valid tensor map; its tile is never loaded
   const int64_t n = t->n, m = t->m;
   const bool rows_mode = (trans == 0);
   const int64_t P = rows_mode ? n : m, K = rows_mode ? m : n;
@@ -604,6 +607,7 @@ cudaError_t tc_pass_run(TcPass* t, int trans, const float* A1, const float* A0, 
   a.chunks_per_split = pl.cps;
   a.stages = stages;
   a.rows_mode = rows_mode ? 1 : 0;
+  a.has_a0 = has_a0 ? 1 : 0;
   a.ncols = ncols;
   a.rank = rank;
   a.part = t->part;

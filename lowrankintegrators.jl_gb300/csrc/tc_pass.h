@@ -42,7 +42,7 @@ void tc_pass_free(TcPass* t);
 cudaError_t tc_pass_set_tiles(TcPass* t, int splits_rows, int splits_cols, int stages);
 
 // out (P x R, ld ldo) = dY X (trans = 0: P = n, X is m x R with ld ldx) or
-// dY^T X (trans = 1: P = m, X is n x R), dY = A1 - A0 (n x m, column-major,
+// dY^T X (trans = 1: P = m, X is n x R), dY = A1 - A0 (A0 may be null: dY = A1) (n x m, column-major,
 // 16-byte aligned).  Active columns: ncols when >= 0, else the device rank
 // (capped at R); the others are written as zeros.  kd (optional, P x R,
 // ld P) receives a copy of out.  A bounded wait that gives up ORs

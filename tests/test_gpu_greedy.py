@@ -121,3 +121,27 @@ def test_greedy_rejects_svd_like_without_data(lri):
     prob = lri.MatrixDEProblem(lri.ZeroOperator(), Y0, (0.0, 1.0))
     with pytest.raises(lri.LriError):
         lri.solve(prob, lri.GreedyIntegrator(), 0.5)
+
+
+@pytest.mark.parametrize("precision,tc,tol", [("fp64", False, 1e-10), ("fp32", True, 1e-5), ("fp32", False, 1e-5)])
+def test_greedy_on_stream_engine_matches_oracle(lri, oracle, precision, tc, tol):
+    """The large-stream engine's greedy step (single-snapshot passes on the
+    tensor or CUDA cores, orthonormal bases by pivoted Cholesky + Newton-Schulz
+    or CholeskyQR) against the oracle's Householder-based greedy step,
+    through Y = U S V^T."""
+    snaps = workloads.data_stream(1024, 512, 6, seed=12)
+    Y0 = oracle.truncated_svd(snaps[0], r=12)
+    so = oracle.solve(oracle.MatrixDataProblem(snaps, Y0), oracle.GreedyIntegrator())
+    eng = lri.DataStreamEngine(1024, 512, 12, 12, 0.0, 1, precision)
+    try:
+        if precision == "fp32":
+            eng.set_tensor_cores(tc)
+        eng.bind(lri.SVDLikeRepresentation(Y0.U, Y0.S, Y0.V))
+        for k in range(1, len(snaps)):
+            eng.greedy_step(eng.to_device(snaps[k]))
+            eng.check_status()
+            yg = eng.download()
+            err = oracle.rel_fro_err(yg.full(), so.Y[k].full())
+            assert err <= tol, f"snapshot {k}: {err:.3e}"
+    finally:
+        eng.close()
