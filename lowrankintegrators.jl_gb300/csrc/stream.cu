@@ -1383,6 +1383,223 @@ __global__ void s_stage_finish(int R, const int32_t* __restrict__ rank, int nz, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fused RK stages of the Burgers flows for small active widths (ka <= 32).
+// At low rank each stage of the K, L and S substep flows is row-local work
+// on an n x ka panel plus small matrices (N_nu, A_xx, Z) and the packed flow
+// tensor T' (np x ka, np = ka (ka + 1) / 2 pairs), all of which fit in shared
+// memory; one kernel per stage replaces the stencil, panel product,
+// Khatri-Rao and combine launches above (same arithmetic per entry, sums in
+// a different order).  One CTA per FUSED_BM rows, with one periodic halo row
+// on each side for the stencils and the Dx of the quadratic term.
+// ---------------------------------------------------------------------------
+constexpr int FUSED_BM = 32;
+constexpr int FUSED_KMAX = 32;
+
+// sum_{a <= b} KR(P, Q)_ab T'[p(a,b), c] with KR(P, Q)_ab = (P_a Q_b + P_b Q_a) / 2
+// (P == Q: P_a P_b), T' at tps[p * ka + c]
+template <typename T>
+__device__ __forceinline__ T kr_dot(int ka, const T* P, const T* Q, const T* tps, int c, bool same) {
+  T acc = T(0);
+  int p = 0;
+  for (int a = 0; a < ka; ++a) {
+    T g1 = T(0), g2 = T(0);
+    for (int b = a; b < ka; ++b, ++p) {
+      const T t = tps[p * ka + c];
+      g1 = fma(Q[b], t, g1);
+      if (!same) g2 = fma(P[b], t, g2);
+    }
+    acc = same ? fma(P[a], g1, acc) : fma(T(0.5), fma(P[a], g1, Q[a] * g2), acc);
+  }
+  return acc;
+}
+
+// loads the packed tensor's active block: tps[p * ka + c] = Tp[p + c PP]
+template <typename T>
+__device__ __forceinline__ void load_tensor(int ka, const T* __restrict__ Tp, int PP, T* tps) {
+  const int np = ka * (ka + 1) / 2;
+  for (int e = threadIdx.x; e < np * ka; e += blockDim.x) {
+    const int pp = e % np, c = e / np;
+    tps[pp * ka + c] = Tp[pp + (int64_t)c * PP];
+  }
+}
+
+// K substep stage: v = (ih2 Dxx Z) N_nu + alpha KR(Dx Z, Z) T'_V + beta Dx(KR(Z, Z) T'_V),
+// Dx = ihx (shift - shift) on the active columns (zero elsewhere), then the RK update.
+template <typename T>
+__global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32_t* __restrict__ rank,
+                                                       const T* __restrict__ Z, const double* __restrict__ Nnu,
+                                                       const T* __restrict__ Tp, int PP, double ih2, double ihx,
+                                                       double alpha, double beta, uint32_t* status, RkStage<T> rk) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ka = min(R, (int)*rank);
+  if (ka > FUSED_KMAX) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
+    return;
+  }
+  const int np = ka * (ka + 1) / 2;
+  const bool nonlin = (alpha != 0.0 || beta != 0.0);
+  T* tps = reinterpret_cast<T*>(smraw);            // np x ka
+  T* zs = tps + (nonlin ? np * ka : 0);             // (BM + 2) x ka: rows i0 - 1 .. i0 + BM
+  T* ks = zs + (FUSED_BM + 2) * ka;                 // (BM + 2) x ka: KR(Z, Z) T'
+  T* ns = ks + (FUSED_BM + 2) * ka;                 // ka x ka: N_nu
+  T* d1 = ns + ka * ka;                             // BM x ka: Dx Z
+  const int i0 = blockIdx.x * FUSED_BM;
+  if (nonlin) load_tensor(ka, Tp, PP, tps);
+  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
+    const int ii = e / ka, a = e % ka;
+    int g = i0 - 1 + ii;
+    g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
+    zs[e] = Z[g + (int64_t)a * N];
+  }
+  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) ns[e] = T(Nnu[(e % ka) + (int64_t)(e / ka) * R]);
+  __syncthreads();
+  if (beta != 0.0)
+    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
+      const int ii = e / ka, c = e % ka;
+      ks[e] = kr_dot(ka, zs + ii * ka, zs + ii * ka, tps, c, true);
+    }
+  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
+    const int ii = e / ka, a = e % ka;
+    d1[e] = T(ihx) * (zs[(ii + 2) * ka + a] - zs[ii * ka + a]);
+  }
+  __syncthreads();
+  const int rows = min(FUSED_BM, N - i0);
+  for (int e = threadIdx.x; e < FUSED_BM * R; e += blockDim.x) {
+    const int ii = e % FUSED_BM, c = e / FUSED_BM;
+    if (ii >= rows) continue;
+    T v = T(0);
+    if (c < ka) {
+      const T* zm = zs + ii * ka;
+      const T* z0 = zm + ka;
+      const T* zp = z0 + ka;
+      for (int a = 0; a < ka; ++a) {
+        const T d2 = T(ih2) * ((zm[a] + zp[a]) - T(2) * z0[a]);
+        v = fma(d2, ns[a + c * ka], v);
+      }
+      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ka, z0, tps, c, false), v);
+      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ka + c] - ks[ii * ka + c], v);
+    }
+    rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, v);
+  }
+}
+
+// L substep stage: v[j, c] = nu_j (Z A_xx)[j, c] + KR(Z, Z)_j T'_L[:, c], then the RK update.
+template <typename T>
+__global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32_t* __restrict__ rank,
+                                                       const T* __restrict__ Z, const T* __restrict__ nu,
+                                                       const double* __restrict__ Axx, const T* __restrict__ Tp,
+                                                       int PP, int nonlin, uint32_t* status, RkStage<T> rk) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ka = min(R, (int)*rank);
+  if (ka > FUSED_KMAX) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
+    return;
+  }
+  const int np = ka * (ka + 1) / 2;
+  T* tps = reinterpret_cast<T*>(smraw);
+  T* zs = tps + (nonlin ? np * ka : 0);   // BM x ka
+  T* as = zs + FUSED_BM * ka;             // ka x ka: A_xx
+  const int j0 = blockIdx.x * FUSED_BM;
+  const int rows = min(FUSED_BM, M - j0);
+  if (nonlin) load_tensor(ka, Tp, PP, tps);
+  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
+    const int jj = e / ka, a = e % ka;
+    zs[e] = (jj < rows) ? Z[(j0 + jj) + (int64_t)a * M] : T(0);
+  }
+  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) as[e] = T(Axx[(e % ka) + (int64_t)(e / ka) * R]);
+  __syncthreads();
+  for (int e = threadIdx.x; e < FUSED_BM * R; e += blockDim.x) {
+    const int jj = e % FUSED_BM, c = e / FUSED_BM;
+    if (jj >= rows) continue;
+    T v = T(0);
+    if (c < ka) {
+      const T* z = zs + jj * ka;
+      T lin = T(0);
+      for (int a = 0; a < ka; ++a) lin = fma(z[a], as[a + c * ka], lin);
+      v = nu[j0 + jj] * lin;
+      if (nonlin) v += kr_dot(ka, z, z, tps, c, true);
+    }
+    rk_apply(rk, (int64_t)(j0 + jj) + (int64_t)c * M, v);
+  }
+}
+
+// S substep stage, row part: with A = Uhat Z (N x ka on the active columns
+// of the augmented panel), P2 = alpha KR(Dx A, A) T'_h + beta Dx(KR(A, A) T'_h)
+// and this CTA's partial of Uhat^T P2 (ka x ka, FP64 at the active indices
+// of part[blockIdx.x], ld 2R).  s_stage_finish adds the partials.
+template <typename T>
+__global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_t* __restrict__ rank,
+                                                      const T* __restrict__ Uh, const double* __restrict__ Zs,
+                                                      const T* __restrict__ Tp, int PP, double ihx, double alpha,
+                                                      double beta, uint32_t* status, double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
+  if (ka > FUSED_KMAX) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
+    return;
+  }
+  const int np = ka * (ka + 1) / 2;
+  T* tps = reinterpret_cast<T*>(smraw);        // np x ka
+  T* us = tps + np * ka;                       // (BM + 2) x ka: Uhat rows i0 - 1 .. i0 + BM
+  T* zm = us + (FUSED_BM + 2) * ka;            // ka x ka: Z
+  T* as = zm + ka * ka;                        // (BM + 2) x ka: A rows
+  T* ks = as + (FUSED_BM + 2) * ka;            // (BM + 2) x ka: KR(A, A) T'
+  T* d1 = ks + (FUSED_BM + 2) * ka;            // BM x ka: Dx A
+  T* p2 = d1 + FUSED_BM * ka;                  // BM x ka: P2
+  const int i0 = blockIdx.x * FUSED_BM;
+  const int rows = min(FUSED_BM, N - i0);
+  load_tensor(ka, Tp, PP, tps);
+  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
+    const int ii = e / ka, a = e % ka;
+    int g = i0 - 1 + ii;
+    g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
+    us[e] = Uh[g + (int64_t)act_col(a, r, R) * N];
+  }
+  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x)
+    zm[e] = T(Zs[act_col(e % ka, r, R) + (int64_t)act_col(e / ka, r, R) * w]);
+  __syncthreads();
+  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {  // A = Uhat Z
+    const int ii = e / ka, c = e % ka;
+    T acc = T(0);
+    for (int k = 0; k < ka; ++k) acc = fma(us[ii * ka + k], zm[k + c * ka], acc);
+    as[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
+    const int ii = e / ka, c = e % ka;
+    if (beta != 0.0) ks[e] = kr_dot(ka, as + ii * ka, as + ii * ka, tps, c, true);
+    if (ii < FUSED_BM) d1[e] = T(ihx) * (as[(ii + 2) * ka + c] - as[ii * ka + c]);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
+    const int ii = e / ka, c = e % ka;
+    T v = T(0);
+    if (ii < rows) {
+      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ka, as + (ii + 1) * ka, tps, c, false), v);
+      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ka + c] - ks[ii * ka + c], v);
+    }
+    p2[e] = v;
+  }
+  __syncthreads();
+  double* dst = part + (int64_t)blockIdx.x * w * w;
+  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {  // Uhat^T P2 over the tile's rows
+    const int a = e % ka, c = e / ka;
+    T acc = T(0);
+    for (int ii = 0; ii < rows; ++ii) acc = fma(us[(ii + 1) * ka + a], p2[ii * ka + c], acc);
+    dst[act_col(a, r, R) + (int64_t)act_col(c, r, R) * w] = (double)acc;
+  }
+}
+
+// dynamic shared memory of the fused stages at the largest width (FUSED_KMAX)
+template <typename T>
+size_t fused_smem(int which) {
+  const size_t K = FUSED_KMAX, np = K * (K + 1) / 2, B = FUSED_BM;
+  if (which == 0) return sizeof(T) * (np * K + 2 * (B + 2) * K + K * K + B * K);
+  if (which == 1) return sizeof(T) * (np * K + B * K + K * K);
+  return sizeof(T) * (np * K + 3 * (B + 2) * K + K * K + 2 * B * K);
+}
+
 // small FP64 helpers of the S step: X (R x R, T, ld R) -> Y (FP64, ld R), optionally transposed
 template <typename T>
 __global__ void small_to_f64(int R, const T* __restrict__ X, int trans, double* __restrict__ Y) {
@@ -1392,7 +1609,6 @@ __global__ void small_to_f64(int R, const T* __restrict__ X, int trans, double* 
   }
 }
 
-// S~0 (w x w) = Mh S0 Nh^T with Mh, Nh (w x R), S0 (R x R, FP64)
 // S (R x R, T) = the active r x r block of B (FP64, ld R), zeros elsewhere
 template <typename T>
 __global__ void store_core(int R, const int32_t* __restrict__ rank, const double* __restrict__ B, T* __restrict__ S) {
@@ -1403,6 +1619,7 @@ __global__ void store_core(int R, const int32_t* __restrict__ rank, const double
   }
 }
 
+// S~0 (w x w) = Mh S0 Nh^T with Mh, Nh (w x R), S0 (R x R, FP64)
 __global__ void small_msn(int w, int R, const double* __restrict__ Mh, const double* __restrict__ S0,
                           const double* __restrict__ Nh, double* __restrict__ tmp, double* __restrict__ out) {
   for (int o = threadIdx.x; o < R * w; o += blockDim.x) {
@@ -1520,8 +1737,13 @@ struct lri_stream {
   // one captured Burgers step (launch shapes depend on r_max only; the rank
   // is read on the device), replayed while dt and the bound factors stay
   cudaStream_t cap = nullptr;
-  cudaGraphExec_t step_exec = nullptr;
-  double graph_dt = 0.0;
+  cudaGraphExec_t step_exec[3] = {nullptr, nullptr, nullptr};  // one per fused class
+  double graph_dt[3] = {0.0, 0.0, 0.0};
+  bool class_seen[3] = {false, false, false};
+  // fused RK-stage kernels for the current rank: 0 none (rank > 32), 1 the K
+  // and L stages (rank <= 32), 2 also the S stage (rank <= 16)
+  int fused = 0;
+  double* fgp = nullptr;  // the fused S stage's per-tile partials: ceil(n / 32) x (2R)^2 FP64
 };
 
 
@@ -1748,6 +1970,12 @@ struct StreamOps {
     const int g = 304;
     cudaError_t e = refresh();
     if (e != cudaSuccess) return e;
+    if (s->fused) {
+      static std::atomic<uint64_t> a0{0}, a1{0}, a2{0};
+      if ((e = set_smem_limit(burgers_k_stage<T>, (int)fused_smem<T>(0), a0)) != cudaSuccess) return e;
+      if ((e = set_smem_limit(burgers_l_stage<T>, (int)fused_smem<T>(1), a1)) != cudaSuccess) return e;
+      if ((e = set_smem_limit(burgers_s_rows<T>, (int)fused_smem<T>(2), a2)) != cudaSuccess) return e;
+    }
     small_to_f64<T><<<16, 256, 0, st>>>(R, S, 0, blk(16));
     small_to_f64<T><<<16, 256, 0, st>>>(R, S, 1, blk(17));
     // operators of the K substep (V0 fixed): N_nu = V0^T diag(nu) V0, T'_V
@@ -1767,6 +1995,11 @@ struct StreamOps {
     if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
     const int zk = kz(n, 0);
     e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, const RkStage<T>& rk) {
+      if (s->fused >= 1) {
+        burgers_k_stage<T><<<(n + FUSED_BM - 1) / FUSED_BM, 256, fused_smem<T>(0), st>>>(
+            n, R, s->d_rank, Z, Nnu, tp(s->tv), (int)pairs_max(), ih2, ihx, ba, bb, s->d_status, rk);
+        return cudaGetLastError();
+      }
       stencil_panel<T><<<g, 256, 0, st>>>(n, R, 0, s->d_rank, Z, ih2, P0, ihx, ba != 0.0 ? P1 : nullptr);
       panel_mul_act<T><<<dim3((n + 31) / 32, (R + 63) / 64), 256, 0, st>>>(n, R, 0, s->d_rank, P0, Nnu, R, P2);
       cudaError_t e2 = cudaGetLastError();
@@ -1784,6 +2017,11 @@ struct StreamOps {
     if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
     const int zl = kz(m, 0);
     e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
+      if (s->fused >= 1) {
+        burgers_l_stage<T><<<(m + FUSED_BM - 1) / FUSED_BM, 256, fused_smem<T>(1), st>>>(
+            m, R, s->d_rank, Z, nu, Axx, tp(s->tl), (int)pairs_max(), nonlin ? 1 : 0, s->d_status, rk);
+        return cudaGetLastError();
+      }
       panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
       cudaError_t e2 = cudaGetLastError();
       if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
@@ -1833,6 +2071,14 @@ struct StreamOps {
           const RkStage<double> rk{sc.b[st_], last ? 0.0 : h * sc.a[st_ + 1], h, st_ == 0, last, Sy, Sz, Sa};
           small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
           small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
+          if (nonlin && s->fused >= 2) {
+            const int nzf = (n + FUSED_BM - 1) / FUSED_BM;
+            burgers_s_rows<T><<<nzf, 256, fused_smem<T>(2), st>>>(n, R, s->d_rank, Uh, Z, tp(s->th),
+                                                                   (int)pairs_max(), ihx, ba, bb, s->d_status, s->fgp);
+            s_stage_finish<<<64, 256, 0, st>>>(R, s->d_rank, nzf, s->fgp, Sk, rk);
+            e = cudaGetLastError();
+            continue;
+          }
           if (nonlin) {
             panel_mul_act<T><<<dim3((n + 31) / 32, (w + 63) / 64), 256, 0, st>>>(n, R, 1, s->d_rank, Uh, Z, w, P0);
             if (ba != 0.0) {
@@ -1966,14 +2212,18 @@ static cudaError_t burgers_step_on(lri_stream* s, cudaStream_t st) {
 }
 
 static void drop_graph(lri_stream* s) {
-  if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
-  s->step_exec = nullptr;
+  for (int c = 0; c < 3; ++c) {
+    if (s->step_exec[c]) cudaGraphExecDestroy(s->step_exec[c]);
+    s->step_exec[c] = nullptr;
+  }
 }
 
-// Capture one step on the private stream (nothing runs); on any failure the
-// steps run eagerly.
+// Capture one step of the current fused class on the private stream (nothing
+// runs); on any failure the steps of that class run eagerly.
 static void capture_step(lri_stream* s) {
-  drop_graph(s);
+  const int c = s->fused;
+  if (s->step_exec[c]) cudaGraphExecDestroy(s->step_exec[c]);
+  s->step_exec[c] = nullptr;
   if (!s->cap && cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess) {
     s->cap = nullptr;
     return;
@@ -1983,11 +2233,22 @@ static void capture_step(lri_stream* s) {
   const cudaError_t e = burgers_step_on(s, s->cap);
   const cudaError_t ec = cudaStreamEndCapture(s->cap, &g);
   if (e == cudaSuccess && ec == cudaSuccess && g) {
-    if (cudaGraphInstantiate(&s->step_exec, g, 0) != cudaSuccess) s->step_exec = nullptr;
-    else s->graph_dt = s->bh_dt;
+    if (cudaGraphInstantiate(&s->step_exec[c], g, 0) != cudaSuccess) s->step_exec[c] = nullptr;
+    else s->graph_dt[c] = s->bh_dt;
   }
   if (g) cudaGraphDestroy(g);
   cudaGetLastError();  // a failed capture leaves no sticky error; clear the last one
+}
+
+// The fused class of the next step from the device rank (synchronises st).
+static cudaError_t fused_class(lri_stream* s, cudaStream_t st, int* cls) {
+  int32_t r = 0;
+  cudaError_t e = cudaMemcpyAsync(&r, s->d_rank, sizeof(r), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  const int ra = std::min<int>((int)s->R, r);
+  *cls = (2 * ra <= lri::FUSED_KMAX) ? 2 : (ra <= lri::FUSED_KMAX ? 1 : 0);
+  return cudaSuccess;
 }
 
 extern "C" {
@@ -2078,6 +2339,7 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
                                    (int64_t)sizeof(double) * ((n + GA_ROWS - 1) / GA_ROWS) * 4 * R * R));
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
+  alloc((void**)&s->fgp, sizeof(double) * ((n + FUSED_BM - 1) / FUSED_BM) * 4 * R * R);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
@@ -2096,19 +2358,28 @@ lri_status lri_burgers_bind(lri_stream* s, void* U, void* S, void* V, const void
 lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stream) {
   if (!s || !s->burgers || nsteps < 0 || !std::isfinite(dt)) return LRI_ERR_ARG;
   if (!s->bound || !s->nu) return LRI_ERR_STATE;
-  if (s->step_exec && s->graph_dt != dt) drop_graph(s);
   s->bh_dt = dt;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
-  int k = 0;
-  if (!s->step_exec && nsteps > 1) {
-    // first step eagerly (one-time kernel attributes), then capture
-    e = burgers_step_on(s, st);
-    ++k;
-    if (e == cudaSuccess) capture_step(s);
+  // Each step takes the launch sequence of its rank class (fused RK-stage
+  // kernels up to rank 32): one captured graph per class, replayed while dt
+  // and the binding stay; a class's first step runs eagerly.
+  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
+    int cls = 0;
+    if ((e = fused_class(s, st, &cls)) != cudaSuccess) break;
+    s->fused = cls;
+    if (s->step_exec[cls] && s->graph_dt[cls] != dt) {
+      cudaGraphExecDestroy(s->step_exec[cls]);
+      s->step_exec[cls] = nullptr;
+    }
+    if (!s->step_exec[cls] && s->class_seen[cls] && nsteps > 1) capture_step(s);
+    if (s->step_exec[cls]) {
+      e = cudaGraphLaunch(s->step_exec[cls], st);
+    } else {
+      e = burgers_step_on(s, st);
+      s->class_seen[cls] = true;
+    }
   }
-  for (; k < nsteps && e == cudaSuccess; ++k)
-    e = s->step_exec ? cudaGraphLaunch(s->step_exec, st) : burgers_step_on(s, st);
   return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
 }
 
@@ -2124,6 +2395,7 @@ lri_status lri_stream_destroy(lri_stream* s) {
   cudaFree(s->kgp);
   cudaFree(s->kap);
   cudaFree(s->pw);
+  cudaFree(s->fgp);
   cudaFree(s->d_rank);
   cudaFree(s->d_status);
   cudaFree(s->Uh);
