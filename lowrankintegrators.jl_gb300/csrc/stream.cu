@@ -1424,6 +1424,9 @@ __device__ __forceinline__ void load_tensor(int ka, const T* __restrict__ Tp, in
   }
 }
 
+// Per-row arrays in shared memory have an odd row stride (ka | 1), so a warp
+// reading one entry of 32 consecutive rows touches 32 distinct banks.
+
 // K substep stage: v = (ih2 Dxx Z) N_nu + alpha KR(Dx Z, Z) T'_V + beta Dx(KR(Z, Z) T'_V),
 // Dx = ihx (shift - shift) on the active columns (zero elsewhere), then the RK update.
 template <typename T>
@@ -1437,31 +1440,31 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
     return;
   }
-  const int np = ka * (ka + 1) / 2;
+  const int np = ka * (ka + 1) / 2, ld = ka | 1;
   const bool nonlin = (alpha != 0.0 || beta != 0.0);
   T* tps = reinterpret_cast<T*>(smraw);            // np x ka
-  T* zs = tps + (nonlin ? np * ka : 0);             // (BM + 2) x ka: rows i0 - 1 .. i0 + BM
-  T* ks = zs + (FUSED_BM + 2) * ka;                 // (BM + 2) x ka: KR(Z, Z) T'
-  T* ns = ks + (FUSED_BM + 2) * ka;                 // ka x ka: N_nu
-  T* d1 = ns + ka * ka;                             // BM x ka: Dx Z
+  T* zs = tps + (nonlin ? np * ka : 0);             // (BM + 2) x ld: rows i0 - 1 .. i0 + BM
+  T* ks = zs + (FUSED_BM + 2) * ld;                 // (BM + 2) x ld: KR(Z, Z) T'
+  T* ns = ks + (FUSED_BM + 2) * ld;                 // ka x ka: N_nu
+  T* d1 = ns + ka * ka;                             // BM x ld: Dx Z
   const int i0 = blockIdx.x * FUSED_BM;
   if (nonlin) load_tensor(ka, Tp, PP, tps);
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-    const int ii = e / ka, a = e % ka;
+    const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
     int g = i0 - 1 + ii;
     g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
-    zs[e] = Z[g + (int64_t)a * N];
+    zs[ii * ld + a] = Z[g + (int64_t)a * N];
   }
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) ns[e] = T(Nnu[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
   if (beta != 0.0)
     for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
       const int ii = e / ka, c = e % ka;
-      ks[e] = kr_dot(ka, zs + ii * ka, zs + ii * ka, tps, c, true);
+      ks[ii * ld + c] = kr_dot(ka, zs + ii * ld, zs + ii * ld, tps, c, true);
     }
   for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int ii = e / ka, a = e % ka;
-    d1[e] = T(ihx) * (zs[(ii + 2) * ka + a] - zs[ii * ka + a]);
+    const int ii = e % FUSED_BM, a = e / FUSED_BM;
+    d1[ii * ld + a] = T(ihx) * (zs[(ii + 2) * ld + a] - zs[ii * ld + a]);
   }
   __syncthreads();
   const int rows = min(FUSED_BM, N - i0);
@@ -1470,15 +1473,15 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
     if (ii >= rows) continue;
     T v = T(0);
     if (c < ka) {
-      const T* zm = zs + ii * ka;
-      const T* z0 = zm + ka;
-      const T* zp = z0 + ka;
+      const T* zm = zs + ii * ld;
+      const T* z0 = zm + ld;
+      const T* zp = z0 + ld;
       for (int a = 0; a < ka; ++a) {
         const T d2 = T(ih2) * ((zm[a] + zp[a]) - T(2) * z0[a]);
         v = fma(d2, ns[a + c * ka], v);
       }
-      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ka, z0, tps, c, false), v);
-      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ka + c] - ks[ii * ka + c], v);
+      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ld, z0, tps, c, false), v);
+      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ld + c] - ks[ii * ld + c], v);
     }
     rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, v);
   }
@@ -1496,16 +1499,16 @@ __global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
     return;
   }
-  const int np = ka * (ka + 1) / 2;
+  const int np = ka * (ka + 1) / 2, ld = ka | 1;
   T* tps = reinterpret_cast<T*>(smraw);
-  T* zs = tps + (nonlin ? np * ka : 0);   // BM x ka
-  T* as = zs + FUSED_BM * ka;             // ka x ka: A_xx
+  T* zs = tps + (nonlin ? np * ka : 0);   // BM x ld
+  T* as = zs + FUSED_BM * ld;             // ka x ka: A_xx
   const int j0 = blockIdx.x * FUSED_BM;
   const int rows = min(FUSED_BM, M - j0);
   if (nonlin) load_tensor(ka, Tp, PP, tps);
   for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int jj = e / ka, a = e % ka;
-    zs[e] = (jj < rows) ? Z[(j0 + jj) + (int64_t)a * M] : T(0);
+    const int jj = e % FUSED_BM, a = e / FUSED_BM;
+    zs[jj * ld + a] = (jj < rows) ? Z[(j0 + jj) + (int64_t)a * M] : T(0);
   }
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) as[e] = T(Axx[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
@@ -1514,7 +1517,7 @@ __global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32
     if (jj >= rows) continue;
     T v = T(0);
     if (c < ka) {
-      const T* z = zs + jj * ka;
+      const T* z = zs + jj * ld;
       T lin = T(0);
       for (int a = 0; a < ka; ++a) lin = fma(z[a], as[a + c * ka], lin);
       v = nu[j0 + jj] * lin;
@@ -1527,7 +1530,8 @@ __global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32
 // S substep stage, row part: with A = Uhat Z (N x ka on the active columns
 // of the augmented panel), P2 = alpha KR(Dx A, A) T'_h + beta Dx(KR(A, A) T'_h)
 // and this CTA's partial of Uhat^T P2 (ka x ka, FP64 at the active indices
-// of part[blockIdx.x], ld 2R).  s_stage_finish adds the partials.
+// of part[blockIdx.x], ld 2R).  s_stage_finish adds the partials.  (Loops
+// here run along the columns: consecutive threads read consecutive entries.)
 template <typename T>
 __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_t* __restrict__ rank,
                                                       const T* __restrict__ Uh, const double* __restrict__ Zs,
@@ -1542,7 +1546,7 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
   const int np = ka * (ka + 1) / 2;
   T* tps = reinterpret_cast<T*>(smraw);        // np x ka
   T* us = tps + np * ka;                       // (BM + 2) x ka: Uhat rows i0 - 1 .. i0 + BM
-  T* zm = us + (FUSED_BM + 2) * ka;            // ka x ka: Z
+  T* zm = us + (FUSED_BM + 2) * ka;            // ka x ka: Z, row-major (zm[k ka + c] = Z[k, c])
   T* as = zm + ka * ka;                        // (BM + 2) x ka: A rows
   T* ks = as + (FUSED_BM + 2) * ka;            // (BM + 2) x ka: KR(A, A) T'
   T* d1 = ks + (FUSED_BM + 2) * ka;            // BM x ka: Dx A
@@ -1551,18 +1555,20 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
   const int rows = min(FUSED_BM, N - i0);
   load_tensor(ka, Tp, PP, tps);
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-    const int ii = e / ka, a = e % ka;
+    const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
     int g = i0 - 1 + ii;
     g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
-    us[e] = Uh[g + (int64_t)act_col(a, r, R) * N];
+    us[ii * ka + a] = Uh[g + (int64_t)act_col(a, r, R) * N];
   }
-  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x)
-    zm[e] = T(Zs[act_col(e % ka, r, R) + (int64_t)act_col(e / ka, r, R) * w]);
+  for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {
+    const int k = e % ka, c = e / ka;
+    zm[k * ka + c] = T(Zs[act_col(k, r, R) + (int64_t)act_col(c, r, R) * w]);
+  }
   __syncthreads();
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {  // A = Uhat Z
     const int ii = e / ka, c = e % ka;
     T acc = T(0);
-    for (int k = 0; k < ka; ++k) acc = fma(us[ii * ka + k], zm[k + c * ka], acc);
+    for (int k = 0; k < ka; ++k) acc = fma(us[ii * ka + k], zm[k * ka + c], acc);
     as[e] = acc;
   }
   __syncthreads();
@@ -1595,8 +1601,9 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
 template <typename T>
 size_t fused_smem(int which) {
   const size_t K = FUSED_KMAX, np = K * (K + 1) / 2, B = FUSED_BM;
-  if (which == 0) return sizeof(T) * (np * K + 2 * (B + 2) * K + K * K + B * K);
-  if (which == 1) return sizeof(T) * (np * K + B * K + K * K);
+  const size_t L = K | 1;  // padded row stride
+  if (which == 0) return sizeof(T) * (np * K + 2 * (B + 2) * L + K * K + B * L);
+  if (which == 1) return sizeof(T) * (np * K + B * L + K * K);
   return sizeof(T) * (np * K + 3 * (B + 2) * K + K * K + 2 * B * K);
 }
 
