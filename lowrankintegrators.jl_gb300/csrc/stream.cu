@@ -1396,36 +1396,50 @@ __global__ void s_stage_finish(int R, const int32_t* __restrict__ rank, int nz, 
 constexpr int FUSED_BM = 32;
 constexpr int FUSED_KMAX = 32;
 
-// sum_{a <= b} KR(P, Q)_ab T'[p(a,b), c] with KR(P, Q)_ab = (P_a Q_b + P_b Q_a) / 2
-// (P == Q: P_a P_b), T' at tps[p * ka + c]
-template <typename T>
-__device__ __forceinline__ T kr_dot(int ka, const T* P, const T* Q, const T* tps, int c, bool same) {
-  T acc = T(0);
+// Four consecutive columns c0 .. c0 + 3 of one row of
+//   sum_{a <= b} KR(P, Q)_ab T'[p(a,b), c],  KR(P, Q)_ab = (P_a Q_b + P_b Q_a) / 2
+// (SAME: P == Q, KR = P_a P_b); P, Q: the row's ka values; T' column-major
+// in shared memory, tpt[c * np + p], zero beyond the active columns.  Each
+// tensor value read serves 4 (8) multiply-adds; a warp's threads share c0,
+// so the tensor reads are broadcasts.
+template <typename T, bool SAME>
+__device__ __forceinline__ void kr_row4(int ka, int np, const T* P, const T* Q, const T* tpt, int c0, T (&acc)[4]) {
   int p = 0;
   for (int a = 0; a < ka; ++a) {
-    T g1 = T(0), g2 = T(0);
+    T g1[4] = {T(0), T(0), T(0), T(0)}, g2[4] = {T(0), T(0), T(0), T(0)};
     for (int b = a; b < ka; ++b, ++p) {
-      const T t = tps[p * ka + c];
-      g1 = fma(Q[b], t, g1);
-      if (!same) g2 = fma(P[b], t, g2);
+      const T qb = Q[b];
+      const T pb = SAME ? qb : P[b];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const T t = tpt[(c0 + v) * np + p];
+        g1[v] = fma(qb, t, g1[v]);
+        if (!SAME) g2[v] = fma(pb, t, g2[v]);
+      }
     }
-    acc = same ? fma(P[a], g1, acc) : fma(T(0.5), fma(P[a], g1, Q[a] * g2), acc);
+    const T pa = P[a];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (SAME) acc[v] = fma(pa, g1[v], acc[v]);
+      else acc[v] = fma(T(0.5), fma(pa, g1[v], Q[a] * g2[v]), acc[v]);
+    }
   }
-  return acc;
 }
 
-// loads the packed tensor's active block: tps[p * ka + c] = Tp[p + c PP]
+// the packed tensor's active block, column-major: tpt[c * np + p] = Tp[p + c PP]
+// for c < ka, zero for ka <= c < kap (kap = ka rounded up to 4)
 template <typename T>
-__device__ __forceinline__ void load_tensor(int ka, const T* __restrict__ Tp, int PP, T* tps) {
+__device__ __forceinline__ void load_tensor(int ka, int kap, const T* __restrict__ Tp, int PP, T* tpt) {
   const int np = ka * (ka + 1) / 2;
-  for (int e = threadIdx.x; e < np * ka; e += blockDim.x) {
+  for (int e = threadIdx.x; e < np * kap; e += blockDim.x) {
     const int pp = e % np, c = e / np;
-    tps[pp * ka + c] = Tp[pp + (int64_t)c * PP];
+    tpt[e] = (c < ka) ? Tp[pp + (int64_t)c * PP] : T(0);
   }
 }
 
-// Per-row arrays in shared memory have an odd row stride (ka | 1), so a warp
-// reading one entry of 32 consecutive rows touches 32 distinct banks.
+// Per-row arrays in shared memory have an odd row stride (ka | 1), and
+// threads run along the rows, so a warp touches 32 distinct banks and its
+// global accesses to a column are coalesced.
 
 // K substep stage: v = (ih2 Dxx Z) N_nu + alpha KR(Dx Z, Z) T'_V + beta Dx(KR(Z, Z) T'_V),
 // Dx = ihx (shift - shift) on the active columns (zero elsewhere), then the RK update.
@@ -1440,15 +1454,16 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
     return;
   }
-  const int np = ka * (ka + 1) / 2, ld = ka | 1;
+  const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3, ncg = kap / 4;
   const bool nonlin = (alpha != 0.0 || beta != 0.0);
-  T* tps = reinterpret_cast<T*>(smraw);            // np x ka
-  T* zs = tps + (nonlin ? np * ka : 0);             // (BM + 2) x ld: rows i0 - 1 .. i0 + BM
-  T* ks = zs + (FUSED_BM + 2) * ld;                 // (BM + 2) x ld: KR(Z, Z) T'
-  T* ns = ks + (FUSED_BM + 2) * ld;                 // ka x ka: N_nu
+  T* tpt = reinterpret_cast<T*>(smraw);            // kap x np
+  T* zs = tpt + (nonlin ? np * kap : 0);            // (BM + 2) x ld: rows i0 - 1 .. i0 + BM
+  T* ks = zs + (FUSED_BM + 2) * ld;                 // (BM + 2) x ld: KR(Z, Z) T' (kap columns used)
+  T* ns = ks + (FUSED_BM + 2) * (kap | 1);          // ka x ka: N_nu
   T* d1 = ns + ka * ka;                             // BM x ld: Dx Z
+  const int ldk = kap | 1;
   const int i0 = blockIdx.x * FUSED_BM;
-  if (nonlin) load_tensor(ka, Tp, PP, tps);
+  if (nonlin) load_tensor(ka, kap, Tp, PP, tpt);
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
     const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
     int g = i0 - 1 + ii;
@@ -1458,9 +1473,12 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) ns[e] = T(Nnu[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
   if (beta != 0.0)
-    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-      const int ii = e / ka, c = e % ka;
-      ks[ii * ld + c] = kr_dot(ka, zs + ii * ld, zs + ii * ld, tps, c, true);
+    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ncg; e += blockDim.x) {
+      const int ii = e % (FUSED_BM + 2), c0 = 4 * (e / (FUSED_BM + 2));
+      T acc[4] = {T(0), T(0), T(0), T(0)};
+      kr_row4<T, true>(ka, np, zs + ii * ld, zs + ii * ld, tpt, c0, acc);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) ks[ii * ldk + c0 + v] = acc[v];
     }
   for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
     const int ii = e % FUSED_BM, a = e / FUSED_BM;
@@ -1468,22 +1486,36 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
   }
   __syncthreads();
   const int rows = min(FUSED_BM, N - i0);
-  for (int e = threadIdx.x; e < FUSED_BM * R; e += blockDim.x) {
-    const int ii = e % FUSED_BM, c = e / FUSED_BM;
+  const int ncg_all = (R + 3) / 4;
+  for (int e = threadIdx.x; e < FUSED_BM * ncg_all; e += blockDim.x) {
+    const int ii = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
     if (ii >= rows) continue;
-    T v = T(0);
-    if (c < ka) {
+    T v[4] = {T(0), T(0), T(0), T(0)};
+    if (c0 < ka) {
       const T* zm = zs + ii * ld;
       const T* z0 = zm + ld;
       const T* zp = z0 + ld;
       for (int a = 0; a < ka; ++a) {
         const T d2 = T(ih2) * ((zm[a] + zp[a]) - T(2) * z0[a]);
-        v = fma(d2, ns[a + c * ka], v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (c0 + q < ka) v[q] = fma(d2, ns[a + (c0 + q) * ka], v[q]);
       }
-      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ld, z0, tps, c, false), v);
-      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ld + c] - ks[ii * ld + c], v);
+      if (alpha != 0.0) {
+        T k1[4] = {T(0), T(0), T(0), T(0)};
+        kr_row4<T, false>(ka, np, d1 + ii * ld, z0, tpt, c0, k1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = fma(T(alpha), k1[q], v[q]);
+      }
+      if (beta != 0.0)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = fma(T(beta * ihx), ks[(ii + 2) * ldk + c0 + q] - ks[ii * ldk + c0 + q], v[q]);
     }
-    rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + q;
+      if (c < R) rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, (c < ka) ? v[q] : T(0));
+    }
   }
 }
 
@@ -1499,39 +1531,53 @@ __global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
     return;
   }
-  const int np = ka * (ka + 1) / 2, ld = ka | 1;
-  T* tps = reinterpret_cast<T*>(smraw);
-  T* zs = tps + (nonlin ? np * ka : 0);   // BM x ld
-  T* as = zs + FUSED_BM * ld;             // ka x ka: A_xx
+  const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3;
+  T* tpt = reinterpret_cast<T*>(smraw);
+  T* zs = tpt + (nonlin ? np * kap : 0);   // BM x ld
+  T* as = zs + FUSED_BM * ld;              // ka x ka: A_xx
   const int j0 = blockIdx.x * FUSED_BM;
   const int rows = min(FUSED_BM, M - j0);
-  if (nonlin) load_tensor(ka, Tp, PP, tps);
+  if (nonlin) load_tensor(ka, kap, Tp, PP, tpt);
   for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
     const int jj = e % FUSED_BM, a = e / FUSED_BM;
     zs[jj * ld + a] = (jj < rows) ? Z[(j0 + jj) + (int64_t)a * M] : T(0);
   }
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) as[e] = T(Axx[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
-  for (int e = threadIdx.x; e < FUSED_BM * R; e += blockDim.x) {
-    const int jj = e % FUSED_BM, c = e / FUSED_BM;
+  const int ncg_all = (R + 3) / 4;
+  for (int e = threadIdx.x; e < FUSED_BM * ncg_all; e += blockDim.x) {
+    const int jj = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
     if (jj >= rows) continue;
-    T v = T(0);
-    if (c < ka) {
+    T v[4] = {T(0), T(0), T(0), T(0)};
+    if (c0 < ka) {
       const T* z = zs + jj * ld;
-      T lin = T(0);
-      for (int a = 0; a < ka; ++a) lin = fma(z[a], as[a + c * ka], lin);
-      v = nu[j0 + jj] * lin;
-      if (nonlin) v += kr_dot(ka, z, z, tps, c, true);
+      T lin[4] = {T(0), T(0), T(0), T(0)};
+      for (int a = 0; a < ka; ++a)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (c0 + q < ka) lin[q] = fma(z[a], as[a + (c0 + q) * ka], lin[q]);
+      const T nj = nu[j0 + jj];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = nj * lin[q];
+      if (nonlin) {
+        T k[4] = {T(0), T(0), T(0), T(0)};
+        kr_row4<T, true>(ka, np, z, z, tpt, c0, k);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] += k[q];
+      }
     }
-    rk_apply(rk, (int64_t)(j0 + jj) + (int64_t)c * M, v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + q;
+      if (c < R) rk_apply(rk, (int64_t)(j0 + jj) + (int64_t)c * M, (c < ka) ? v[q] : T(0));
+    }
   }
 }
 
 // S substep stage, row part: with A = Uhat Z (N x ka on the active columns
 // of the augmented panel), P2 = alpha KR(Dx A, A) T'_h + beta Dx(KR(A, A) T'_h)
 // and this CTA's partial of Uhat^T P2 (ka x ka, FP64 at the active indices
-// of part[blockIdx.x], ld 2R).  s_stage_finish adds the partials.  (Loops
-// here run along the columns: consecutive threads read consecutive entries.)
+// of part[blockIdx.x], ld 2R).  s_stage_finish_warp adds the partials.
 template <typename T>
 __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_t* __restrict__ rank,
                                                       const T* __restrict__ Uh, const double* __restrict__ Zs,
@@ -1543,22 +1589,22 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_BAD_SHAPE);
     return;
   }
-  const int np = ka * (ka + 1) / 2;
-  T* tps = reinterpret_cast<T*>(smraw);        // np x ka
-  T* us = tps + np * ka;                       // (BM + 2) x ka: Uhat rows i0 - 1 .. i0 + BM
-  T* zm = us + (FUSED_BM + 2) * ka;            // ka x ka: Z, row-major (zm[k ka + c] = Z[k, c])
-  T* as = zm + ka * ka;                        // (BM + 2) x ka: A rows
-  T* ks = as + (FUSED_BM + 2) * ka;            // (BM + 2) x ka: KR(A, A) T'
-  T* d1 = ks + (FUSED_BM + 2) * ka;            // BM x ka: Dx A
-  T* p2 = d1 + FUSED_BM * ka;                  // BM x ka: P2
+  const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3, ncg = kap / 4, ldk = kap | 1;
+  T* tpt = reinterpret_cast<T*>(smraw);        // kap x np
+  T* us = tpt + np * kap;                      // (BM + 2) x ld: Uhat rows i0 - 1 .. i0 + BM
+  T* zm = us + (FUSED_BM + 2) * ld;            // ka x ka: Z, row-major (zm[k ka + c] = Z[k, c])
+  T* as = zm + ka * ka;                        // (BM + 2) x ld: A rows
+  T* ks = as + (FUSED_BM + 2) * ld;            // (BM + 2) x ldk: KR(A, A) T'
+  T* d1 = ks + (FUSED_BM + 2) * ldk;           // BM x ld: Dx A
+  T* p2 = d1 + FUSED_BM * ld;                  // BM x ldk: P2
   const int i0 = blockIdx.x * FUSED_BM;
   const int rows = min(FUSED_BM, N - i0);
-  load_tensor(ka, Tp, PP, tps);
+  load_tensor(ka, kap, Tp, PP, tpt);
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
     const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
     int g = i0 - 1 + ii;
     g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
-    us[ii * ka + a] = Uh[g + (int64_t)act_col(a, r, R) * N];
+    us[ii * ld + a] = Uh[g + (int64_t)act_col(a, r, R) * N];
   }
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {
     const int k = e % ka, c = e / ka;
@@ -1566,34 +1612,69 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
   }
   __syncthreads();
   for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {  // A = Uhat Z
-    const int ii = e / ka, c = e % ka;
+    const int ii = e % (FUSED_BM + 2), c = e / (FUSED_BM + 2);
     T acc = T(0);
-    for (int k = 0; k < ka; ++k) acc = fma(us[ii * ka + k], zm[k * ka + c], acc);
-    as[e] = acc;
+    for (int k = 0; k < ka; ++k) acc = fma(us[ii * ld + k], zm[k * ka + c], acc);
+    as[ii * ld + c] = acc;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-    const int ii = e / ka, c = e % ka;
-    if (beta != 0.0) ks[e] = kr_dot(ka, as + ii * ka, as + ii * ka, tps, c, true);
-    if (ii < FUSED_BM) d1[e] = T(ihx) * (as[(ii + 2) * ka + c] - as[ii * ka + c]);
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int ii = e / ka, c = e % ka;
-    T v = T(0);
-    if (ii < rows) {
-      if (alpha != 0.0) v = fma(T(alpha), kr_dot(ka, d1 + ii * ka, as + (ii + 1) * ka, tps, c, false), v);
-      if (beta != 0.0) v = fma(T(beta * ihx), ks[(ii + 2) * ka + c] - ks[ii * ka + c], v);
+  if (beta != 0.0)
+    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ncg; e += blockDim.x) {
+      const int ii = e % (FUSED_BM + 2), c0 = 4 * (e / (FUSED_BM + 2));
+      T acc[4] = {T(0), T(0), T(0), T(0)};
+      kr_row4<T, true>(ka, np, as + ii * ld, as + ii * ld, tpt, c0, acc);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) ks[ii * ldk + c0 + v] = acc[v];
     }
-    p2[e] = v;
+  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
+    const int ii = e % FUSED_BM, c = e / FUSED_BM;
+    d1[ii * ld + c] = T(ihx) * (as[(ii + 2) * ld + c] - as[ii * ld + c]);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < FUSED_BM * ncg; e += blockDim.x) {
+    const int ii = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
+    T v[4] = {T(0), T(0), T(0), T(0)};
+    if (ii < rows) {
+      if (alpha != 0.0) {
+        T k1[4] = {T(0), T(0), T(0), T(0)};
+        kr_row4<T, false>(ka, np, d1 + ii * ld, as + (ii + 1) * ld, tpt, c0, k1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = fma(T(alpha), k1[q], v[q]);
+      }
+      if (beta != 0.0)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = fma(T(beta * ihx), ks[(ii + 2) * ldk + c0 + q] - ks[ii * ldk + c0 + q], v[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) p2[ii * ldk + c0 + q] = v[q];
   }
   __syncthreads();
   double* dst = part + (int64_t)blockIdx.x * w * w;
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {  // Uhat^T P2 over the tile's rows
     const int a = e % ka, c = e / ka;
     T acc = T(0);
-    for (int ii = 0; ii < rows; ++ii) acc = fma(us[(ii + 1) * ka + a], p2[ii * ka + c], acc);
+    for (int ii = 0; ii < rows; ++ii) acc = fma(us[(ii + 1) * ld + a], p2[ii * ldk + c], acc);
     dst[act_col(a, r, R) + (int64_t)act_col(c, r, R) * w] = (double)acc;
+  }
+}
+
+// S-flow stage of the fused path: v[a, c] = C[a, c] + sum_z part[z][a, c] on
+// the active block, one warp per entry (lane-strided partials, a fixed
+// shuffle tree: deterministic), then the RK update of the FP64 stage arrays.
+__global__ void __launch_bounds__(256) s_stage_finish_warp(int R, const int32_t* __restrict__ rank, int nz,
+                                                           const double* __restrict__ part,
+                                                           const double* __restrict__ C, RkStage<double> rk) {
+  const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
+  const int lane = threadIdx.x & 31;
+  const int64_t len = (int64_t)ka * ka;
+  for (int64_t o = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; o < len;
+       o += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t idx = act_col((int)(o % ka), r, R) + (int64_t)act_col((int)(o / ka), r, R) * w;
+    double v = 0.0;
+    for (int z = lane; z < nz; z += 32) v += part[z * (int64_t)w * w + idx];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) rk_apply(rk, idx, C[idx] + v);
   }
 }
 
@@ -1604,7 +1685,7 @@ size_t fused_smem(int which) {
   const size_t L = K | 1;  // padded row stride
   if (which == 0) return sizeof(T) * (np * K + 2 * (B + 2) * L + K * K + B * L);
   if (which == 1) return sizeof(T) * (np * K + B * L + K * K);
-  return sizeof(T) * (np * K + 3 * (B + 2) * K + K * K + 2 * B * K);
+  return sizeof(T) * (np * K + 3 * (B + 2) * L + K * K + 2 * B * L);
 }
 
 // small FP64 helpers of the S step: X (R x R, T, ld R) -> Y (FP64, ld R), optionally transposed
@@ -2082,7 +2163,7 @@ struct StreamOps {
             const int nzf = (n + FUSED_BM - 1) / FUSED_BM;
             burgers_s_rows<T><<<nzf, 256, fused_smem<T>(2), st>>>(n, R, s->d_rank, Uh, Z, tp(s->th),
                                                                    (int)pairs_max(), ihx, ba, bb, s->d_status, s->fgp);
-            s_stage_finish<<<64, 256, 0, st>>>(R, s->d_rank, nzf, s->fgp, Sk, rk);
+            s_stage_finish_warp<<<128, 256, 0, st>>>(R, s->d_rank, nzf, s->fgp, Sk, rk);
             e = cudaGetLastError();
             continue;
           }
