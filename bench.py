@@ -137,13 +137,13 @@ def _pool_init():
 
 
 def _cpu_worker(args):
-    idx, steps, warmup = args
+    idx, steps, warmup, count = args
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     import workloads
     from oracle import lri_oracle as O
     integs = []
     for i in idx:
-        e = workloads.lyapunov_ensemble(first=i, limit=1)[0]
+        e = workloads.lyapunov_ensemble(count=count, first=i, limit=1)[0]
         p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
                               (0.0, DT * (steps + warmup)))
         integs.append(O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT))
@@ -159,12 +159,12 @@ def _cpu_worker(args):
 
 def _oracle_finals(args):
     """The oracle's factors (dense) after `steps` steps of each instance."""
-    idx, steps = args
+    idx, steps, count = args
     import workloads
     from oracle import lri_oracle as O
     out = []
     for i in idx:
-        e = workloads.lyapunov_ensemble(first=i, limit=1)[0]
+        e = workloads.lyapunov_ensemble(count=count, first=i, limit=1)[0]
         p = O.MatrixDEProblem(O.SylvesterTridiagOp(e.A, e.B), O.SVDLikeRepresentation(e.U, e.S, e.V),
                               (0.0, DT * steps))
         integ = O.init(p, O.UnconventionalAlgorithm(O.RK4(NSUB)), DT)
@@ -186,7 +186,7 @@ def cpu_baseline(count, sample_every, steps, warmup=0, cores=None):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(len(chunks), initializer=_pool_init) as pool:
-        busy = pool.map(_cpu_worker, [(c, steps, warmup) for c in chunks])
+        busy = pool.map(_cpu_worker, [(c, steps, warmup, count) for c in chunks])
     wall = time.perf_counter() - t0
     # instance-steps per second of the whole pool, scaled to the full ensemble
     inst_steps = len(sample) * steps
@@ -882,7 +882,7 @@ def main():
         chunks = [c for c in (sample[k::cores] for k in range(cores)) if c]
         t0 = time.perf_counter()
         with mp.get_context("spawn").Pool(len(chunks), initializer=_pool_init) as pool:
-            finals = pool.map(_oracle_finals, [(c, W + K) for c in chunks])
+            finals = pool.map(_oracle_finals, [(c, W + K, args.count) for c in chunks])
         wall = time.perf_counter() - t0
         ref = {i: Y for part in finals for i, Y in part}
         from oracle import lri_oracle as O
