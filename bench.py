@@ -54,10 +54,11 @@ def peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
-# step of each class's step kernel, from one ncu capture of the 1024-instance
+# step of each class's step kernel, from an ncu capture of the 1024-instance
 # slice of this ensemble (655 FP32-class and 369 double-float-class
-# instances: 0.256 GB and 1.770 GB per launch); scaled by instance counts.
-TRAFFIC_PER_INSTANCE = {"fp32": 0.256e9 / 655, "df": 1.770e9 / 369}
+# instances: 0.2596 GB and 1.7816 GB per steady launch of step_kernel<T, 3>);
+# scaled by the instance counts.
+TRAFFIC_PER_INSTANCE = {"fp32": 0.2596e9 / 655, "df": 1.7816e9 / 369}
 
 
 def algorithmic(shapes, nsub=NSUB, esize=4):
@@ -984,8 +985,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": TRAFFIC_PER_INSTANCE["fp32"] * n_fp32
                                 + TRAFFIC_PER_INSTANCE["df"] * (args.count - n_fp32),
-                     "traffic_source": "ncu dram bytes per instance-step of each class (1024-instance capture), "
-                                       "scaled by the instance counts",
+                     "traffic_source": "ncu dram bytes per instance-step of each class (1024-instance capture of "
+                                       "step_kernel<T, 3>, profiles/step_kernel_lyapunov_ensemble.md), scaled "
+                                       "by the instance counts",
                      "peak_source": src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "compulsory bytes per batched step (factors and operators read, factors "
