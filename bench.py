@@ -986,8 +986,7 @@ def main():
                      "traffic": TRAFFIC_PER_INSTANCE["fp32"] * n_fp32
                                 + TRAFFIC_PER_INSTANCE["df"] * (args.count - n_fp32),
                      "traffic_source": "ncu dram bytes per instance-step of each class (1024-instance capture of "
-                                       "step_kernel<T, 3>, profiles/step_kernel_lyapunov_ensemble.md), scaled "
-                                       "by the instance counts",
+                                       "step_kernel<T, 3>), scaled by the instance counts",
                      "peak_source": src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "compulsory bytes per batched step (factors and operators read, factors "
