@@ -12,13 +12,16 @@
 // contraction index) in chunks of 32:
 //   warp 4   TMA producer: per chunk, the A(t+dt) and A(t) tiles (128 x 32)
 //            and the chunk's 32 rows of the split right factor (hi and lo);
-//   warps 0-3 form dY = A(t+dt) - A(t) in shared memory (exact in FP32 for
-//            nearby snapshots), split it into TF32 hi + lo parts in place,
-//            written in the K-major 128-byte-swizzled operand layout;
+//   warps 0-3 form row i of dY = A(t+dt) - A(t) (exact in FP32 for nearby
+//            snapshots) in thread i's registers, split it into TF32 hi + lo
+//            parts and store both into tensor memory (tcgen05.st): the A
+//            operand never goes back through shared memory, whose bandwidth
+//            (TMA writes, operand reads) bounds the pass otherwise;
 //   warp 5   allocates tensor memory and issues, per 8-wide K slice,
-//            tcgen05.mma (kind::tf32, M = 128, N = active columns rounded
-//            up to 16): hi*hi into one FP32 accumulator, hi*lo + lo*hi into
-//            a second (correction) one;
+//            tcgen05.mma (kind::tf32, A from tensor memory, B from shared
+//            memory, M = 128, N = active columns rounded up to 16): hi*hi
+//            into one FP32 accumulator, hi*lo + lo*hi into a second
+//            (correction) one;
 //   warps 0-3 also drain the accumulators: the tensor cores' FP32
 //            accumulation truncates, so its error grows with the number of
 //            MMAs summed into one accumulator (1.4e-5 relative over 2048
@@ -29,12 +32,12 @@
 //   warps 0-3 finally write the CTA's split-K partial; a second kernel sums
 //            the partials in a fixed order (deterministic) and writes the
 //            panel.
-// Rows of dY^T X: the snapshot tile arrives through TMA with the 128-byte
-// swizzle already in operand layout (K = rows of the snapshot are
-// contiguous), so forming and splitting dY is element-wise.  Rows of dY X:
-// the tile arrives row-contiguous and the four warps transpose it through
-// registers.  3xTF32 drops only the lo*lo term: products accurate to about
-// 2^-21 relative, summed in FP32.
+// Rows of dY^T X: the snapshot tile arrives through TMA K-major with the
+// 128-byte swizzle (K = rows of the snapshot are contiguous); rows of dY X:
+// it arrives row-contiguous and each thread gathers its row down the tile's
+// columns.  Two A slots in tensor memory let the split of chunk k + 1 overlap
+// the MMAs of chunk k.  3xTF32 drops only the lo*lo term: products accurate
+// to about 2^-21 relative, summed in FP32.
 //
 // Every mbarrier wait is bounded (about two seconds of SM clock); a wait
 // that gives up sets a status bit, the CTA stops issuing work, waits (again
@@ -65,6 +68,7 @@ constexpr int TC_DRAIN_LAG = 2;                   // chunks of the next block qu
 constexpr int TC_SMEM_LIMIT = 232448;             // 227 KB opt-in per CTA
 constexpr int TC_CTRL_BYTES = 1024;               // barriers, tensor-memory address, abort flag
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
+constexpr int TC_A_SLOTS = 2;                     // A operand slots in tensor memory (hi: 32, lo: 32 columns each)
 
 struct TcArgs {
   int P, R, NB, nchunks, chunks_per_split, stages, rows_mode, ncols;
@@ -142,13 +146,27 @@ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
+// D (+)= A B^T, A (M x 8: one TF32 value per 32-bit column, row m in lane m)
+// read from tensor memory, B (N x 8, K-major) from shared memory
+__device__ __forceinline__ void umma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accumulate) {
   asm volatile(
       "{\n.reg .pred p;\n"
       "setp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// a warp's 32 lanes x 32 consecutive columns: thread t writes lane (base + t)
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]), "f"(v[17]), "f"(v[18]),
+      "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]), "f"(v[25]), "f"(v[26]), "f"(v[27]),
+      "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
       : "memory");
 }
 
@@ -220,6 +238,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   auto acc_full = [&](int b) { return bar0 + 8u * (3 * TC_MAX_STAGES + b); };       // a block's MMAs done
   auto acc_empty = [&](int b) { return bar0 + 8u * (3 * TC_MAX_STAGES + 2 + b); };  // a block drained
   const uint32_t done = bar0 + 8u * (3 * TC_MAX_STAGES + 4);                 // every MMA done
+  auto aempty = [&](int t) { return bar0 + 8u * (3 * TC_MAX_STAGES + 5 + t); };  // MMAs done with A slot t
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ctrl + 256);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(ctrl + 260);
 
@@ -231,8 +250,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int ka = active_cols(a);
   const int N = min(a.NB, max(16, (ka + 15) & ~15));
   // accumulator buffer b: hi*hi sums in columns [2 b NB, 2 b NB + N), the
-  // hi*lo + lo*hi corrections NB columns further
-  const uint32_t ncols_tmem = (4 * a.NB > 256) ? 512u : ((4 * a.NB > 128) ? 256u : 128u);
+  // hi*lo + lo*hi corrections NB columns further; the A operand of chunk it
+  // (dY hi, then lo, 32 columns each) in slot it % 2 from column 4 NB
+  const uint32_t a_col = 4u * (uint32_t)a.NB;
+  const uint32_t ncols_tmem = (a_col + 64 * TC_A_SLOTS > 256) ? 512u : 256u;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
@@ -244,6 +265,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(acc_full(b), 1);
       mbar_init(acc_empty(b), 128);
     }
+    for (int t = 0; t < TC_A_SLOTS; ++t) mbar_init(aempty(t), 1);
     mbar_init(done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -302,21 +324,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (first && bi >= 2 && !mbar_wait(acc_empty(b), (uint32_t)((bi >> 1) - 1) & 1u, abort_flag, a)) break;
         if (!mbar_wait(full(s), par, abort_flag, a) || !mbar_wait(tfull(s), par, abort_flag, a)) break;
         tc_fence_after();
-        const uint32_t sa1 = smem_u32(base + (size_t)s * stage_bytes);
-        const uint32_t sa0 = sa1 + TC_TILE_BYTES;
-        const uint32_t sxh = sa1 + 2 * TC_TILE_BYTES;
+        const uint32_t sxh = smem_u32(base + (size_t)s * stage_bytes) + 2 * TC_TILE_BYTES;
         const uint32_t sxl = sxh + xbytes;
         const uint32_t dmain = tmem + (uint32_t)(2 * b * a.NB), dcorr = dmain + (uint32_t)a.NB;
+        const uint32_t tah = tmem + a_col + (uint32_t)(64 * (it % TC_A_SLOTS)), tal = tah + 32u;
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 8; ++kk) {
-          const uint64_t ah = sw128_desc(sa1 + 32u * kk), al = sw128_desc(sa0 + 32u * kk);
           const uint64_t bh = sw128_desc(sxh + 32u * kk), bl = sw128_desc(sxl + 32u * kk);
           const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
-          umma_tf32(dmain, ah, bh, idesc, acc);
-          umma_tf32(dcorr, ah, bl, idesc, acc);
-          umma_tf32(dcorr, al, bh, idesc, 1u);
+          umma_tf32_ts(dmain, tah + 8u * kk, bh, idesc, acc);
+          umma_tf32_ts(dcorr, tah + 8u * kk, bl, idesc, acc);
+          umma_tf32_ts(dcorr, tal + 8u * kk, bh, idesc, 1u);
         }
         umma_commit(empty(s));
+        umma_commit(aempty(it % TC_A_SLOTS));
         if ((it % TC_DRAIN) == TC_DRAIN - 1 || it == nk - 1) umma_commit(acc_full(b));
       }
       umma_commit(done);  // arrives once every MMA issued above has completed
@@ -362,46 +383,53 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         aborted = true;
         break;
       }
-      float* a1 = reinterpret_cast<float*>(base + (size_t)s * stage_bytes);
-      float* a0 = a1 + TC_BM * TC_BK;
+      const float* a1 = reinterpret_cast<const float*>(base + (size_t)s * stage_bytes);
+      const float* a0 = a1 + TC_BM * TC_BK;
+      // row tid of dY for the chunk's 32 K values
+      float h[TC_BK], l[TC_BK];
       if (a.rows_mode) {
-        // tile rows j (32) of 128 contiguous i; operand row i = this thread
-        float d[TC_BK];
+        // tile rows j (32) of 128 contiguous i
 #pragma unroll
-        for (int j = 0; j < TC_BK; ++j) d[j] = a.has_a0 ? a1[j * TC_BM + tid] - a0[j * TC_BM + tid] : a1[j * TC_BM + tid];
-        bar_any(false);  // every thread has read its column before the tile is overwritten
-        unsigned char* h8 = reinterpret_cast<unsigned char*>(a1);
-        unsigned char* l8 = reinterpret_cast<unsigned char*>(a0);
+        for (int j = 0; j < TC_BK; ++j) h[j] = a.has_a0 ? a1[j * TC_BM + tid] - a0[j * TC_BM + tid] : a1[j * TC_BM + tid];
+      } else {
+        // K-major tile with the 128-byte swizzle: the 16-byte group c of row
+        // i sits at group c ^ (i & 7) of the row's 128 bytes
         const int rb = (tid >> 3) * 1024 + (tid & 7) * 128;
+        const unsigned char* b1 = reinterpret_cast<const unsigned char*>(a1);
+        const unsigned char* b0 = reinterpret_cast<const unsigned char*>(a0);
 #pragma unroll
         for (int c = 0; c < TC_BK / 4; ++c) {
-          float4 h, l;
-          split(d[4 * c + 0], h.x, l.x);
-          split(d[4 * c + 1], h.y, l.y);
-          split(d[4 * c + 2], h.z, l.z);
-          split(d[4 * c + 3], h.w, l.w);
           const int off = rb + ((c ^ (tid & 7)) << 4);
-          *reinterpret_cast<float4*>(h8 + off) = h;
-          *reinterpret_cast<float4*>(l8 + off) = l;
-        }
-      } else {
-        // the tile is already in operand layout: element-wise
-        float4* p1 = reinterpret_cast<float4*>(a1);
-        float4* p0 = reinterpret_cast<float4*>(a0);
-#pragma unroll
-        for (int u = 0; u < (TC_BM * TC_BK / 4) / 128; ++u) {
-          const int q = tid + 128 * u;
-          const float4 x1 = p1[q], x0 = a.has_a0 ? p0[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          float4 h, l;
-          split(x1.x - x0.x, h.x, l.x);
-          split(x1.y - x0.y, h.y, l.y);
-          split(x1.z - x0.z, h.z, l.z);
-          split(x1.w - x0.w, h.w, l.w);
-          p1[q] = h;
-          p0[q] = l;
+          float4 x1 = *reinterpret_cast<const float4*>(b1 + off);
+          if (a.has_a0) {
+            const float4 x0 = *reinterpret_cast<const float4*>(b0 + off);
+            x1.x -= x0.x;
+            x1.y -= x0.y;
+            x1.z -= x0.z;
+            x1.w -= x0.w;
+          }
+          h[4 * c + 0] = x1.x;
+          h[4 * c + 1] = x1.y;
+          h[4 * c + 2] = x1.z;
+          h[4 * c + 3] = x1.w;
         }
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
+#pragma unroll
+      for (int j = 0; j < TC_BK; ++j) split(h[j], h[j], l[j]);
+      // A slot it % 2 is free once the MMAs of chunk it - 2 have completed
+      if (it >= TC_A_SLOTS) {
+        const bool okA = mbar_wait(aempty(it % TC_A_SLOTS), (uint32_t)(it / TC_A_SLOTS - 1) & 1u, abort_flag, a);
+        if (bar_any(!okA)) {
+          aborted = true;
+          break;
+        }
+        tc_fence_after();
+      }
+      const uint32_t ta = tmem + lane_base + a_col + (uint32_t)(64 * (it % TC_A_SLOTS));
+      tmem_st32(ta, h);
+      tmem_st32(ta + 32u, l);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
       mbar_arrive(tfull(s));
       // the previous block is drained once this block has a few chunks queued
       if ((it % TC_DRAIN) == TC_DRAIN_LAG && it >= TC_DRAIN) {
