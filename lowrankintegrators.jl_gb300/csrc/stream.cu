@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "../../include/lri.h"
+#include "core_svd.h"
 #include "engine.cuh"
 #include "tc_pass.h"
 
@@ -2198,12 +2199,33 @@ struct StreamOps {
     const int R = (int)s->R;
     T* S = tp(s->S);
     cudaError_t e;
-    const int abytes = 200 * 1024;  // CORE_MAT + tiles
-    static std::atomic<uint64_t> attr_done{0};
-    if ((e = set_smem_limit(core_step<T, ST>, abytes, attr_done)) != cudaSuccess) return e;
     // S~ = Mh S0 Nh^T + D on the active block, over the whole GPU (T1 in block 14, S~ in block 13)
     form_t1<T><<<64, 256, 0, st>>>(R, s->d_rank, S, blk(4), blk(14));
     form_core<<<128, 256, 0, st>>>(R, s->d_rank, blk(3), blk(14), blk(5), blk(13));
+    if constexpr (std::is_same<T, float>::value) {
+      // FP32 panels: the SVD on a thread-block cluster (blocks 6, 7, 10..12 as scratch)
+      CoreSvdArgs ca{};
+      ca.R = R;
+      ca.F = blk(13);
+      ca.S0 = S;
+      ca.rank = s->d_rank;
+      ca.tol = s->tol;
+      ca.rmin = s->rmin;
+      ca.scr[0] = blk(6);
+      ca.scr[1] = blk(7);
+      ca.scr[2] = blk(10);
+      ca.scr[3] = blk(11);
+      ca.scr[4] = blk(12);
+      ca.P1 = blk(8);
+      ca.Q1 = blk(9);
+      ca.status = s->d_status;
+      ca.st_noconv = ST_SVD_NOCONV;
+      ca.st_nonfinite = ST_NONFINITE;
+      return core_svd_cluster(ca, st);
+    }
+    const int abytes = 200 * 1024;  // CORE_MAT + tiles
+    static std::atomic<uint64_t> attr_done{0};
+    if ((e = set_smem_limit(core_step<T, ST>, abytes, attr_done)) != cudaSuccess) return e;
     ST* scr = reinterpret_cast<ST*>(blk(6));  // blocks 6 and 7: 2 w^2 values
     // blocks 10..12: FP32 copies and double-float products of the mixed-precision SVD
     core_step<T, ST><<<1, NTS, abytes, st>>>(R, blk(13), S, s->d_rank, s->tol, s->rmin, scr, scr + (int64_t)w * w,
