@@ -92,20 +92,81 @@ __device__ __forceinline__ dfloat ld_cg(const dfloat* p) {
   return dfloat(v.x, v.y);
 }
 
+// Rotation parameters of a pair with al = |x|^2, be = |y|^2, ga = x.y: the
+// measure dl = |ga| / sqrt(al be), and, when dl > eps, tan = t of the
+// rotation angle (zeta = (be - al) / 2 ga, t = sign(zeta) / (|zeta| +
+// sqrt(1 + zeta^2))) with cs = (1 + t^2)^(-1/2), sn = cs t.  The angle needs
+// FP32 accuracy only (an angle off by a relative delta leaves delta of the
+// pair's product, far below the next sweep's quadratic residual); cs and sn
+// are orthonormal to the working precision, so the right vectors stay
+// orthogonal.  FP32 approximate intrinsics (MUFU) keep the rotation's
+// dependency chain short.
+__device__ __forceinline__ float rot_tan(float d, float ga) {
+  const float zeta = __fdividef(d, 2.0f * ga);
+  const float az = fabsf(zeta);
+  return (az > 1.0e15f) ? __fdividef(0.5f, zeta)
+                        : copysignf(__fdividef(1.0f, az + sqrtf(fmaf(zeta, zeta, 1.0f))), zeta);
+}
+
+__device__ __forceinline__ bool rot_params(float al, float be, float ga, float eps, float& cs, float& sn, float& dl) {
+  dl = fabsf(ga) * rsqrtf(al) * rsqrtf(be);
+  if (!(dl > eps) || ga == 0.0f) return false;
+  const float t = rot_tan(be - al, ga);
+  cs = rsqrtf(fmaf(t, t, 1.0f));
+  sn = cs * t;
+  return true;
+}
+
+// (1 + t^2)^(-1/2) in double-float: the FP32 estimate and one Newton step
+// y (1 + e / 2), e = 1 - q y^2 (relative error about 1e-13)
+__device__ __forceinline__ dfloat rsqrt_1pt2(float t) {
+  const dfloat q = fma(dfloat(t), dfloat(t), dfloat(1.0f));
+  const float y = rsqrtf(q.hi);
+  const dfloat e = dfloat(1.0f) - q * (dfloat(y) * dfloat(y));
+  return lri_df::fast_two_sum(y, 0.5f * y * e.hi);
+}
+
+__device__ __forceinline__ bool rot_params(dfloat al, dfloat be, dfloat ga, dfloat eps, dfloat& cs, dfloat& sn,
+                                           float& dl) {
+  dl = fabsf(ga.hi) * rsqrtf(al.hi) * rsqrtf(be.hi);
+  if (!(dl > eps.hi) || ga.hi == 0.0f) return false;
+  const float t = rot_tan((be - al).hi, ga.hi);  // be - al in double-float: no cancellation
+  cs = rsqrt_1pt2(t);
+  sn = cs * dfloat(t);
+  return true;
+}
+
 // One Jacobi rotation of columns (ap, aq) with right vectors (vp, vq) by a
-// group of G lanes (gl = lane in the group); every lane of the warp takes part
-// in the reductions.  Same test and rotation as the one-CTA sweeps.
-template <typename T>
-__device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool valid, int wa, int gl, int G, T eps,
-                                            T tiny, T reach, bool skip_noise, ClusterState& cs) {
+// group of G lanes (gl = lane in the group; the group's rows i = gl + k G stay
+// in registers between the dot products and the rotation); every lane of the
+// warp takes part in the reductions.  Same test and rotation as the one-CTA
+// sweeps, with the parameters above.  A rotation sets fl and raises dm (the
+// rotation measure) in the lane's registers; the sweep reduces them once at
+// its end.
+template <typename T, int G>
+__device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool valid, int wa, int gl, T eps, T tiny,
+                                            T reach, bool skip_noise, unsigned& fl, float& dm) {
+  constexpr int KR = (CORE_SVD_MAX_WA + G - 1) / G;
+  T x[KR], y[KR];
   T al = T(0), be = T(0), ga = T(0);
-  if (valid)
-    for (int i = gl; i < wa; i += G) {
-      const T x = ap[i], y = aq[i];
-      al = fma(x, x, al);
-      be = fma(y, y, be);
-      ga = fma(x, y, ga);
+#pragma unroll
+  for (int k = 0; k < KR; ++k) {
+    const int i = gl + k * G;
+    if (valid && i < wa) {
+      x[k] = ap[i];
+      y[k] = aq[i];
+    } else {
+      x[k] = T(0);
+      y[k] = T(0);
     }
+    al = fma_acc(x[k], x[k], al);
+    be = fma_acc(y[k], y[k], be);
+    ga = fma_acc(x[k], y[k], ga);
+  }
+  al = renorm(al);
+  be = renorm(be);
+  ga = renorm(ga);
+#pragma unroll
   for (int o = G >> 1; o > 0; o >>= 1) {
     al += shfl_xor(al, o);
     be += shfl_xor(be, o);
@@ -113,28 +174,28 @@ __device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool val
   }
   const bool live =
       valid && (skip_noise ? (al > tiny && be > tiny && (al > reach || be > reach)) : (al > tiny || be > tiny));
-  if (live && fabs(ga) > eps * sqrt(al) * sqrt(be) && ga != T(0)) {
-    const T zeta = (be - al) / (T(2) * ga);
-    const T tt = (fabs(zeta) > T(1.0e15)) ? T(0.5) / zeta
-                                           : copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-    const T cs_ = T(1) / sqrt(T(1) + tt * tt);
-    const T sn = cs_ * tt;
-    for (int i = gl; i < wa; i += G) {
-      const T x = ap[i], y = aq[i];
-      ap[i] = cs_ * x - sn * y;
-      aq[i] = sn * x + cs_ * y;
+  T cs_, sn;
+  float dl;
+  if (live && rot_params(al, be, ga, eps, cs_, sn, dl)) {
+#pragma unroll
+    for (int k = 0; k < KR; ++k) {
+      const int i = gl + k * G;
+      if (i < wa) {
+        ap[i] = cs_ * x[k] - sn * y[k];
+        aq[i] = sn * x[k] + cs_ * y[k];
+      }
     }
-    for (int i = gl; i < wa; i += G) {
-      const T x = vp[i], y = vq[i];
-      vp[i] = cs_ * x - sn * y;
-      vq[i] = sn * x + cs_ * y;
+#pragma unroll
+    for (int k = 0; k < KR; ++k) {
+      const int i = gl + k * G;
+      if (i < wa) {
+        const T u = vp[i], v = vq[i];
+        vp[i] = cs_ * u - sn * v;
+        vq[i] = sn * u + cs_ * v;
+      }
     }
-    if (gl == 0) {
-      const float dl =
-          (float)as_double(fabs(ga)) / ((float)as_double(sqrt(al)) * (float)as_double(sqrt(be)));
-      atomicOr(&cs.lflag, 1u);
-      atomicMax(&cs.ldmax, __float_as_uint(dl));
-    }
+    fl = 1u;
+    dm = fmaxf(dm, dl);
   }
 }
 
@@ -184,6 +245,12 @@ __device__ bool cluster_jacobi(cg::cluster_group& cl, ClusterState& cs, T* base,
   const int wbe = wb + (wb & 1);  // even number of players inside a block
   const int G = (wbe <= CS_NT / 32) ? 32 : 16;
   const int gid = tid / G, gl = tid % G;
+  auto rotate = [&](T* ap, T* aq, T* vp, T* vq, bool valid, unsigned& fl, float& dm) {
+    if (G == 32)
+      rotate_pair<T, 32>(ap, aq, vp, vq, valid, wa, gl, eps, tiny, reach, skip_noise, fl, dm);
+    else
+      rotate_pair<T, 16>(ap, aq, vp, vq, valid, wa, gl, eps, tiny, reach, skip_noise, fl, dm);
+  };
   const size_t bsz16 = bstride * sizeof(T) / 16;
   bool converged = false;
   for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
@@ -191,6 +258,8 @@ __device__ bool cluster_jacobi(cg::cluster_group& cl, ClusterState& cs, T* base,
       cs.lflag = 0u;
       cs.ldmax = 0u;
     }
+    unsigned fl = 0u;  // this lane's group rotated in this sweep
+    float dm = 0.0f;   // and its largest rotation measure
     __syncthreads();
     for (int t = 0; t < CS_NBLK - 1; ++t) {
       const int b0 = blk_first(cr, t), b1 = blk_second(cr, t);
@@ -218,8 +287,8 @@ __device__ bool cluster_jacobi(cg::cluster_group& cl, ClusterState& cs, T* base,
           const bool valid = gid < wbe && y < wb && b * wb + y < wa;
           T* Bk = slot ? B1 : B0;
           const int xs = valid ? x : 0, ys = valid ? y : 0;
-          rotate_pair<T>(Bk + (size_t)xs * wa, Bk + (size_t)ys * wa, Bk + (size_t)(wb + xs) * wa,
-                         Bk + (size_t)(wb + ys) * wa, valid, wa, gl, G, eps, tiny, reach, skip_noise, cs);
+          rotate(Bk + (size_t)xs * wa, Bk + (size_t)ys * wa, Bk + (size_t)(wb + xs) * wa, Bk + (size_t)(wb + ys) * wa,
+                 valid, fl, dm);
           __syncthreads();
         }
       }
@@ -240,7 +309,7 @@ __device__ bool cluster_jacobi(cg::cluster_group& cl, ClusterState& cs, T* base,
           vp = vq;
           vq = t1;
         }
-        rotate_pair<T>(ap, aq, vp, vq, valid, wa, gl, G, eps, tiny, reach, skip_noise, cs);
+        rotate(ap, aq, vp, vq, valid, fl, dm);
         __syncthreads();
       }
       // every block to its place in the next round (buffer cur ^ 1)
@@ -252,19 +321,32 @@ __device__ bool cluster_jacobi(cg::cluster_group& cl, ClusterState& cs, T* base,
         float4* dst = cl.map_shared_rank(reinterpret_cast<float4*>(block(cur ^ 1, ds)), dk);
         for (size_t e = tid; e < bsz16; e += CS_NT) dst[e] = src[e];
       }
-      if (t == CS_NBLK - 2 && tid < CS_C) {
-        *cl.map_shared_rank(&cs.flag[sweep & 1][cr], tid) = cs.lflag;
-        *cl.map_shared_rank(&cs.dmax[sweep & 1][cr], tid) = cs.ldmax;
+      if (t == CS_NBLK - 2) {
+        // the sweep's flag and largest measure: lanes, warps, then every CTA
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+          dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+        }
+        if (lane == 0) {
+          atomicOr(&cs.lflag, fl);
+          atomicMax(&cs.ldmax, __float_as_uint(dm));  // non-negative: the bits order as the values
+        }
+        __syncthreads();
+        if (tid < CS_C) {
+          *cl.map_shared_rank(&cs.flag[sweep & 1][cr], tid) = cs.lflag;
+          *cl.map_shared_rank(&cs.dmax[sweep & 1][cr], tid) = cs.ldmax;
+        }
       }
       cl.sync();
       cur ^= 1;
     }
-    unsigned any = 0u, dm = 0u;
+    unsigned any = 0u, dmc = 0u;
     for (int k = 0; k < CS_C; ++k) {
       any |= cs.flag[sweep & 1][k];
-      dm = max(dm, cs.dmax[sweep & 1][k]);
+      dmc = max(dmc, cs.dmax[sweep & 1][k]);
     }
-    converged = (any == 0u) || (__uint_as_float(dm) <= delta_stop);
+    converged = (any == 0u) || (__uint_as_float(dmc) <= delta_stop);
   }
   return converged;
 }
