@@ -203,9 +203,13 @@ __global__ void __launch_bounds__(256) pass_cols(int n, int m, int R, const int3
 }
 
 // ---------------------------------------------------------------------------
-// Gram partials: part[blk] (a x c, FP64, ld a) = X(rows of blk)^T Y(rows),
-// X (N x a, ld ldx), Y (N x c, ld ldy); a, c <= 2*SMAX.  Grid
-// (row blocks of GROWS) x (64 x 64 output tiles).  Then gram_reduce.
+// Gram partials: part[blk] = X(rows of blk)^T Y(rows) on the active columns,
+// X (N x a, ld ldx), Y (N x c, ld ldy); a, c <= 2*SMAX.  A panel of 2R
+// columns has the first r of each half active, one of R (or fewer) columns
+// the first r (r = *rank, read on the device; the other columns are zero).
+// The partial holds entry (ia, jc) of the active indices at ia + jc a (FP64).
+// Grid (row blocks of GROWS) x (64 x 64 tiles of the largest active block);
+// tiles beyond the active sizes exit.  Then gram_reduce.
 // ---------------------------------------------------------------------------
 // FP32 panels: exact products, double-float sums (the FP64 pipe of GB300
 // runs at 1/64 of the FP32 rate); FP64 panels: FP64.
@@ -216,17 +220,31 @@ __device__ __forceinline__ dfloat gacc_mul(dfloat acc, float x, float y) { retur
 __device__ __forceinline__ double gacc_val(double a) { return a; }
 __device__ __forceinline__ double gacc_val(dfloat a) { return (double)a.hi + (double)a.lo; }
 
+// active width of a panel of `a` columns (2R: both halves)
+__device__ __forceinline__ int panel_active(int a, int r, int R) { return (a == 2 * R) ? 2 * r : min(a, r); }
+// panel column of active index j
+__device__ __forceinline__ int panel_col(int a, int j, int r, int R) { return (a == 2 * R) ? act_col(j, r, R) : j; }
+// active index of panel column p, or -1
+__device__ __forceinline__ int panel_act_index(int a, int p, int r, int R) {
+  if (a == 2 * R) return (p < R) ? (p < r ? p : -1) : (p - R < r ? r + (p - R) : -1);
+  return (p < r) ? p : -1;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* __restrict__ X, int ldx,
-                                                 const T* __restrict__ Y, int ldy, double* __restrict__ part) {
+__global__ void __launch_bounds__(256) gram_part(int N, int a, int c, int R, const int32_t* __restrict__ rank,
+                                                 const T* __restrict__ X, int ldx, const T* __restrict__ Y, int ldy,
+                                                 double* __restrict__ part) {
   using A = typename GramAcc<T>::type;
   constexpr int TI = 32;
   __shared__ T xs[TI][65];
   __shared__ T ys[TI][65];
   const int tid = threadIdx.x;
   const int blk = blockIdx.x;
+  const int r = min(R, (int)*rank);
+  const int ka = panel_active(a, r, R), kc = panel_active(c, r, R);
   const int ta = blockIdx.y % ((a + 63) / 64), tc = blockIdx.y / ((a + 63) / 64);
   const int a0 = ta * 64, c0 = tc * 64;
+  if (a0 >= ka || c0 >= kc) return;  // the whole CTA
   const int r0 = blk * GROWS, r1 = min(N, r0 + GROWS);
   const int pa = tid & 15, pc = tid >> 4;  // 4 x 4 outputs: a0 + 4pa.., c0 + 4pc..
   A acc[4][4];
@@ -239,8 +257,8 @@ __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* _
       const int ii = e % TI, k = e / TI;
       const int i = i0 + ii;
       const bool ok = i < r1;
-      xs[ii][k] = (ok && a0 + k < a) ? X[i + (int64_t)(a0 + k) * ldx] : T(0);
-      ys[ii][k] = (ok && c0 + k < c) ? Y[i + (int64_t)(c0 + k) * ldy] : T(0);
+      xs[ii][k] = (ok && a0 + k < ka) ? X[i + (int64_t)panel_col(a, a0 + k, r, R) * ldx] : T(0);
+      ys[ii][k] = (ok && c0 + k < kc) ? Y[i + (int64_t)panel_col(c, c0 + k, r, R) * ldy] : T(0);
     }
     __syncthreads();
 #pragma unroll 4
@@ -267,18 +285,23 @@ __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, const T* _
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int ia = a0 + 4 * pa + p, jc = c0 + 4 * pc + q;
-      if (ia < a && jc < c) dst[ia + (int64_t)jc * a] = gacc_val(acc[p][q]);
+      if (ia < ka && jc < kc) dst[ia + (int64_t)jc * a] = gacc_val(acc[p][q]);
     }
 }
 
-// out (a x c, ld ldo) = alpha * sum_blk part[blk] + beta * out
-__global__ void gram_reduce(int nblk, int a, int c, const double* __restrict__ part, double alpha, double beta,
-                            double* __restrict__ out, int ldo) {
+// out (a x c, ld ldo) = alpha * sum_blk part[blk] + beta * out on the active
+// entries, beta * out elsewhere (the Gram of zero columns)
+__global__ void gram_reduce(int nblk, int a, int c, int R, const int32_t* __restrict__ rank,
+                            const double* __restrict__ part, double alpha, double beta, double* __restrict__ out,
+                            int ldo) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= a * c) return;
-  double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * a * c + o];
+  const int r = min(R, (int)*rank);
   const int i = o % a, j = o / a;
+  const int ia = panel_act_index(a, i, r, R), jc = panel_act_index(c, j, r, R);
+  double s = 0.0;
+  if (ia >= 0 && jc >= 0)
+    for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * a * c + ia + (int64_t)jc * a];
   double* d = out + i + (int64_t)j * ldo;
   *d = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *d);
 }
@@ -1853,8 +1876,9 @@ struct StreamOps {
                    double* out, int ldo) const {
     const int nblk = (N + GROWS - 1) / GROWS;
     dim3 grid(nblk, ((a + 63) / 64) * ((c + 63) / 64));
-    gram_part<T><<<grid, 256, 0, st>>>(N, a, c, X, ldx, Y, ldy, s->part);
-    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(nblk, a, c, s->part, alpha, beta, out, ldo);
+    gram_part<T><<<grid, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, s->part);
+    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(nblk, a, c, (int)s->R, s->d_rank, s->part, alpha, beta, out,
+                                                     ldo);
     return cudaGetLastError();
   }
   cudaError_t mul(int N, int a, int c, const T* X, int ldx, const double* B, int ldb, T beta, T* out,
