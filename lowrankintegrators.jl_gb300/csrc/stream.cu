@@ -43,7 +43,6 @@ namespace lri {
 namespace {
 
 constexpr int SMAX = 96;      // largest r_max
-constexpr int GROWS = 128;    // rows per Gram partial block (a few hundred CTAs for the panels here)
 
 // active column j (0 <= j < ka) -> panel column: the first r of each half
 __device__ __forceinline__ int act_col(int j, int r, int R) { return (j < r) ? j : R + (j - r); }
@@ -203,13 +202,15 @@ __global__ void __launch_bounds__(256) pass_cols(int n, int m, int R, const int3
 }
 
 // ---------------------------------------------------------------------------
-// Gram partials: part[blk] = X(rows of blk)^T Y(rows) on the active columns,
-// X (N x a, ld ldx), Y (N x c, ld ldy); a, c <= 2*SMAX.  A panel of 2R
-// columns has the first r of each half active, one of R (or fewer) columns
-// the first r (r = *rank, read on the device; the other columns are zero).
-// The partial holds entry (ia, jc) of the active indices at ia + jc a (FP64).
-// Grid (row blocks of GROWS) x (64 x 64 tiles of the largest active block);
-// tiles beyond the active sizes exit.  Then gram_reduce.
+// Gram products out = X^T Y on the active columns, X (N x a, ld ldx), Y
+// (N x c, ld ldy); a, c <= 2*SMAX.  A panel of 2R columns has the first r of
+// each half active, one of R (or fewer) columns the first r (r = *rank, read
+// on the device; the other columns are zero).  The active block is cut into
+// 64 x 64 tiles (ntile of them) and the rows into nrb blocks, nrb =
+// max(1, ctas / ntile) rounded to whole 32-row slabs, so every rank keeps
+// about `ctas` CTAs busy.  Work item (row block, tile) writes its 64 x 64
+// partial at part[item * 4096]; gram_reduce sums the row blocks in order
+// (deterministic).
 // ---------------------------------------------------------------------------
 // FP32 panels: exact products, double-float sums (the FP64 pipe of GB300
 // runs at 1/64 of the FP32 rate); FP64 panels: FP64.
@@ -219,6 +220,9 @@ __device__ __forceinline__ double gacc_mul(double acc, double x, double y) { ret
 __device__ __forceinline__ dfloat gacc_mul(dfloat acc, float x, float y) { return acc_mul_acc(acc, x, y); }
 __device__ __forceinline__ double gacc_val(double a) { return a; }
 __device__ __forceinline__ double gacc_val(dfloat a) { return (double)a.hi + (double)a.lo; }
+
+constexpr int GRAM_TILE = 64;
+constexpr int GRAM_TILE_MAX = 9;  // (2 SMAX / 64)^2 tiles
 
 // active width of a panel of `a` columns (2R: both halves)
 __device__ __forceinline__ int panel_active(int a, int r, int R) { return (a == 2 * R) ? 2 * r : min(a, r); }
@@ -230,78 +234,96 @@ __device__ __forceinline__ int panel_act_index(int a, int p, int r, int R) {
   return (p < r) ? p : -1;
 }
 
+// the split of a Gram product: tiles of the active block, row blocks
+struct GramSplit {
+  int ka, kc, ta, ntile, rows, nrb;
+};
+__device__ __forceinline__ GramSplit gram_split(int N, int a, int c, int R, int r, int ctas) {
+  GramSplit g;
+  g.ka = panel_active(a, r, R);
+  g.kc = panel_active(c, r, R);
+  g.ta = (g.ka + GRAM_TILE - 1) / GRAM_TILE;
+  g.ntile = g.ta * ((g.kc + GRAM_TILE - 1) / GRAM_TILE);
+  const int want = max(1, ctas / max(1, g.ntile));
+  g.rows = max(32, (((N + want - 1) / want) + 31) / 32 * 32);
+  g.nrb = (N + g.rows - 1) / g.rows;
+  return g;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, int R, const int32_t* __restrict__ rank,
                                                  const T* __restrict__ X, int ldx, const T* __restrict__ Y, int ldy,
                                                  double* __restrict__ part) {
   using A = typename GramAcc<T>::type;
   constexpr int TI = 32;
-  __shared__ T xs[TI][65];
-  __shared__ T ys[TI][65];
+  __shared__ T xs[TI][GRAM_TILE + 1];
+  __shared__ T ys[TI][GRAM_TILE + 1];
   const int tid = threadIdx.x;
-  const int blk = blockIdx.x;
   const int r = min(R, (int)*rank);
-  const int ka = panel_active(a, r, R), kc = panel_active(c, r, R);
-  const int ta = blockIdx.y % ((a + 63) / 64), tc = blockIdx.y / ((a + 63) / 64);
-  const int a0 = ta * 64, c0 = tc * 64;
-  if (a0 >= ka || c0 >= kc) return;  // the whole CTA
-  const int r0 = blk * GROWS, r1 = min(N, r0 + GROWS);
+  const GramSplit g = gram_split(N, a, c, R, r, (int)gridDim.x);
   const int pa = tid & 15, pc = tid >> 4;  // 4 x 4 outputs: a0 + 4pa.., c0 + 4pc..
-  A acc[4][4];
-#pragma unroll
-  for (int p = 0; p < 4; ++p)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[p][q] = A(0.0);
-  for (int i0 = r0; i0 < r1; i0 += TI) {
-    for (int e = tid; e < TI * 64; e += 256) {
-      const int ii = e % TI, k = e / TI;
-      const int i = i0 + ii;
-      const bool ok = i < r1;
-      xs[ii][k] = (ok && a0 + k < ka) ? X[i + (int64_t)panel_col(a, a0 + k, r, R) * ldx] : T(0);
-      ys[ii][k] = (ok && c0 + k < kc) ? Y[i + (int64_t)panel_col(c, c0 + k, r, R) * ldy] : T(0);
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int ii = 0; ii < TI; ++ii) {
-      T xv[4], yv[4];
-#pragma unroll
-      for (int p = 0; p < 4; ++p) xv[p] = xs[ii][4 * pa + p];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) yv[q] = ys[ii][4 * pc + q];
-#pragma unroll
-      for (int p = 0; p < 4; ++p)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[p][q] = gacc_mul(acc[p][q], xv[p], yv[q]);
-    }
+  for (int item = blockIdx.x; item < g.nrb * g.ntile; item += gridDim.x) {
+    const int rb = item / g.ntile, tile = item % g.ntile;
+    const int a0 = (tile % g.ta) * GRAM_TILE, c0 = (tile / g.ta) * GRAM_TILE;
+    const int r0 = rb * g.rows, r1 = min(N, r0 + g.rows);
+    A acc[4][4];
 #pragma unroll
     for (int p = 0; p < 4; ++p)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[p][q] = renorm(acc[p][q]);
-    __syncthreads();
-  }
-  double* dst = part + (int64_t)blk * a * c;
+      for (int q = 0; q < 4; ++q) acc[p][q] = A(0.0);
+    for (int i0 = r0; i0 < r1; i0 += TI) {
+      __syncthreads();  // the previous slab (or item) is consumed
+      for (int e = tid; e < TI * GRAM_TILE; e += 256) {
+        const int ii = e % TI, k = e / TI;
+        const int i = i0 + ii;
+        const bool ok = i < r1;
+        xs[ii][k] = (ok && a0 + k < g.ka) ? X[i + (int64_t)panel_col(a, a0 + k, r, R) * ldx] : T(0);
+        ys[ii][k] = (ok && c0 + k < g.kc) ? Y[i + (int64_t)panel_col(c, c0 + k, r, R) * ldy] : T(0);
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int ii = 0; ii < TI; ++ii) {
+        T xv[4], yv[4];
 #pragma unroll
-  for (int p = 0; p < 4; ++p)
+        for (int p = 0; p < 4; ++p) xv[p] = xs[ii][4 * pa + p];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int ia = a0 + 4 * pa + p, jc = c0 + 4 * pc + q;
-      if (ia < ka && jc < kc) dst[ia + (int64_t)jc * a] = gacc_val(acc[p][q]);
+        for (int q = 0; q < 4; ++q) yv[q] = ys[ii][4 * pc + q];
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[p][q] = gacc_mul(acc[p][q], xv[p], yv[q]);
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = renorm(acc[p][q]);
     }
+    double* dst = part + (int64_t)item * GRAM_TILE * GRAM_TILE;
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dst[(4 * pa + p) + (4 * pc + q) * GRAM_TILE] = gacc_val(acc[p][q]);
+  }
 }
 
-// out (a x c, ld ldo) = alpha * sum_blk part[blk] + beta * out on the active
-// entries, beta * out elsewhere (the Gram of zero columns)
-__global__ void gram_reduce(int nblk, int a, int c, int R, const int32_t* __restrict__ rank,
+// out (a x c, ld ldo) = alpha * sum of the row blocks' partials + beta * out
+// on the active entries, beta * out elsewhere (the Gram of zero columns);
+// `ctas` as in gram_part's launch
+__global__ void gram_reduce(int N, int a, int c, int R, const int32_t* __restrict__ rank, int ctas,
                             const double* __restrict__ part, double alpha, double beta, double* __restrict__ out,
                             int ldo) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= a * c) return;
   const int r = min(R, (int)*rank);
+  const GramSplit g = gram_split(N, a, c, R, r, ctas);
   const int i = o % a, j = o / a;
   const int ia = panel_act_index(a, i, r, R), jc = panel_act_index(c, j, r, R);
   double s = 0.0;
-  if (ia >= 0 && jc >= 0)
-    for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * a * c + ia + (int64_t)jc * a];
+  if (ia >= 0 && jc >= 0) {
+    const int tile = (ia / GRAM_TILE) + (jc / GRAM_TILE) * g.ta;
+    const int64_t off = (ia % GRAM_TILE) + (int64_t)(jc % GRAM_TILE) * GRAM_TILE;
+    for (int b = 0; b < g.nrb; ++b) s += part[((int64_t)b * g.ntile + tile) * GRAM_TILE * GRAM_TILE + off];
+  }
   double* d = out + i + (int64_t)j * ldo;
   *d = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *d);
 }
@@ -1810,6 +1832,7 @@ using namespace lri;
 struct lri_stream {
   int32_t dtype;
   int64_t n, m, R;
+  int sms = 0;  // streaming multiprocessors of the device (Gram launches: two CTAs per SM)
   double tol;
   int32_t rmin;
   size_t es;
@@ -1865,6 +1888,8 @@ namespace {
 constexpr int kBlocksSmall = 24;  // FP64 scratch of (2R)^2 each (14, 15, 23: refresh; 13..23: the Burgers step)
 constexpr int kZmax = 8;          // pair splits of the Khatri-Rao products (fill the GPU for short panels)
 
+int gram_ctas(const lri_stream* s) { return 2 * std::max(1, s->sms); }
+
 template <typename T>
 struct StreamOps {
   lri_stream* s;
@@ -1874,10 +1899,9 @@ struct StreamOps {
 
   cudaError_t gram(int N, int a, int c, const T* X, int ldx, const T* Y, int ldy, double alpha, double beta,
                    double* out, int ldo) const {
-    const int nblk = (N + GROWS - 1) / GROWS;
-    dim3 grid(nblk, ((a + 63) / 64) * ((c + 63) / 64));
-    gram_part<T><<<grid, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, s->part);
-    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(nblk, a, c, (int)s->R, s->d_rank, s->part, alpha, beta, out,
+    const int ctas = gram_ctas(s);
+    gram_part<T><<<ctas, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, s->part);
+    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, ctas, s->part, alpha, beta, out,
                                                      ldo);
     return cudaGetLastError();
   }
@@ -2404,8 +2428,12 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   s->rmin = r_min;
   s->es = dtype == LRI_F32 ? 4 : 8;
   const int64_t R = r_max;
-  const int64_t nblk = (std::max(n, m) + GROWS - 1) / GROWS;
   cudaError_t e = cudaSuccess;
+  {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   auto alloc = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMalloc(p, bytes < 16 ? 16 : bytes);
   };
@@ -2416,7 +2444,9 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   alloc(&s->Xk, s->es * n * R);
   alloc(&s->Xl, s->es * m * R);
   alloc(&s->Zp, s->es * std::max(n, m) * 2 * R);
-  alloc((void**)&s->part, sizeof(double) * nblk * 4 * R * R);
+  // Gram partials: at most max(ctas, tiles) 64 x 64 work items
+  alloc((void**)&s->part, sizeof(double) * (size_t)(lri::gram_ctas(s) + lri::GRAM_TILE_MAX) * lri::GRAM_TILE *
+                              lri::GRAM_TILE);
   alloc((void**)&s->small, sizeof(double) * kBlocksSmall * 4 * R * R);
   alloc((void**)&s->d_ncols, sizeof(int32_t));
   if (e == cudaSuccess && dtype == LRI_F32 && lri::tc_pass_supported(n, m, (int)R)) {
