@@ -624,104 +624,152 @@ __device__ bool jacobi_svd_mixed(int P, const dfloat* a, dfloat* as, dfloat* v, 
 // k orthonormal columns up to about (error of G) / tol_rel and zero columns
 // after them.  Columns whose squared norm is <= tol_rel of the largest are
 // rounding noise of the panel and are dropped before the scaling (which
-// would hide that).  Factor and inverse in shared memory (2 r^2 ST).
+// would hide that).  Factor and inverse in shared memory (2 r (r + 1) ST); one CTA
+// of NTP threads: the pivot steps are a chain of barriers, so few warps.
+// R^{-1} by 16 x 16 blocks: the diagonal blocks by back substitution (one
+// warp each, a lane per column), then the block diagonals d = 1, 2, ... as
+// Ri_IJ = -Ri_II sum_{K = I+1..J} R_IK Ri_KJ (one thread per entry).
+constexpr int NTP = 256;
+constexpr int PCB = 16;  // block size of the triangular inverse
+static_assert(NTP == PCB * PCB, "one thread per entry of a 16 x 16 block");
 template <typename ST>
-__global__ void __launch_bounds__(NTS) pchol_factor(int a, const double* __restrict__ G, const int32_t* rank,
+__global__ void __launch_bounds__(NTP) pchol_factor(int a, const double* __restrict__ G, const int32_t* rank,
                                                     double tol_rel, double* __restrict__ Bout) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int r = min(a, (int)*rank);
-  ST* A = reinterpret_cast<ST*>(smraw);  // r x r, column-major
-  ST* Ri = A + r * r;                     // r x r
+  const int ld = r + 1;                   // odd: rows of A read across lanes hit distinct banks
+  ST* A = reinterpret_cast<ST*>(smraw);  // r x r, column-major, ld
+  ST* Ri = A + r * ld;                    // r x r, ld
   __shared__ double d[SMAX];
   __shared__ int piv[SMAX];
+  __shared__ double red[NTP / 32];
+  __shared__ __align__(16) unsigned char tb_raw[PCB * PCB * sizeof(ST)];
+  ST* Tb = reinterpret_cast<ST*>(tb_raw);
   __shared__ int pk_s, kk_s;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NWP = NTP / 32;
+  double gm = 0.0;
+  for (int j = tid; j < r; j += NTP) gm = fmax(gm, G[j + (int64_t)j * a]);
+  for (int o = 16; o > 0; o >>= 1) gm = fmax(gm, __shfl_xor_sync(0xffffffffu, gm, o));
+  if (lane == 0) red[warp] = gm;
+  __syncthreads();
   double gmax = 0.0;
-  for (int j = 0; j < r; ++j) gmax = fmax(gmax, G[j + (int64_t)j * a]);
-  for (int j = tid; j < r; j += NTS) {
+  for (int w = 0; w < NWP; ++w) gmax = fmax(gmax, red[w]);
+  for (int j = tid; j < r; j += NTP) {
     const double g = G[j + (int64_t)j * a];
     d[j] = (g > tol_rel * gmax && g > 0.0) ? 1.0 / sqrt(g) : 0.0;
     piv[j] = j;
   }
   __syncthreads();
-  for (int o = tid; o < r * r; o += NTS) {
+  for (int o = tid; o < r * r; o += NTP) {
     const int i = o % r, j = o / r;
-    A[o] = ST(d[i] * G[i + (int64_t)j * a] * d[j]);
+    A[i + j * ld] = ST(d[i] * G[i + (int64_t)j * a] * d[j]);
   }
   if (tid == 0) kk_s = r;
   __syncthreads();
   for (int k = 0; k < r; ++k) {
-    if (tid < 32) {  // pivot: the largest remaining diagonal entry (first on ties)
-      double best = -1.0;
+    if (warp == 0) {  // pivot: the largest remaining diagonal entry (first on ties), compared in ST
+      ST best = ST(-1.0);
       int bi = k;
-      for (int j = k + tid; j < r; j += 32) {
-        const double v = to_d(A[j + j * r]);
+      for (int j = k + lane; j < r; j += 32) {
+        const ST v = A[j + j * ld];
         if (v > best) { best = v; bi = j; }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const ST ob = shfl_xor(best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
       }
-      if (tid == 0) {
+      if (lane == 0) {
         pk_s = bi;
-        if (!(best > tol_rel)) kk_s = k;
+        if (!(best > ST(tol_rel))) kk_s = k;
       }
     }
     __syncthreads();
     if (kk_s == k) break;
     const int p = pk_s;
-    if (p != k) {  // symmetric swap of rows and columns k and p (R's rows above k: columns only)
-      for (int i = tid; i < r; i += NTS) {
-        const ST t = A[i + k * r];
-        A[i + k * r] = A[i + p * r];
-        A[i + p * r] = t;
-      }
-      __syncthreads();
-      for (int j = tid; j < r; j += NTS) {
-        const ST t = A[k + j * r];
-        A[k + j * r] = A[p + j * r];
-        A[p + j * r] = t;
-      }
-      if (tid == 0) {
-        const int t = piv[k];
-        piv[k] = piv[p];
-        piv[p] = t;
+    if (p != k) {
+      // symmetric swap of rows and columns k < p in one pass: R's rows above
+      // k swap columns only, the trailing symmetric block rows and columns,
+      // the diagonal entries trade places and A[k, p] = A[p, k] stays
+      for (int i = tid; i < r; i += NTP) {
+        if (i == k) {
+          const ST t = A[k + k * ld];
+          A[k + k * ld] = A[p + p * ld];
+          A[p + p * ld] = t;
+          const int tp = piv[k];
+          piv[k] = piv[p];
+          piv[p] = tp;
+        } else if (i != p) {
+          const ST t = A[i + k * ld];
+          A[i + k * ld] = A[i + p * ld];
+          A[i + p * ld] = t;
+          if (i > k) {
+            const ST u = A[k + i * ld];
+            A[k + i * ld] = A[p + i * ld];
+            A[p + i * ld] = u;
+          }
+        }
       }
       __syncthreads();
     }
-    const ST rkk = sqrt(A[k + k * r]);
+    const ST rkk = sqrt(A[k + k * ld]);
     const ST inv = ST(1.0) / rkk;
-    for (int j = k + 1 + tid; j < r; j += NTS) A[k + j * r] = A[k + j * r] * inv;
+    for (int j = k + 1 + tid; j < r; j += NTP) A[k + j * ld] = A[k + j * ld] * inv;
     __syncthreads();
-    if (tid == 0) A[k + k * r] = rkk;
-    // trailing update of the full symmetric block (rows and columns > k)
-    const int cnt = r - k - 1;
-    for (int e = tid; e < cnt * cnt; e += NTS) {
-      const int i = k + 1 + e % cnt, j = k + 1 + e / cnt;
-      A[i + j * r] = A[i + j * r] - A[k + i * r] * A[k + j * r];
+    if (tid == 0) A[k + k * ld] = rkk;
+    // trailing update of the full symmetric block (rows and columns > k):
+    // a warp per column, lanes down the rows
+    for (int j = k + 1 + warp; j < r; j += NWP) {
+      const ST akj = A[k + j * ld];
+      for (int i = k + 1 + lane; i < r; i += 32) A[i + j * ld] = A[i + j * ld] - A[k + i * ld] * akj;
     }
     __syncthreads();
   }
   const int kk = kk_s;
-  // R^{-1} (kk x kk) row by row from the bottom (one barrier per row)
-  for (int o = tid; o < r * r; o += NTS) Ri[o] = ST(0.0);
+  // R^{-1} (kk x kk, upper triangular; R in the upper triangle of A)
+  for (int o = tid; o < r * ld; o += NTP) Ri[o] = ST(0.0);
   __syncthreads();
-  for (int i = kk - 1; i >= 0; --i) {
-    const ST rii = ST(1.0) / A[i + i * r];
-    for (int j = i + tid; j < kk; j += NTS) {
-      ST sacc = (i == j) ? ST(1.0) : ST(0.0);
-      for (int q = i + 1; q <= j; ++q) sacc = sacc - A[i + q * r] * Ri[q + j * r];
-      Ri[i + j * r] = sacc * rii;
+  const int nb = (kk + PCB - 1) / PCB;
+  for (int b = warp; b < nb; b += NWP) {  // diagonal blocks: lane = column
+    const int b0 = b * PCB, mb = min(PCB, kk - b0);
+    if (lane < mb) {
+      const int j = b0 + lane;
+      Ri[j + j * ld] = ST(1.0) / A[j + j * ld];
+      for (int i = j - 1; i >= b0; --i) {
+        ST sacc = ST(0.0);
+        for (int q = i + 1; q <= j; ++q) sacc = sacc + A[i + q * ld] * Ri[q + j * ld];
+        Ri[i + j * ld] = -(sacc / A[i + i * ld]);
+      }
     }
-    __syncthreads();
   }
-  for (int o = tid; o < a * a; o += NTS) Bout[o] = 0.0;
   __syncthreads();
-  for (int o = tid; o < kk * kk; o += NTS) {
+  for (int dd = 1; dd < nb; ++dd)
+    for (int I = 0; I + dd < nb; ++I) {
+      const int i0 = I * PCB, j0 = (I + dd) * PCB;
+      const int mi = min(PCB, kk - i0), mj = min(PCB, kk - j0);
+      const int ii = tid % PCB, jj = tid / PCB;  // NTP = PCB^2 entries
+      const int i = i0 + ii, j = j0 + jj;
+      const bool ok = ii < mi && jj < mj;
+      if (ok) {  // T = sum_{K = I+1..J} R_IK Ri_KJ (Ri_KJ is zero below row j)
+        ST sacc = ST(0.0);
+        for (int q = i0 + PCB; q <= j; ++q) sacc = sacc + A[i + q * ld] * Ri[q + j * ld];
+        Tb[ii + jj * PCB] = sacc;
+      }
+      __syncthreads();
+      if (ok) {  // Ri_IJ = -Ri_II T
+        ST sacc = ST(0.0);
+        for (int q = i; q < i0 + mi; ++q) sacc = sacc + Ri[i + q * ld] * Tb[(q - i0) + jj * PCB];
+        Ri[i + j * ld] = -sacc;
+      }
+      __syncthreads();
+    }
+  for (int o = tid; o < a * a; o += NTP) Bout[o] = 0.0;
+  __syncthreads();
+  for (int o = tid; o < kk * kk; o += NTP) {
     const int i = o % kk, j = o / kk;
     const int pi = piv[i];
-    Bout[pi + (int64_t)j * a] = d[pi] * to_d(Ri[i + j * r]);
+    Bout[pi + (int64_t)j * a] = d[pi] * to_d(Ri[i + j * ld]);
   }
 }
 
@@ -1933,7 +1981,7 @@ struct StreamOps {
   using ST = typename SmallT<T>::type;
   cudaError_t pchol(int a, const double* G, double* B) const {
     static std::atomic<uint64_t> attr_done{0};
-    cudaError_t e = set_smem_limit(pchol_factor<ST>, (int)(2 * SMAX * SMAX * sizeof(ST)), attr_done);
+    cudaError_t e = set_smem_limit(pchol_factor<ST>, (int)(2 * SMAX * (SMAX + 1) * sizeof(ST)), attr_done);
     if (e != cudaSuccess) return e;
     // directions whose squared distance from the span of the others (unit
     // columns) is below tol_rel are treated as dependent.  The columns of
@@ -1942,7 +1990,7 @@ struct StreamOps {
     // double-float sums) and for FP64 panels (~1e-16), so that one
     // CholeskyQR pass afterwards is well conditioned.
     const double tol_rel = sizeof(T) == 4 ? 1e-11 : 1e-13;
-    pchol_factor<ST><<<1, NTS, 2 * (size_t)a * a * sizeof(ST), st>>>(a, G, s->d_rank, tol_rel, B);
+    pchol_factor<ST><<<1, NTP, 2 * (size_t)a * (a + 1) * sizeof(ST), st>>>(a, G, s->d_rank, tol_rel, B);
     return cudaGetLastError();
   }
   cudaError_t cholinv(int a, const double* G, double* B, double shift_rel) const {
