@@ -1484,31 +1484,37 @@ __global__ void s_stage_finish(int R, const int32_t* __restrict__ rank, int nz, 
 // tensor T' (np x ka, np = ka (ka + 1) / 2 pairs), all of which fit in shared
 // memory; one kernel per stage replaces the stencil, panel product,
 // Khatri-Rao and combine launches above (same arithmetic per entry, sums in
-// a different order).  One CTA per FUSED_BM rows, with one periodic halo row
-// on each side for the stencils and the Dx of the quadratic term.
+// a different order).  One CTA per FUSED_BMH rows (K and S flows, with one
+// periodic halo row on each side for the stencils and the Dx of the
+// quadratic term: 32 rows of Khatri-Rao work, one per thread and column
+// group) or FUSED_BML rows (L flow).  The tensor sits pair-major in shared
+// memory, tpt[p kpp + c] with kpp = ka rounded up to 4, plus 4: one 16-byte
+// load (a broadcast across the warp) serves four columns.
 // ---------------------------------------------------------------------------
-constexpr int FUSED_BM = 32;
+constexpr int FUSED_BMH = 30;
+constexpr int FUSED_BML = 64;
 constexpr int FUSED_KMAX = 32;
 
 // Four consecutive columns c0 .. c0 + 3 of one row of
 //   sum_{a <= b} KR(P, Q)_ab T'[p(a,b), c],  KR(P, Q)_ab = (P_a Q_b + P_b Q_a) / 2
-// (SAME: P == Q, KR = P_a P_b); P, Q: the row's ka values; T' column-major
-// in shared memory, tpt[c * np + p], zero beyond the active columns.  Each
-// tensor value read serves 4 (8) multiply-adds; a warp's threads share c0,
+// (SAME: P == Q, KR = P_a P_b); P, Q: the row's ka values; T' pair-major in
+// shared memory, tpt[p kpp + c], zero beyond the active columns.  Each
+// 16-byte tensor load serves 4 (8) multiply-adds; a warp's threads share c0,
 // so the tensor reads are broadcasts.
 template <typename T, bool SAME>
-__device__ __forceinline__ void kr_row4(int ka, int np, const T* P, const T* Q, const T* tpt, int c0, T (&acc)[4]) {
-  int p = 0;
+__device__ __forceinline__ void kr_row4(int ka, int kpp, const T* P, const T* Q, const T* tpt, int c0, T (&acc)[4]) {
+  const T* tp = tpt + c0;
   for (int a = 0; a < ka; ++a) {
     T g1[4] = {T(0), T(0), T(0), T(0)}, g2[4] = {T(0), T(0), T(0), T(0)};
-    for (int b = a; b < ka; ++b, ++p) {
+    for (int b = a; b < ka; ++b, tp += kpp) {
       const T qb = Q[b];
       const T pb = SAME ? qb : P[b];
+      T t[4];
+      ld_vec<4>(tp, t);
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const T t = tpt[(c0 + v) * np + p];
-        g1[v] = fma(qb, t, g1[v]);
-        if (!SAME) g2[v] = fma(pb, t, g2[v]);
+        g1[v] = fma(qb, t[v], g1[v]);
+        if (!SAME) g2[v] = fma(pb, t[v], g2[v]);
       }
     }
     const T pa = P[a];
@@ -1520,14 +1526,18 @@ __device__ __forceinline__ void kr_row4(int ka, int np, const T* P, const T* Q, 
   }
 }
 
-// the packed tensor's active block, column-major: tpt[c * np + p] = Tp[p + c PP]
-// for c < ka, zero for ka <= c < kap (kap = ka rounded up to 4)
+// row stride of the pair-major tensor in shared memory
+__host__ __device__ constexpr int tensor_kpp(int kap) { return kap + 4; }
+
+// the packed tensor's active block, pair-major: tpt[p kpp + c] = Tp[p + c PP]
+// for c < ka, zero for ka <= c < kpp (kap = ka rounded up to 4); global
+// reads run along the pairs (coalesced)
 template <typename T>
 __device__ __forceinline__ void load_tensor(int ka, int kap, const T* __restrict__ Tp, int PP, T* tpt) {
-  const int np = ka * (ka + 1) / 2;
-  for (int e = threadIdx.x; e < np * kap; e += blockDim.x) {
+  const int np = ka * (ka + 1) / 2, kpp = tensor_kpp(kap);
+  for (int e = threadIdx.x; e < np * kpp; e += blockDim.x) {
     const int pp = e % np, c = e / np;
-    tpt[e] = (c < ka) ? Tp[pp + (int64_t)c * PP] : T(0);
+    tpt[pp * kpp + c] = (c < ka) ? Tp[pp + (int64_t)c * PP] : T(0);
   }
 }
 
@@ -1550,16 +1560,16 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
   }
   const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3, ncg = kap / 4;
   const bool nonlin = (alpha != 0.0 || beta != 0.0);
-  T* tpt = reinterpret_cast<T*>(smraw);            // kap x np
-  T* zs = tpt + (nonlin ? np * kap : 0);            // (BM + 2) x ld: rows i0 - 1 .. i0 + BM
-  T* ks = zs + (FUSED_BM + 2) * ld;                 // (BM + 2) x ld: KR(Z, Z) T' (kap columns used)
-  T* ns = ks + (FUSED_BM + 2) * (kap | 1);          // ka x ka: N_nu
+  T* tpt = reinterpret_cast<T*>(smraw);            // np x kpp
+  T* zs = tpt + (nonlin ? np * tensor_kpp(kap) : 0);  // (BM + 2) x ld: rows i0 - 1 .. i0 + BM
+  T* ks = zs + (FUSED_BMH + 2) * ld;                 // (BM + 2) x ld: KR(Z, Z) T' (kap columns used)
+  T* ns = ks + (FUSED_BMH + 2) * (kap | 1);          // ka x ka: N_nu
   T* d1 = ns + ka * ka;                             // BM x ld: Dx Z
   const int ldk = kap | 1;
-  const int i0 = blockIdx.x * FUSED_BM;
+  const int i0 = blockIdx.x * FUSED_BMH;
   if (nonlin) load_tensor(ka, kap, Tp, PP, tpt);
-  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-    const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
+  for (int e = threadIdx.x; e < (FUSED_BMH + 2) * ka; e += blockDim.x) {
+    const int ii = e % (FUSED_BMH + 2), a = e / (FUSED_BMH + 2);
     int g = i0 - 1 + ii;
     g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
     zs[ii * ld + a] = Z[g + (int64_t)a * N];
@@ -1567,49 +1577,50 @@ __global__ void __launch_bounds__(256) burgers_k_stage(int N, int R, const int32
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) ns[e] = T(Nnu[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
   if (beta != 0.0)
-    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ncg; e += blockDim.x) {
-      const int ii = e % (FUSED_BM + 2), c0 = 4 * (e / (FUSED_BM + 2));
+    for (int e = threadIdx.x; e < (FUSED_BMH + 2) * ncg; e += blockDim.x) {
+      const int ii = e % (FUSED_BMH + 2), c0 = 4 * (e / (FUSED_BMH + 2));
       T acc[4] = {T(0), T(0), T(0), T(0)};
-      kr_row4<T, true>(ka, np, zs + ii * ld, zs + ii * ld, tpt, c0, acc);
+      kr_row4<T, true>(ka, tensor_kpp(kap), zs + ii * ld, zs + ii * ld, tpt, c0, acc);
 #pragma unroll
       for (int v = 0; v < 4; ++v) ks[ii * ldk + c0 + v] = acc[v];
     }
-  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int ii = e % FUSED_BM, a = e / FUSED_BM;
+  for (int e = threadIdx.x; e < FUSED_BMH * ka; e += blockDim.x) {
+    const int ii = e % FUSED_BMH, a = e / FUSED_BMH;
     d1[ii * ld + a] = T(ihx) * (zs[(ii + 2) * ld + a] - zs[ii * ld + a]);
   }
   __syncthreads();
-  const int rows = min(FUSED_BM, N - i0);
-  const int ncg_all = (R + 3) / 4;
-  for (int e = threadIdx.x; e < FUSED_BM * ncg_all; e += blockDim.x) {
-    const int ii = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
+  const int rows = min(FUSED_BMH, N - i0);
+  for (int e = threadIdx.x; e < FUSED_BMH * ncg; e += blockDim.x) {  // active column groups
+    const int ii = e % FUSED_BMH, c0 = 4 * (e / FUSED_BMH);
     if (ii >= rows) continue;
     T v[4] = {T(0), T(0), T(0), T(0)};
-    if (c0 < ka) {
-      const T* zm = zs + ii * ld;
-      const T* z0 = zm + ld;
-      const T* zp = z0 + ld;
-      for (int a = 0; a < ka; ++a) {
-        const T d2 = T(ih2) * ((zm[a] + zp[a]) - T(2) * z0[a]);
+    const T* zm = zs + ii * ld;
+    const T* z0 = zm + ld;
+    const T* zp = z0 + ld;
+    for (int a = 0; a < ka; ++a) {
+      const T d2 = T(ih2) * ((zm[a] + zp[a]) - T(2) * z0[a]);
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (c0 + q < ka) v[q] = fma(d2, ns[a + (c0 + q) * ka], v[q]);
-      }
-      if (alpha != 0.0) {
-        T k1[4] = {T(0), T(0), T(0), T(0)};
-        kr_row4<T, false>(ka, np, d1 + ii * ld, z0, tpt, c0, k1);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = fma(T(alpha), k1[q], v[q]);
-      }
-      if (beta != 0.0)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = fma(T(beta * ihx), ks[(ii + 2) * ldk + c0 + q] - ks[ii * ldk + c0 + q], v[q]);
+      for (int q = 0; q < 4; ++q)
+        if (c0 + q < ka) v[q] = fma(d2, ns[a + (c0 + q) * ka], v[q]);
     }
+    if (alpha != 0.0) {
+      T k1[4] = {T(0), T(0), T(0), T(0)};
+      kr_row4<T, false>(ka, tensor_kpp(kap), d1 + ii * ld, z0, tpt, c0, k1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = fma(T(alpha), k1[q], v[q]);
+    }
+    if (beta != 0.0)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = fma(T(beta * ihx), ks[(ii + 2) * ldk + c0 + q] - ks[ii * ldk + c0 + q], v[q]);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int c = c0 + q;
       if (c < R) rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, (c < ka) ? v[q] : T(0));
     }
+  }
+  for (int e = threadIdx.x; e < FUSED_BMH * (R - kap); e += blockDim.x) {  // inactive columns: zero rate
+    const int ii = e % FUSED_BMH, c = kap + e / FUSED_BMH;
+    if (ii < rows) rk_apply(rk, (int64_t)(i0 + ii) + (int64_t)c * N, T(0));
   }
 }
 
@@ -1627,44 +1638,46 @@ __global__ void __launch_bounds__(256) burgers_l_stage(int M, int R, const int32
   }
   const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3;
   T* tpt = reinterpret_cast<T*>(smraw);
-  T* zs = tpt + (nonlin ? np * kap : 0);   // BM x ld
-  T* as = zs + FUSED_BM * ld;              // ka x ka: A_xx
-  const int j0 = blockIdx.x * FUSED_BM;
-  const int rows = min(FUSED_BM, M - j0);
+  T* zs = tpt + (nonlin ? np * tensor_kpp(kap) : 0);  // BM x ld
+  T* as = zs + FUSED_BML * ld;              // ka x ka: A_xx
+  const int j0 = blockIdx.x * FUSED_BML;
+  const int rows = min(FUSED_BML, M - j0);
   if (nonlin) load_tensor(ka, kap, Tp, PP, tpt);
-  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int jj = e % FUSED_BM, a = e / FUSED_BM;
+  for (int e = threadIdx.x; e < FUSED_BML * ka; e += blockDim.x) {
+    const int jj = e % FUSED_BML, a = e / FUSED_BML;
     zs[jj * ld + a] = (jj < rows) ? Z[(j0 + jj) + (int64_t)a * M] : T(0);
   }
   for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) as[e] = T(Axx[(e % ka) + (int64_t)(e / ka) * R]);
   __syncthreads();
-  const int ncg_all = (R + 3) / 4;
-  for (int e = threadIdx.x; e < FUSED_BM * ncg_all; e += blockDim.x) {
-    const int jj = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
+  const int ncg = kap / 4;
+  for (int e = threadIdx.x; e < FUSED_BML * ncg; e += blockDim.x) {  // active column groups
+    const int jj = e % FUSED_BML, c0 = 4 * (e / FUSED_BML);
     if (jj >= rows) continue;
     T v[4] = {T(0), T(0), T(0), T(0)};
-    if (c0 < ka) {
-      const T* z = zs + jj * ld;
-      T lin[4] = {T(0), T(0), T(0), T(0)};
-      for (int a = 0; a < ka; ++a)
+    const T* z = zs + jj * ld;
+    T lin[4] = {T(0), T(0), T(0), T(0)};
+    for (int a = 0; a < ka; ++a)
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (c0 + q < ka) lin[q] = fma(z[a], as[a + (c0 + q) * ka], lin[q]);
-      const T nj = nu[j0 + jj];
+      for (int q = 0; q < 4; ++q)
+        if (c0 + q < ka) lin[q] = fma(z[a], as[a + (c0 + q) * ka], lin[q]);
+    const T nj = nu[j0 + jj];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = nj * lin[q];
-      if (nonlin) {
-        T k[4] = {T(0), T(0), T(0), T(0)};
-        kr_row4<T, true>(ka, np, z, z, tpt, c0, k);
+    for (int q = 0; q < 4; ++q) v[q] = nj * lin[q];
+    if (nonlin) {
+      T k[4] = {T(0), T(0), T(0), T(0)};
+      kr_row4<T, true>(ka, tensor_kpp(kap), z, z, tpt, c0, k);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] += k[q];
-      }
+      for (int q = 0; q < 4; ++q) v[q] += k[q];
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int c = c0 + q;
       if (c < R) rk_apply(rk, (int64_t)(j0 + jj) + (int64_t)c * M, (c < ka) ? v[q] : T(0));
     }
+  }
+  for (int e = threadIdx.x; e < FUSED_BML * (R - kap); e += blockDim.x) {  // inactive columns: zero rate
+    const int jj = e % FUSED_BML, c = kap + e / FUSED_BML;
+    if (jj < rows) rk_apply(rk, (int64_t)(j0 + jj) + (int64_t)c * M, T(0));
   }
 }
 
@@ -1684,18 +1697,18 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
     return;
   }
   const int np = ka * (ka + 1) / 2, ld = ka | 1, kap = (ka + 3) & ~3, ncg = kap / 4, ldk = kap | 1;
-  T* tpt = reinterpret_cast<T*>(smraw);        // kap x np
-  T* us = tpt + np * kap;                      // (BM + 2) x ld: Uhat rows i0 - 1 .. i0 + BM
-  T* zm = us + (FUSED_BM + 2) * ld;            // ka x ka: Z, row-major (zm[k ka + c] = Z[k, c])
+  T* tpt = reinterpret_cast<T*>(smraw);        // np x kpp
+  T* us = tpt + np * tensor_kpp(kap);          // (BM + 2) x ld: Uhat rows i0 - 1 .. i0 + BM
+  T* zm = us + (FUSED_BMH + 2) * ld;            // ka x ka: Z, row-major (zm[k ka + c] = Z[k, c])
   T* as = zm + ka * ka;                        // (BM + 2) x ld: A rows
-  T* ks = as + (FUSED_BM + 2) * ld;            // (BM + 2) x ldk: KR(A, A) T'
-  T* d1 = ks + (FUSED_BM + 2) * ldk;           // BM x ld: Dx A
-  T* p2 = d1 + FUSED_BM * ld;                  // BM x ldk: P2
-  const int i0 = blockIdx.x * FUSED_BM;
-  const int rows = min(FUSED_BM, N - i0);
+  T* ks = as + (FUSED_BMH + 2) * ld;            // (BM + 2) x ldk: KR(A, A) T'
+  T* d1 = ks + (FUSED_BMH + 2) * ldk;           // BM x ld: Dx A
+  T* p2 = d1 + FUSED_BMH * ld;                  // BM x ldk: P2
+  const int i0 = blockIdx.x * FUSED_BMH;
+  const int rows = min(FUSED_BMH, N - i0);
   load_tensor(ka, kap, Tp, PP, tpt);
-  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {
-    const int ii = e % (FUSED_BM + 2), a = e / (FUSED_BM + 2);
+  for (int e = threadIdx.x; e < (FUSED_BMH + 2) * ka; e += blockDim.x) {
+    const int ii = e % (FUSED_BMH + 2), a = e / (FUSED_BMH + 2);
     int g = i0 - 1 + ii;
     g = (g < 0) ? g + N : ((g >= N) ? g - N : g);
     us[ii * ld + a] = Uh[g + (int64_t)act_col(a, r, R) * N];
@@ -1705,33 +1718,33 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
     zm[k * ka + c] = T(Zs[act_col(k, r, R) + (int64_t)act_col(c, r, R) * w]);
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < (FUSED_BM + 2) * ka; e += blockDim.x) {  // A = Uhat Z
-    const int ii = e % (FUSED_BM + 2), c = e / (FUSED_BM + 2);
+  for (int e = threadIdx.x; e < (FUSED_BMH + 2) * ka; e += blockDim.x) {  // A = Uhat Z
+    const int ii = e % (FUSED_BMH + 2), c = e / (FUSED_BMH + 2);
     T acc = T(0);
     for (int k = 0; k < ka; ++k) acc = fma(us[ii * ld + k], zm[k * ka + c], acc);
     as[ii * ld + c] = acc;
   }
   __syncthreads();
   if (beta != 0.0)
-    for (int e = threadIdx.x; e < (FUSED_BM + 2) * ncg; e += blockDim.x) {
-      const int ii = e % (FUSED_BM + 2), c0 = 4 * (e / (FUSED_BM + 2));
+    for (int e = threadIdx.x; e < (FUSED_BMH + 2) * ncg; e += blockDim.x) {
+      const int ii = e % (FUSED_BMH + 2), c0 = 4 * (e / (FUSED_BMH + 2));
       T acc[4] = {T(0), T(0), T(0), T(0)};
-      kr_row4<T, true>(ka, np, as + ii * ld, as + ii * ld, tpt, c0, acc);
+      kr_row4<T, true>(ka, tensor_kpp(kap), as + ii * ld, as + ii * ld, tpt, c0, acc);
 #pragma unroll
       for (int v = 0; v < 4; ++v) ks[ii * ldk + c0 + v] = acc[v];
     }
-  for (int e = threadIdx.x; e < FUSED_BM * ka; e += blockDim.x) {
-    const int ii = e % FUSED_BM, c = e / FUSED_BM;
+  for (int e = threadIdx.x; e < FUSED_BMH * ka; e += blockDim.x) {
+    const int ii = e % FUSED_BMH, c = e / FUSED_BMH;
     d1[ii * ld + c] = T(ihx) * (as[(ii + 2) * ld + c] - as[ii * ld + c]);
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < FUSED_BM * ncg; e += blockDim.x) {
-    const int ii = e % FUSED_BM, c0 = 4 * (e / FUSED_BM);
+  for (int e = threadIdx.x; e < FUSED_BMH * ncg; e += blockDim.x) {
+    const int ii = e % FUSED_BMH, c0 = 4 * (e / FUSED_BMH);
     T v[4] = {T(0), T(0), T(0), T(0)};
     if (ii < rows) {
       if (alpha != 0.0) {
         T k1[4] = {T(0), T(0), T(0), T(0)};
-        kr_row4<T, false>(ka, np, d1 + ii * ld, as + (ii + 1) * ld, tpt, c0, k1);
+        kr_row4<T, false>(ka, tensor_kpp(kap), d1 + ii * ld, as + (ii + 1) * ld, tpt, c0, k1);
 #pragma unroll
         for (int q = 0; q < 4; ++q) v[q] = fma(T(alpha), k1[q], v[q]);
       }
@@ -1775,11 +1788,11 @@ __global__ void __launch_bounds__(256) s_stage_finish_warp(int R, const int32_t*
 // dynamic shared memory of the fused stages at the largest width (FUSED_KMAX)
 template <typename T>
 size_t fused_smem(int which) {
-  const size_t K = FUSED_KMAX, np = K * (K + 1) / 2, B = FUSED_BM;
+  const size_t K = FUSED_KMAX, np = K * (K + 1) / 2, KP = tensor_kpp(FUSED_KMAX);
   const size_t L = K | 1;  // padded row stride
-  if (which == 0) return sizeof(T) * (np * K + 2 * (B + 2) * L + K * K + B * L);
-  if (which == 1) return sizeof(T) * (np * K + B * L + K * K);
-  return sizeof(T) * (np * K + 3 * (B + 2) * L + K * K + 2 * B * L);
+  if (which == 0) return sizeof(T) * (np * KP + 2 * (FUSED_BMH + 2) * L + K * K + FUSED_BMH * L);
+  if (which == 1) return sizeof(T) * (np * KP + FUSED_BML * L + K * K);
+  return sizeof(T) * (np * KP + 3 * (FUSED_BMH + 2) * L + K * K + 2 * FUSED_BMH * L);
 }
 
 // small FP64 helpers of the S step: X (R x R, T, ld R) -> Y (FP64, ld R), optionally transposed
@@ -1926,7 +1939,7 @@ struct lri_stream {
   // fused RK-stage kernels for the current rank: 0 none (rank > 32), 1 the K
   // and L stages (rank <= 32), 2 also the S stage (rank <= 16)
   int fused = 0;
-  double* fgp = nullptr;  // the fused S stage's per-tile partials: ceil(n / 32) x (2R)^2 FP64
+  double* fgp = nullptr;  // the fused S stage's per-tile partials: ceil(n / FUSED_BMH) x (2R)^2 FP64
 };
 
 
@@ -2181,7 +2194,7 @@ struct StreamOps {
     const int zk = kz(n, 0);
     e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, const RkStage<T>& rk) {
       if (s->fused >= 1) {
-        burgers_k_stage<T><<<(n + FUSED_BM - 1) / FUSED_BM, 256, fused_smem<T>(0), st>>>(
+        burgers_k_stage<T><<<(n + FUSED_BMH - 1) / FUSED_BMH, 256, fused_smem<T>(0), st>>>(
             n, R, s->d_rank, Z, Nnu, tp(s->tv), (int)pairs_max(), ih2, ihx, ba, bb, s->d_status, rk);
         return cudaGetLastError();
       }
@@ -2203,7 +2216,7 @@ struct StreamOps {
     const int zl = kz(m, 0);
     e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
       if (s->fused >= 1) {
-        burgers_l_stage<T><<<(m + FUSED_BM - 1) / FUSED_BM, 256, fused_smem<T>(1), st>>>(
+        burgers_l_stage<T><<<(m + FUSED_BML - 1) / FUSED_BML, 256, fused_smem<T>(1), st>>>(
             m, R, s->d_rank, Z, nu, Axx, tp(s->tl), (int)pairs_max(), nonlin ? 1 : 0, s->d_status, rk);
         return cudaGetLastError();
       }
@@ -2257,7 +2270,7 @@ struct StreamOps {
           small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
           small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
           if (nonlin && s->fused >= 2) {
-            const int nzf = (n + FUSED_BM - 1) / FUSED_BM;
+            const int nzf = (n + FUSED_BMH - 1) / FUSED_BMH;
             burgers_s_rows<T><<<nzf, 256, fused_smem<T>(2), st>>>(n, R, s->d_rank, Uh, Z, tp(s->th),
                                                                    (int)pairs_max(), ihx, ba, bb, s->d_status, s->fgp);
             s_stage_finish_warp<<<128, 256, 0, st>>>(R, s->d_rank, nzf, s->fgp, Sk, rk);
@@ -2551,7 +2564,7 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
                                    (int64_t)sizeof(double) * ((n + GA_ROWS - 1) / GA_ROWS) * 4 * R * R));
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
-  alloc((void**)&s->fgp, sizeof(double) * ((n + FUSED_BM - 1) / FUSED_BM) * 4 * R * R);
+  alloc((void**)&s->fgp, sizeof(double) * ((n + lri::FUSED_BMH - 1) / lri::FUSED_BMH) * 4 * R * R);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
