@@ -1534,10 +1534,21 @@ __host__ __device__ constexpr int tensor_kpp(int kap) { return kap + 4; }
 // reads run along the pairs (coalesced)
 template <typename T>
 __device__ __forceinline__ void load_tensor(int ka, int kap, const T* __restrict__ Tp, int PP, T* tpt) {
-  const int np = ka * (ka + 1) / 2, kpp = tensor_kpp(kap);
-  for (int e = threadIdx.x; e < np * kpp; e += blockDim.x) {
-    const int pp = e % np, c = e / np;
-    tpt[pp * kpp + c] = (c < ka) ? Tp[pp + (int64_t)c * PP] : T(0);
+  const int np = ka * (ka + 1) / 2, kpp = tensor_kpp(kap), total = np * kpp;
+  constexpr int U = 8;  // loads in flight per thread
+  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int pp = e % np, c = e / np;
+      v[u] = (e < total && c < ka) ? Tp[pp + (int64_t)c * PP] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e < total) tpt[(e % np) * kpp + e / np] = v[u];
+    }
   }
 }
 
@@ -1689,7 +1700,9 @@ template <typename T>
 __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_t* __restrict__ rank,
                                                       const T* __restrict__ Uh, const double* __restrict__ Zs,
                                                       const T* __restrict__ Tp, int PP, double ihx, double alpha,
-                                                      double beta, uint32_t* status, double* __restrict__ part) {
+                                                      double beta, uint32_t* status, double* __restrict__ part,
+                                                      const double* __restrict__ Nnu, const double* __restrict__ Axx,
+                                                      double* __restrict__ C) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int r = min(R, (int)*rank), ka = 2 * r, w = 2 * R;
   if (ka > FUSED_KMAX) {
@@ -1762,6 +1775,34 @@ __global__ void __launch_bounds__(256) burgers_s_rows(int N, int R, const int32_
     T acc = T(0);
     for (int ii = 0; ii < rows; ++ii) acc = fma(us[(ii + 1) * ld + a], p2[ii * ldk + c], acc);
     dst[act_col(a, r, R) + (int64_t)act_col(c, r, R) * w] = (double)acc;
+  }
+  if (blockIdx.x == 0) {
+    // the linear part of the stage, C = A_xx Z N_nu on the active block
+    // (T1 = Z N_nu first), in the tensor's area once every thread is past it
+    __syncthreads();
+    T* nn = tpt;           // N_nu, row-major
+    T* ax = nn + ka * ka;  // A_xx, row-major
+    T* t1 = ax + ka * ka;  // Z N_nu, row-major
+    for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {
+      const int k = e / ka, c = e % ka;
+      const int64_t g = act_col(k, r, R) + (int64_t)act_col(c, r, R) * w;
+      nn[e] = T(Nnu[g]);
+      ax[e] = T(Axx[g]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {
+      const int i = e / ka, c = e % ka;
+      T acc = T(0);
+      for (int k = 0; k < ka; ++k) acc = fma(zm[i * ka + k], nn[k * ka + c], acc);
+      t1[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ka * ka; e += blockDim.x) {
+      const int i = e % ka, c = e / ka;
+      T acc = T(0);
+      for (int k = 0; k < ka; ++k) acc = fma(ax[i * ka + k], t1[k * ka + c], acc);
+      C[act_col(i, r, R) + (int64_t)act_col(c, r, R) * w] = (double)acc;
+    }
   }
 }
 
@@ -2267,16 +2308,18 @@ struct StreamOps {
           const double* Z = (st_ == 0) ? Sy : Sz;
           const bool last = (st_ + 1 == sc.nstages);
           const RkStage<double> rk{sc.b[st_], last ? 0.0 : h * sc.a[st_ + 1], h, st_ == 0, last, Sy, Sz, Sa};
-          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
-          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
           if (nonlin && s->fused >= 2) {
+            // burgers_s_rows also forms C = A_xx Z N_nu (its first CTA)
             const int nzf = (n + FUSED_BMH - 1) / FUSED_BMH;
             burgers_s_rows<T><<<nzf, 256, fused_smem<T>(2), st>>>(n, R, s->d_rank, Uh, Z, tp(s->th),
-                                                                   (int)pairs_max(), ihx, ba, bb, s->d_status, s->fgp);
+                                                                   (int)pairs_max(), ihx, ba, bb, s->d_status, s->fgp,
+                                                                   Nnuh, Axxh, Sk);
             s_stage_finish_warp<<<128, 256, 0, st>>>(R, s->d_rank, nzf, s->fgp, Sk, rk);
             e = cudaGetLastError();
             continue;
           }
+          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Z, Nnuh, Stmp);
+          small_gemm_act<T><<<gsm, 256, 0, st>>>(R, s->d_rank, Axxh, Stmp, Sk);
           if (nonlin) {
             panel_mul_act<T><<<dim3((n + 31) / 32, (w + 63) / 64), 256, 0, st>>>(n, R, 1, s->d_rank, Uh, Z, w, P0);
             if (ba != 0.0) {
