@@ -1889,7 +1889,6 @@ __global__ void ns_refresh(int R, const int32_t* __restrict__ rank, const double
   const int r = min(R, (int)*rank);
   float* E = reinterpret_cast<float*>(smraw);  // r x r: Eu / 2, then Ev / 2
   float* Sf = E + r * r;                        // r x r: S, then tmp
-  float* Cf = Sf + r * r;                       // r x r: correction
   for (int o = threadIdx.x; o < R * R; o += blockDim.x) {
     const int i = o % R, j = o / R;
     const bool act = i < r && j < r;
@@ -1974,6 +1973,10 @@ struct lri_stream {
   // one captured Burgers step (launch shapes depend on r_max only; the rank
   // is read on the device), replayed while dt and the bound factors stay
   cudaStream_t cap = nullptr;
+  // the L substep flow runs beside the K flow (fused stages: no shared
+  // scratch), forked from and joined to the step's stream by these events
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t step_exec[3] = {nullptr, nullptr, nullptr};  // one per fused class
   double graph_dt[3] = {0.0, 0.0, 0.0};
   bool class_seen[3] = {false, false, false};
@@ -2176,15 +2179,29 @@ struct StreamOps {
     if (e == cudaSuccess) e = gram(m, R, R, V, m, V, m, 1.0, 0.0, Gv, R);
     if (e != cudaSuccess) return e;
     static std::atomic<uint64_t> attr_done{0};
-    e = set_smem_limit(ns_refresh, (int)(3 * SMAX * SMAX * sizeof(float)), attr_done);
+    e = set_smem_limit(ns_refresh, (int)(2 * SMAX * SMAX * sizeof(float)), attr_done);
     if (e != cudaSuccess) return e;
-    ns_refresh<<<1, 1024, 3 * (size_t)R * R * sizeof(float), st>>>(R, s->d_rank, Gu, Gv, Xu, Xv,
+    ns_refresh<<<1, 1024, 2 * (size_t)R * R * sizeof(float), st>>>(R, s->d_rank, Gu, Gv, Xu, Xv,
                                                                   reinterpret_cast<float*>(s->S), blk(23));
     if ((e = mul(n, R, R, U, n, Xu, R, T(0), tp(s->Zp), n)) != cudaSuccess) return e;
     copy_cols<T><<<304, 256, 0, st>>>(n, R, tp(s->Zp), n, U, n);
     if ((e = mul(m, R, R, V, m, Xv, R, T(0), tp(s->Zp), m)) != cudaSuccess) return e;
     copy_cols<T><<<304, 256, 0, st>>>(m, R, tp(s->Zp), m, V, m);
     return cudaGetLastError();
+  }
+
+  // one fused L-flow stage on this object's stream
+  cudaError_t l_stage_fused(const T* Z, const double* Axx, bool nonlin, const RkStage<T>& rk) const {
+    const int m = (int)s->m, R = (int)s->R;
+    burgers_l_stage<T><<<(m + FUSED_BML - 1) / FUSED_BML, 256, fused_smem<T>(1), st>>>(
+        m, R, s->d_rank, Z, static_cast<const T*>(s->nu), Axx, tp(s->tl), (int)pairs_max(), nonlin ? 1 : 0,
+        s->d_status, rk);
+    return cudaGetLastError();
+  }
+  // the whole L substep flow with the fused stages (Lp holds L0 and its RK panels)
+  cudaError_t l_flow_fused(T* Lp, const double* Axx, bool nonlin) const {
+    return rk_panel((int64_t)s->m * s->R, Lp,
+                    [&](const T* Z, const RkStage<T>& rk) { return l_stage_fused(Z, Axx, nonlin, rk); });
   }
 
   cudaError_t burgers_step() const {
@@ -2229,9 +2246,23 @@ struct StreamOps {
     if ((e = gram(n, R, R, U, n, P0, n, 1.0, 0.0, Axx, R)) != cudaSuccess) return e;
     if (ba != 0.0 && (e = tensor(n, 0, P1, U, U, ba, 0, tp(s->tl))) != cudaSuccess) return e;
     if (bb != 0.0 && (e = tensor(n, 0, U, U, P1, -bb, ba != 0.0, tp(s->tl))) != cudaSuccess) return e;
-    // K step: K0 = U0 S0, K' = (Dxx K) N_nu + alpha KR(Dx K, K) T'_V + beta Dx(KR(K, K) T'_V)
+    // K step: K0 = U0 S0, K' = (Dxx K) N_nu + alpha KR(Dx K, K) T'_V + beta Dx(KR(K, K) T'_V);
+    // L step: L0 = V0 S0^T, L' = diag(nu) L A_xx + KR(L, L) T'_L.  The two
+    // flows are independent (both start from the old factors): with the
+    // fused stages the L flow runs on the side stream beside the K flow.
     T* Kp = tp(s->Kp);
+    T* Lp = tp(s->Lp);
     if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
+    if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
+    const bool fork = s->fused >= 1 && s->side;
+    cudaError_t el = cudaSuccess;
+    if (fork) {
+      if ((e = cudaEventRecord(s->ev_fork, st)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(s->side, s->ev_fork, 0)) != cudaSuccess) return e;
+      el = StreamOps<T>{s, s->side}.l_flow_fused(Lp, Axx, nonlin);
+      const cudaError_t ej = cudaEventRecord(s->ev_join, s->side);
+      if (el == cudaSuccess) el = ej;
+    }
     const int zk = kz(n, 0);
     e = rk_panel((int64_t)n * R, Kp, [&](const T* Z, const RkStage<T>& rk) {
       if (s->fused >= 1) {
@@ -2250,25 +2281,24 @@ struct StreamOps {
                                          bb != 0.0 ? kap2 : nullptr, zk, ba, bb, ihx, nullptr, rk);
       return cudaGetLastError();
     });
+    if (fork) {  // join before anything can return (a capture must end with the side stream joined)
+      const cudaError_t ew = cudaStreamWaitEvent(st, s->ev_join, 0);
+      if (e == cudaSuccess) e = (el != cudaSuccess) ? el : ew;
+    }
     if (e != cudaSuccess) return e;
-    // L step: L0 = V0 S0^T, L' = diag(nu) L A_xx + KR(L, L) T'_L
-    T* Lp = tp(s->Lp);
-    if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
-    const int zl = kz(m, 0);
-    e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
-      if (s->fused >= 1) {
-        burgers_l_stage<T><<<(m + FUSED_BML - 1) / FUSED_BML, 256, fused_smem<T>(1), st>>>(
-            m, R, s->d_rank, Z, nu, Axx, tp(s->tl), (int)pairs_max(), nonlin ? 1 : 0, s->d_status, rk);
+    if (!fork) {
+      const int zl = kz(m, 0);
+      e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
+        if (s->fused >= 1) return l_stage_fused(Z, Axx, nonlin, rk);
+        panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
+        cudaError_t e2 = cudaGetLastError();
+        if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
+        if (e2 != cudaSuccess) return e2;
+        flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, rk);
         return cudaGetLastError();
-      }
-      panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
-      cudaError_t e2 = cudaGetLastError();
-      if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
-      if (e2 != cudaSuccess) return e2;
-      flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, rk);
-      return cudaGetLastError();
-    });
-    if (e != cudaSuccess) return e;
+      });
+      if (e != cudaSuccess) return e;
+    }
     // augmented bases Uhat = [U0 | orth((I - U0 U0^T) K1)], Vhat likewise
     copy_cols<T><<<304, 256, 0, st>>>(n, R, Kp, n, Xk, n);
     copy_cols<T><<<304, 256, 0, st>>>(m, R, Lp, m, Xl, m);
@@ -2608,6 +2638,9 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
   alloc((void**)&s->fgp, sizeof(double) * ((n + lri::FUSED_BMH - 1) / lri::FUSED_BMH) * 4 * R * R);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
@@ -2655,6 +2688,9 @@ lri_status lri_stream_destroy(lri_stream* s) {
   if (!s) return LRI_ERR_ARG;
   drop_graph(s);
   if (s->cap) cudaStreamDestroy(s->cap);
+  if (s->side) cudaStreamDestroy(s->side);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
   cudaFree(s->Kp);
   cudaFree(s->Lp);
   cudaFree(s->tv);
