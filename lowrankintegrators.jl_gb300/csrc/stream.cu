@@ -1497,33 +1497,52 @@ constexpr int FUSED_KMAX = 32;
 
 // Four consecutive columns c0 .. c0 + 3 of one row of
 //   sum_{a <= b} KR(P, Q)_ab T'[p(a,b), c],  KR(P, Q)_ab = (P_a Q_b + P_b Q_a) / 2
-// (SAME: P == Q, KR = P_a P_b); P, Q: the row's ka values; T' pair-major in
-// shared memory, tpt[p kpp + c], zero beyond the active columns.  Each
-// 16-byte tensor load serves 4 (8) multiply-adds; a warp's threads share c0,
-// so the tensor reads are broadcasts.
-template <typename T, bool SAME>
-__device__ __forceinline__ void kr_row4(int ka, int kpp, const T* P, const T* Q, const T* tpt, int c0, T (&acc)[4]) {
+// (SAME: P == Q, KR = P_a P_b); P, Q: the row's ka <= 32 values; T'
+// pair-major in shared memory, tpt[p kpp + c], zero beyond the active
+// columns.  Each 16-byte tensor load serves 4 (8) multiply-adds and is the
+// loop's only shared-memory read; a warp's threads share c0, so the tensor
+// reads are broadcasts.
+template <typename T, int KMAX, bool SAME>
+__device__ __forceinline__ void kr_row4_k(int ka, int kpp, const T* P, const T* Q, const T* tpt, int c0,
+                                          T (&acc)[4]) {
+  // the row's values in registers (zero beyond ka); loops unrolled over the
+  // KMAX x KMAX triangle, pairs beyond ka skipped (ka is uniform)
+  T qv[KMAX], pv[SAME ? 1 : KMAX];
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    qv[k] = (k < ka) ? Q[k] : T(0);
+    if (!SAME) pv[SAME ? 0 : k] = (k < ka) ? P[k] : T(0);
+  }
   const T* tp = tpt + c0;
-  for (int a = 0; a < ka; ++a) {
-    T g1[4] = {T(0), T(0), T(0), T(0)}, g2[4] = {T(0), T(0), T(0), T(0)};
-    for (int b = a; b < ka; ++b, tp += kpp) {
-      const T qb = Q[b];
-      const T pb = SAME ? qb : P[b];
-      T t[4];
-      ld_vec<4>(tp, t);
+#pragma unroll
+  for (int a = 0; a < KMAX; ++a) {
+    if (a < ka) {
+      T g1[4] = {T(0), T(0), T(0), T(0)}, g2[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+      for (int b = a; b < KMAX; ++b) {
+        if (b < ka) {
+          T t[4];
+          ld_vec<4>(tp, t);
+          tp += kpp;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            g1[v] = fma(qv[b], t[v], g1[v]);
+            if (!SAME) g2[v] = fma(pv[SAME ? 0 : b], t[v], g2[v]);
+          }
+        }
+      }
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        g1[v] = fma(qb, t[v], g1[v]);
-        if (!SAME) g2[v] = fma(pb, t[v], g2[v]);
+        if (SAME) acc[v] = fma(qv[a], g1[v], acc[v]);
+        else acc[v] = fma(T(0.5), fma(pv[SAME ? 0 : a], g1[v], qv[a] * g2[v]), acc[v]);
       }
     }
-    const T pa = P[a];
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      if (SAME) acc[v] = fma(pa, g1[v], acc[v]);
-      else acc[v] = fma(T(0.5), fma(pa, g1[v], Q[a] * g2[v]), acc[v]);
-    }
   }
+}
+template <typename T, bool SAME>
+__device__ __forceinline__ void kr_row4(int ka, int kpp, const T* P, const T* Q, const T* tpt, int c0, T (&acc)[4]) {
+  if (ka <= 16) kr_row4_k<T, 16, SAME>(ka, kpp, P, Q, tpt, c0, acc);
+  else kr_row4_k<T, 32, SAME>(ka, kpp, P, Q, tpt, c0, acc);
 }
 
 // row stride of the pair-major tensor in shared memory
