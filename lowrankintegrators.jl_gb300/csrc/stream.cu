@@ -308,12 +308,14 @@ __global__ void __launch_bounds__(256) gram_part(int N, int a, int c, int R, con
 
 // out (a x c, ld ldo) = alpha * sum of the row blocks' partials + beta * out
 // on the active entries, beta * out elsewhere (the Gram of zero columns);
-// `ctas` as in gram_part's launch
-__global__ void gram_reduce(int N, int a, int c, int R, const int32_t* __restrict__ rank, int ctas,
-                            const double* __restrict__ part, double alpha, double beta, double* __restrict__ out,
-                            int ldo) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= a * c) return;
+// `ctas` as in gram_part's launch.  One warp per entry: the lanes stride over
+// the row blocks, a fixed shuffle tree adds them (deterministic).
+__global__ void __launch_bounds__(256) gram_reduce(int N, int a, int c, int R, const int32_t* __restrict__ rank,
+                                                   int ctas, const double* __restrict__ part, double alpha,
+                                                   double beta, double* __restrict__ out, int ldo) {
+  const int lane = threadIdx.x & 31;
+  const int o = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  if (o >= a * c) return;  // warp-uniform
   const int r = min(R, (int)*rank);
   const GramSplit g = gram_split(N, a, c, R, r, ctas);
   const int i = o % a, j = o / a;
@@ -322,10 +324,13 @@ __global__ void gram_reduce(int N, int a, int c, int R, const int32_t* __restric
   if (ia >= 0 && jc >= 0) {
     const int tile = (ia / GRAM_TILE) + (jc / GRAM_TILE) * g.ta;
     const int64_t off = (ia % GRAM_TILE) + (int64_t)(jc % GRAM_TILE) * GRAM_TILE;
-    for (int b = 0; b < g.nrb; ++b) s += part[((int64_t)b * g.ntile + tile) * GRAM_TILE * GRAM_TILE + off];
+    for (int b = lane; b < g.nrb; b += 32) s += part[((int64_t)b * g.ntile + tile) * GRAM_TILE * GRAM_TILE + off];
   }
-  double* d = out + i + (int64_t)j * ldo;
-  *d = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *d);
+  for (int x = 16; x > 0; x >>= 1) s += __shfl_xor_sync(0xffffffffu, s, x);
+  if (lane == 0) {
+    double* d = out + i + (int64_t)j * ldo;
+    *d = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *d);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2025,8 +2030,8 @@ struct StreamOps {
                    double* out, int ldo) const {
     const int ctas = gram_ctas(s);
     gram_part<T><<<ctas, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, s->part);
-    gram_reduce<<<(a * c + 255) / 256, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, ctas, s->part, alpha, beta, out,
-                                                     ldo);
+    gram_reduce<<<(a * c + 7) / 8, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, ctas, s->part, alpha, beta, out,
+                                                 ldo);
     return cudaGetLastError();
   }
   cudaError_t mul(int N, int a, int c, const T* X, int ldx, const double* B, int ldb, T beta, T* out,
