@@ -101,11 +101,17 @@ __device__ __forceinline__ dfloat ld_cg(const dfloat* p) {
 // are orthonormal to the working precision, so the right vectors stay
 // orthogonal.  FP32 approximate intrinsics (MUFU) keep the rotation's
 // dependency chain short.
+// t = sign(d) 2ga / (|d| + sqrt(d^2 + 4ga^2)) (d = be - al; the same as
+// sign(zeta) / (|zeta| + sqrt(1 + zeta^2)) with zeta = d / 2ga), after
+// scaling d and 2ga by the larger of the two (no overflow; the root's
+// argument lies in [1, 2])
 __device__ __forceinline__ float rot_tan(float d, float ga) {
-  const float zeta = __fdividef(d, 2.0f * ga);
-  const float az = fabsf(zeta);
-  return (az > 1.0e15f) ? __fdividef(0.5f, zeta)
-                        : copysignf(__fdividef(1.0f, az + sqrtf(fmaf(zeta, zeta, 1.0f))), zeta);
+  const float g2 = 2.0f * ga;
+  const float sc = __frcp_rn(fmaxf(fabsf(d), fabsf(g2)));
+  const float dn = d * sc, gn = g2 * sc;
+  const float h = fmaf(dn, dn, gn * gn);
+  const float t = __fdividef(gn, fabsf(dn) + h * rsqrtf(h));
+  return (d < 0.0f) ? -t : t;
 }
 
 __device__ __forceinline__ bool rot_params(float al, float be, float ga, float eps, float& cs, float& sn, float& dl) {
@@ -137,8 +143,9 @@ __device__ __forceinline__ bool rot_params(dfloat al, dfloat be, dfloat ga, dflo
 }
 
 // One Jacobi rotation of columns (ap, aq) with right vectors (vp, vq) by a
-// group of G lanes (gl = lane in the group; the group's rows i = gl + k G stay
-// in registers between the dot products and the rotation); every lane of the
+// group of G lanes (gl = lane in the group; the group's rows i = gl + k G of
+// the columns and of the right vectors are loaded at once and stay in
+// registers until the rotation); every lane of the
 // warp takes part in the reductions.  Same test and rotation as the one-CTA
 // sweeps, with the parameters above.  A rotation sets fl and raises dm (the
 // rotation measure) in the lane's registers; the sweep reduces them once at
@@ -147,7 +154,7 @@ template <typename T, int G>
 __device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool valid, int wa, int gl, T eps, T tiny,
                                             T reach, bool skip_noise, unsigned& fl, float& dm) {
   constexpr int KR = (CORE_SVD_MAX_WA + G - 1) / G;
-  T x[KR], y[KR];
+  T x[KR], y[KR], u[KR], w[KR];  // the group's rows of the columns and of the right vectors
   T al = T(0), be = T(0), ga = T(0);
 #pragma unroll
   for (int k = 0; k < KR; ++k) {
@@ -155,9 +162,13 @@ __device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool val
     if (valid && i < wa) {
       x[k] = ap[i];
       y[k] = aq[i];
+      u[k] = vp[i];
+      w[k] = vq[i];
     } else {
       x[k] = T(0);
       y[k] = T(0);
+      u[k] = T(0);
+      w[k] = T(0);
     }
     al = fma_acc(x[k], x[k], al);
     be = fma_acc(y[k], y[k], be);
@@ -189,9 +200,8 @@ __device__ __forceinline__ void rotate_pair(T* ap, T* aq, T* vp, T* vq, bool val
     for (int k = 0; k < KR; ++k) {
       const int i = gl + k * G;
       if (i < wa) {
-        const T u = vp[i], v = vq[i];
-        vp[i] = cs_ * u - sn * v;
-        vq[i] = sn * u + cs_ * v;
+        vp[i] = cs_ * u[k] - sn * w[k];
+        vq[i] = sn * u[k] + cs_ * w[k];
       }
     }
     fl = 1u;
