@@ -67,3 +67,22 @@ def test_stream_engine_wide_core(lri, oracle, precision, tol):
         assert err <= tol, f"snapshot {k}: {err:.3e}"
     Yf = sg.Y[-1]
     assert np.abs(Yf.U.T @ Yf.U - np.eye(90)).max() <= (1e-12 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
+def test_stream_engine_low_rank(lri, oracle, precision, tol):
+    """From rank 1 on a noise-free rank-3 stream (the oracle's ranks: 1, 2,
+    4, 8, 8, 8 with r_max 8): the core has 2 to 16 columns, so most of the
+    core SVD's column blocks (16 over the cluster) are empty or hold one
+    column."""
+    snaps = workloads.data_stream(384, 256, 6, seed=3, K=3, noise=0.0)
+    X0 = oracle.truncated_svd(snaps[0], r=1)
+    so = oracle.solve(oracle.MatrixDataProblem(snaps, X0), oracle.RankAdaptiveUnconventionalAlgorithm(1e-6, rmax=8))
+    prob = lri.MatrixDataProblem(snaps, lri.SVDLikeRepresentation(X0.U, X0.S, X0.V))
+    sg = lri.solve_stream(prob, lri.RankAdaptiveUnconventionalAlgorithm(1e-6, rmax=8), precision=precision)
+    ranks = [y.S.shape[0] for y in sg.Y]
+    assert ranks == [y.S.shape[0] for y in so.Y]
+    assert max(ranks) > 1
+    for k, (yg, yo) in enumerate(zip(sg.Y, so.Y)):
+        err = oracle.rel_fro_err(yg.full(), yo.full())
+        assert err <= tol, f"snapshot {k}: {err:.3e}"
