@@ -629,12 +629,19 @@ class History:
                       "lri_history_create")
         self.pending = []
 
-    def record(self) -> int:
-        """Queues a copy of the batch's current factors; returns its number."""
+    def host_buffers(self):
+        """Page-locked host buffers (U, S, V, ranks) sized for one record."""
         t, b = self.torch, self.b
         pin = lambda k, dt: t.empty(max(int(k), 1), dtype=dt, pin_memory=True)
-        hU, hS, hV = pin(b.U.numel(), b.dtype), pin(b.S.numel(), b.dtype), pin(b.V.numel(), b.dtype)
-        hR = pin(b.count, t.int32)
+        return pin(b.U.numel(), b.dtype), pin(b.S.numel(), b.dtype), pin(b.V.numel(), b.dtype), pin(b.count, t.int32)
+
+    def record(self, host=None) -> int:
+        """Queues a copy of the batch's current factors; returns its number.
+        host: optional buffers from host_buffers() to copy into (the caller
+        reuses them once wait() returned for the record that last used
+        them); by default new ones are allocated."""
+        b = self.b
+        hU, hS, hV, hR = host if host is not None else self.host_buffers()
         seq = C.c_int64(0)
         ptr = lambda x: C.c_void_p(x.data_ptr())
         _native.check(self.lib.lri_history_record(self.handle, ptr(hU), ptr(hS), ptr(hV),
@@ -642,6 +649,10 @@ class History:
                                                   C.byref(seq)), "lri_history_record")
         self.pending.append((seq.value, hU, hS, hV, hR))
         return seq.value
+
+    def wait(self, seq: int):
+        """Blocks until record seq is in its host buffers."""
+        _native.check(self.lib.lri_history_wait(self.handle, int(seq)), "lri_history_wait")
 
     def collect(self) -> List[List[SVDLikeRepresentation]]:
         """Waits for every queued record; their per-instance factors, in order."""
