@@ -477,13 +477,17 @@ def leg_burgers(steps, warmup):
         return np.trace((a.U.T @ b.U) @ b.S @ (b.V.T @ a.V) @ a.S.T)
     d2 = gram_fro(y32, y32) - 2 * gram_fro(y32, y64) + gram_fro(y64, y64)
     err = float(np.sqrt(max(d2, 0.0) / gram_fro(y64, y64)))
-    # e2e through the public solve: factors from host memory, result back to host
-    prob = lri.MatrixDEProblem(op, Y0, (0.0, 3 * dt))
+    # e2e through the public solve: factors from host memory, every step's
+    # factors back to the host (save_everystep), K steps
+    kE = max(1, K)
+    prob = lri.MatrixDEProblem(op, Y0, (0.0, kE * dt))
     alg = lri.RankAdaptiveUnconventionalAlgorithm(tol, rmax=R, K_alg=lri.RK4(nsub), rmin=16)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    lri.solve_burgers_large(prob, alg, dt)
-    e2e_s = (time.perf_counter() - t0) / 3
+    sol_e2e = lri.solve_burgers_large(prob, alg, dt, save_everystep=True)
+    e2e_s = (time.perf_counter() - t0) / kE
+    d2h_e2e = 4 * (R * n + R * R + R * m)  # each step's U, S, V buffers (FP32, r_max wide)
+    del sol_e2e
     # CPU: the oracle's first step on the first m_s = 2048 samples with 1 and
     # 2 RK4 substeps; the step's cost is linear in m and in the substeps, so
     # t(m, 64) = (m / m_s) (t1 + 63 (t2 - t1))
@@ -533,8 +537,8 @@ def leg_burgers(steps, warmup):
                                        f"({tcpu[0]:.1f} s, {tcpu[1]:.1f} s), scaled linearly to {m} samples "
                                        f"and {nsub} substeps"},
             "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s",
-                    "h2d_bytes_per_step": ((n + m) * r0 + r0 * r0 + m) * 4 // 3,
-                    "d2h_bytes_per_step": ((n + m) * R + R * R) * 4 // 3}}
+                    "h2d_bytes_per_step": ((n + m) * r0 + r0 * r0 + m) * 4 / kE,
+                    "d2h_bytes_per_step": d2h_e2e, "steps": kE}}
     return line
 
 

@@ -2004,6 +2004,7 @@ struct lri_stream {
   cudaGraphExec_t step_exec[3] = {nullptr, nullptr, nullptr};  // one per fused class
   double graph_dt[3] = {0.0, 0.0, 0.0};
   bool class_seen[3] = {false, false, false};
+  double last_dt[3] = {0.0, 0.0, 0.0};  // dt of the class's previous step (a repeat of it is captured)
   // fused RK-stage kernels for the current rank: 0 none (rank > 32), 1 the K
   // and L stages (rank <= 32), 2 also the S stage (rank <= 16)
   int fused = 0;
@@ -2688,7 +2689,9 @@ lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stre
   cudaError_t e = cudaSuccess;
   // Each step takes the launch sequence of its rank class (fused RK-stage
   // kernels up to rank 32): one captured graph per class, replayed while dt
-  // and the binding stay; a class's first step runs eagerly.
+  // and the binding stay; a class's first step runs eagerly, and the graph
+  // is captured at its next step with the same dt (also across calls of one
+  // step each, as a solve that reads every step back makes).
   for (int k = 0; k < nsteps && e == cudaSuccess; ++k) {
     int cls = 0;
     if ((e = fused_class(s, st, &cls)) != cudaSuccess) break;
@@ -2697,13 +2700,14 @@ lri_status lri_burgers_step(lri_stream* s, double dt, int32_t nsteps, void* stre
       cudaGraphExecDestroy(s->step_exec[cls]);
       s->step_exec[cls] = nullptr;
     }
-    if (!s->step_exec[cls] && s->class_seen[cls] && nsteps > 1) capture_step(s);
+    if (!s->step_exec[cls] && s->class_seen[cls] && (nsteps > 1 || s->last_dt[cls] == dt)) capture_step(s);
     if (s->step_exec[cls]) {
       e = cudaGraphLaunch(s->step_exec[cls], st);
     } else {
       e = burgers_step_on(s, st);
       s->class_seen[cls] = true;
     }
+    s->last_dt[cls] = dt;
   }
   return e == cudaSuccess ? LRI_OK : LRI_ERR_CUDA;
 }
