@@ -1997,10 +1997,15 @@ struct lri_stream {
   // one captured Burgers step (launch shapes depend on r_max only; the rank
   // is read on the device), replayed while dt and the bound factors stay
   cudaStream_t cap = nullptr;
-  // the L substep flow runs beside the K flow (fused stages: no shared
-  // scratch), forked from and joined to the step's stream by these events
+  // independent halves of a step run on a second stream, forked from and
+  // joined to the step's stream by these events: the V-side
+  // orthonormalisation (with the second scratch set below) and the fused
+  // L substep flow
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  double* part2 = nullptr;   // Gram partials of the side stream
+  double* small2 = nullptr;  // three (2R)^2 FP64 scratch blocks of the side stream
+  void* zp2 = nullptr;       // max(n, m) x R panel product of the side stream
   cudaGraphExec_t step_exec[3] = {nullptr, nullptr, nullptr};  // one per fused class
   double graph_dt[3] = {0.0, 0.0, 0.0};
   bool class_seen[3] = {false, false, false};
@@ -2024,14 +2029,19 @@ template <typename T>
 struct StreamOps {
   lri_stream* s;
   cudaStream_t st;
+  int sid = 0;  // scratch set: 0 the step's stream, 1 the side stream
   double* blk(int i) const { return s->small + (int64_t)i * 4 * s->R * s->R; }
   T* tp(void* p) const { return static_cast<T*>(p); }
+  // the scratch of the Grams and of the orthonormalisation (per scratch set)
+  double* gpart() const { return sid ? s->part2 : s->part; }
+  double* sblk(int i) const { return sid ? s->small2 + (int64_t)i * 4 * s->R * s->R : blk(i); }
+  T* zpan() const { return tp(sid ? s->zp2 : s->Zp); }
 
   cudaError_t gram(int N, int a, int c, const T* X, int ldx, const T* Y, int ldy, double alpha, double beta,
                    double* out, int ldo) const {
     const int ctas = gram_ctas(s);
-    gram_part<T><<<ctas, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, s->part);
-    gram_reduce<<<(a * c + 7) / 8, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, ctas, s->part, alpha, beta, out,
+    gram_part<T><<<ctas, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, X, ldx, Y, ldy, gpart());
+    gram_reduce<<<(a * c + 7) / 8, 256, 0, st>>>(N, a, c, (int)s->R, s->d_rank, ctas, gpart(), alpha, beta, out,
                                                  ldo);
     return cudaGetLastError();
   }
@@ -2086,11 +2096,11 @@ struct StreamOps {
   // X <- X - Y0 (Y0^T X) for the orthonormal columns of Y0 (N x R)
   cudaError_t project_out(int N, T* X, const T* Y0) const {
     const int R = (int)s->R;
-    cudaError_t e = gram(N, R, R, Y0, N, X, N, 1.0, 0.0, blk(0), R);  // C = Y0^T X
+    cudaError_t e = gram(N, R, R, Y0, N, X, N, 1.0, 0.0, sblk(0), R);  // C = Y0^T X
     if (e != cudaSuccess) return e;
     // panel_mul computes Y0 (-C) + X
-    negate<<<(R * R + 255) / 256, 256, 0, st>>>(R * R, blk(0));
-    return mul(N, R, R, Y0, N, blk(0), R, T(1), X, N);
+    negate<<<(R * R + 255) / 256, 256, 0, st>>>(R * R, sblk(0));
+    return mul(N, R, R, Y0, N, sblk(0), R, T(1), X, N);
   }
   // X (N x R) <- orthonormal basis of the part of X orthogonal to the
   // orthonormal columns of Y0 (N x R); blocks 0..2 are scratch.  Block
@@ -2110,19 +2120,19 @@ struct StreamOps {
     const int npass = std::is_same<T, float>::value ? 3 : 2;
     for (int pass = 0; pass < npass && e == cudaSuccess; ++pass) {
       if (pass == 1 && Y0) e = project_out(N, X, Y0);
-      if (e == cudaSuccess) e = gram(N, R, R, X, N, X, N, 1.0, 0.0, blk(1), R);         // G = X^T X
+      if (e == cudaSuccess) e = gram(N, R, R, X, N, X, N, 1.0, 0.0, sblk(1), R);        // G = X^T X
       if (e == cudaSuccess) {
-        if (pass == 0) e = pchol(R, blk(1), blk(2));
+        if (pass == 0) e = pchol(R, sblk(1), sblk(2));
         else if (std::is_same<T, float>::value) {
-          ns_factor<<<(R * R + 255) / 256, 256, 0, st>>>(R, blk(1), blk(2));
+          ns_factor<<<(R * R + 255) / 256, 256, 0, st>>>(R, sblk(1), sblk(2));
           e = cudaGetLastError();
-        } else e = cholinv(R, blk(1), blk(2), 0.0);
+        } else e = cholinv(R, sblk(1), sblk(2), 0.0);
       }
       if (e == cudaSuccess)
-        e = (pass == 0) ? mul_precise(N, R, R, X, N, blk(2), R, tp(s->Zp), N)            // Z = X B
-                        : mul(N, R, R, X, N, blk(2), R, T(0), tp(s->Zp), N);
+        e = (pass == 0) ? mul_precise(N, R, R, X, N, sblk(2), R, zpan(), N)              // Z = X B
+                        : mul(N, R, R, X, N, sblk(2), R, T(0), zpan(), N);
       if (e == cudaSuccess) {
-        copy_cols<T><<<304, 256, 0, st>>>(N, R, tp(s->Zp), N, X, N);
+        copy_cols<T><<<304, 256, 0, st>>>(N, R, zpan(), N, X, N);
         e = cudaGetLastError();
       }
     }
@@ -2213,6 +2223,42 @@ struct StreamOps {
     if ((e = mul(m, R, R, V, m, Xv, R, T(0), tp(s->Zp), m)) != cudaSuccess) return e;
     copy_cols<T><<<304, 256, 0, st>>>(m, R, tp(s->Zp), m, V, m);
     return cudaGetLastError();
+  }
+
+  // Uhat = [U0 | orth((I - U0 U0^T) Xk)] (K side: n rows), Vhat likewise
+  // from Xl (V side: m rows), Mh = Uhat^T U0 into block 3, Nh = Vhat^T V0
+  // into block 4.  The two sides are independent: the V side runs on the
+  // side stream with the second scratch set, forked and joined by events.
+  cudaError_t bases() const {
+    const int n = (int)s->n, m = (int)s->m, R = (int)s->R, w = 2 * R;
+    auto side = [&](const StreamOps<T>& o, int N, T* X, const T* Y0, T* H, double* Mout) -> cudaError_t {
+      cudaError_t e = o.orth_against(N, X, Y0);
+      if (e != cudaSuccess) return e;
+      copy_cols<T><<<304, 256, 0, o.st>>>(N, R, Y0, N, H, N);
+      copy_cols<T><<<304, 256, 0, o.st>>>(N, R, X, N, H + (int64_t)R * N, N);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      return o.gram(N, w, R, H, N, Y0, N, 1.0, 0.0, Mout, w);
+    };
+    T* U = tp(s->U);
+    T* V = tp(s->V);
+    const bool fork = s->side != nullptr;
+    cudaError_t ev = cudaSuccess;
+    if (fork) {
+      cudaError_t e = cudaEventRecord(s->ev_fork, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+      if (e != cudaSuccess) return e;
+      ev = side(StreamOps<T>{s, s->side, 1}, m, tp(s->Xl), V, tp(s->Vh), blk(4));
+      const cudaError_t ej = cudaEventRecord(s->ev_join, s->side);
+      if (ev == cudaSuccess) ev = ej;
+    }
+    cudaError_t e = side(*this, n, tp(s->Xk), U, tp(s->Uh), blk(3));
+    if (fork) {  // join before anything can return (a capture must end with the side stream joined)
+      const cudaError_t ew = cudaStreamWaitEvent(st, s->ev_join, 0);
+      if (e == cudaSuccess) e = (ev != cudaSuccess) ? ev : ew;
+      return e;
+    }
+    if (e != cudaSuccess) return e;
+    return side(*this, m, tp(s->Xl), V, tp(s->Vh), blk(4));
   }
 
   // one fused L-flow stage on this object's stream
@@ -2324,17 +2370,10 @@ struct StreamOps {
       });
       if (e != cudaSuccess) return e;
     }
-    // augmented bases Uhat = [U0 | orth((I - U0 U0^T) K1)], Vhat likewise
+    // augmented bases Uhat = [U0 | orth((I - U0 U0^T) K1)], Vhat likewise; Mh, Nh
     copy_cols<T><<<304, 256, 0, st>>>(n, R, Kp, n, Xk, n);
     copy_cols<T><<<304, 256, 0, st>>>(m, R, Lp, m, Xl, m);
-    if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
-    if ((e = orth_against(m, Xl, V)) != cudaSuccess) return e;
-    copy_cols<T><<<304, 256, 0, st>>>(n, R, U, n, Uh, n);
-    copy_cols<T><<<304, 256, 0, st>>>(n, R, Xk, n, Uh + (int64_t)R * n, n);
-    copy_cols<T><<<304, 256, 0, st>>>(m, R, V, m, Vh, m);
-    copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, Vh + (int64_t)R * m, m);
-    if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
-    if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
+    if ((e = bases()) != cudaSuccess) return e;
     // operators of the S substep: A_xx = Uhat^T Dxx Uhat, N_nu = Vhat^T diag(nu) Vhat, T'_Vhat
     double* Axxh = blk(15);
     double* Nnuh = blk(23);
@@ -2494,16 +2533,9 @@ struct StreamOps {
       e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
-    // Uhat = [U0 | orth((I - U0 U0^T) dY V0)], Vhat likewise
-    if ((e = orth_against(n, Xk, U)) != cudaSuccess) return e;
-    if ((e = orth_against(m, Xl, V)) != cudaSuccess) return e;
-    copy_cols<T><<<304, 256, 0, st>>>(n, R, U, n, Uh, n);
-    copy_cols<T><<<304, 256, 0, st>>>(n, R, Xk, n, Uh + (int64_t)R * n, n);
-    copy_cols<T><<<304, 256, 0, st>>>(m, R, V, m, Vh, m);
-    copy_cols<T><<<304, 256, 0, st>>>(m, R, Xl, m, Vh + (int64_t)R * m, m);
-    // Mh = Uhat^T U0, Nh = Vhat^T V0 (w x R)
-    if ((e = gram(n, w, R, Uh, n, U, n, 1.0, 0.0, blk(3), w)) != cudaSuccess) return e;
-    if ((e = gram(m, w, R, Vh, m, V, m, 1.0, 0.0, blk(4), w)) != cudaSuccess) return e;
+    // Uhat = [U0 | orth((I - U0 U0^T) dY V0)], Vhat likewise; Mh = Uhat^T U0,
+    // Nh = Vhat^T V0 (w x R)
+    if ((e = bases()) != cudaSuccess) return e;
     // data pass 3: Z = dY Vhat; D = Uhat^T Z.  On the tensor cores only
     // dY Q_V is new (Vhat = [V0 | Q_V]): dY V0 is the copy kept by pass 1.
     if (tc) {
@@ -2607,7 +2639,14 @@ lri_status lri_stream_create(lri_stream** out, int32_t dtype, int64_t n, int64_t
   alloc((void**)&s->part, sizeof(double) * (size_t)(lri::gram_ctas(s) + lri::GRAM_TILE_MAX) * lri::GRAM_TILE *
                               lri::GRAM_TILE);
   alloc((void**)&s->small, sizeof(double) * kBlocksSmall * 4 * R * R);
+  alloc((void**)&s->part2, sizeof(double) * (size_t)(lri::gram_ctas(s) + lri::GRAM_TILE_MAX) * lri::GRAM_TILE *
+                               lri::GRAM_TILE);
+  alloc((void**)&s->small2, sizeof(double) * 3 * 4 * R * R);
+  alloc(&s->zp2, s->es * std::max(n, m) * R);
   alloc((void**)&s->d_ncols, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess && dtype == LRI_F32 && lri::tc_pass_supported(n, m, (int)R)) {
     alloc(&s->Kd, s->es * n * R);
     if (e == cudaSuccess) e = lri::tc_pass_init(&s->tc, n, m, (int)R);
@@ -2663,9 +2702,6 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
   alloc((void**)&s->fgp, sizeof(double) * ((n + lri::FUSED_BMH - 1) / lri::FUSED_BMH) * 4 * R * R);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
@@ -2736,6 +2772,9 @@ lri_status lri_stream_destroy(lri_stream* s) {
   cudaFree(s->Xl);
   cudaFree(s->Zp);
   cudaFree(s->part);
+  cudaFree(s->part2);
+  cudaFree(s->small2);
+  cudaFree(s->zp2);
   cudaFree(s->small);
   cudaFree(s->Kd);
   cudaFree(s->d_ncols);

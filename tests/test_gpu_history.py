@@ -75,3 +75,54 @@ def test_history_tracks_rank_changes(lri, oracle):
     integ.batch.close()
     assert [y.S.shape[0] for y in sol.Y[1:]] == ranks
     assert len(set(ranks)) > 1, "the rank should change along this stream"
+
+
+def test_history_reused_host_buffers(lri):
+    """Three caller-owned host buffer sets cycled over nine records (each
+    reused once wait() returned for its previous record): every record, read
+    right after its wait, holds exactly the factors of its step."""
+    shapes = [(64, 70, 4), (96, 96, 6)]
+    insts = [_sylvester(30 + i, *s) for i, s in enumerate(shapes)]
+    alg = lri.UnconventionalAlgorithm(lri.RK4(1))
+    kind = lri._native.LRI_OP_SYLVESTER_TRIDIAG
+    factors = [lri.SVDLikeRepresentation(U, S, V) for (A, B, U, S, V) in insts]
+    ops = [lri.SylvesterTridiagOperator(A, B) for (A, B, U, S, V) in insts]
+    mk = lambda: lri.Batch([s[0] for s in shapes], [s[1] for s in shapes], [s[2] for s in shapes], alg, kind, "fp32")
+    ref = mk()
+    ref.upload(factors, ops)
+    expected = []
+    for k in range(9):
+        ref.step(k * 1e-2, 1e-2, 1)
+        expected.append([y.full() for y in ref.download()])
+    ref.close()
+    b = mk()
+    b.upload(factors, ops)
+    h = lri.History(b, slots=2)
+    bufs = [h.host_buffers() for _ in range(3)]
+    seq = [None] * 3
+    got = [None] * 9
+    owner = [None] * 3
+
+    def harvest(slot):
+        hU, hS, hV, hR = bufs[slot]
+        k = owner[slot]
+        got[k] = [y.full() for y in b.unpack(hU.numpy()[:b.U.numel()], hS.numpy()[:b.S.numel()],
+                                             hV.numpy()[:b.V.numel()], hR.numpy()[:b.count])]
+
+    for k in range(9):
+        b.step(k * 1e-2, 1e-2, 1)
+        slot = k % 3
+        if seq[slot] is not None:
+            h.wait(seq[slot])
+            harvest(slot)
+        seq[slot] = h.record(host=bufs[slot])
+        owner[slot] = k
+    for slot in range(3):
+        h.wait(seq[slot])
+        harvest(slot)
+    h.close()
+    b.check_status()
+    b.close()
+    for k in range(9):
+        for i, (y, e) in enumerate(zip(got[k], expected[k])):
+            assert np.array_equal(y, e), f"step {k}, instance {i}"
