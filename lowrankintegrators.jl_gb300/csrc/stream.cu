@@ -2210,19 +2210,44 @@ struct StreamOps {
     double* Gv = blk(15);
     double* Xu = Gu + (int64_t)R * R;
     double* Xv = Gv + (int64_t)R * R;
-    cudaError_t e = gram(n, R, R, U, n, U, n, 1.0, 0.0, Gu, R);
-    if (e == cudaSuccess) e = gram(m, R, R, V, m, V, m, 1.0, 0.0, Gv, R);
+    cudaError_t e = fork_join([&](const StreamOps<T>& o) { return o.gram(n, R, R, U, n, U, n, 1.0, 0.0, Gu, R); },
+                              [&](const StreamOps<T>& o) { return o.gram(m, R, R, V, m, V, m, 1.0, 0.0, Gv, R); });
     if (e != cudaSuccess) return e;
     static std::atomic<uint64_t> attr_done{0};
     e = set_smem_limit(ns_refresh, (int)(2 * SMAX * SMAX * sizeof(float)), attr_done);
     if (e != cudaSuccess) return e;
     ns_refresh<<<1, 1024, 2 * (size_t)R * R * sizeof(float), st>>>(R, s->d_rank, Gu, Gv, Xu, Xv,
                                                                   reinterpret_cast<float*>(s->S), blk(23));
-    if ((e = mul(n, R, R, U, n, Xu, R, T(0), tp(s->Zp), n)) != cudaSuccess) return e;
-    copy_cols<T><<<304, 256, 0, st>>>(n, R, tp(s->Zp), n, U, n);
-    if ((e = mul(m, R, R, V, m, Xv, R, T(0), tp(s->Zp), m)) != cudaSuccess) return e;
-    copy_cols<T><<<304, 256, 0, st>>>(m, R, tp(s->Zp), m, V, m);
-    return cudaGetLastError();
+    auto apply = [&](const StreamOps<T>& o, int N, T* Y, const double* X) -> cudaError_t {
+      cudaError_t e2 = o.mul(N, R, R, Y, N, X, R, T(0), o.zpan(), N);
+      if (e2 != cudaSuccess) return e2;
+      copy_cols<T><<<304, 256, 0, o.st>>>(N, R, o.zpan(), N, Y, N);
+      return cudaGetLastError();
+    };
+    return fork_join([&](const StreamOps<T>& o) { return apply(o, n, U, Xu); },
+                     [&](const StreamOps<T>& o) { return apply(o, m, V, Xv); });
+  }
+
+  // a(ops on the step's stream) and b(ops on the side stream, second scratch
+  // set) run concurrently: b forked after the work queued so far, joined
+  // before anything queued later (a capture must end with the side stream
+  // joined, so the join happens even when a or b fails)
+  template <class FA, class FB>
+  cudaError_t fork_join(const FA& a, const FB& b) const {
+    if (!s->side) {
+      const cudaError_t e = a(*this);
+      return e != cudaSuccess ? e : b(*this);
+    }
+    cudaError_t e = cudaEventRecord(s->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    cudaError_t eb = b(StreamOps<T>{s, s->side, 1});
+    const cudaError_t ej = cudaEventRecord(s->ev_join, s->side);
+    if (eb == cudaSuccess) eb = ej;
+    e = a(*this);
+    const cudaError_t ew = cudaStreamWaitEvent(st, s->ev_join, 0);
+    if (e == cudaSuccess) e = (eb != cudaSuccess) ? eb : ew;
+    return e;
   }
 
   // Uhat = [U0 | orth((I - U0 U0^T) Xk)] (K side: n rows), Vhat likewise
@@ -2241,24 +2266,8 @@ struct StreamOps {
     };
     T* U = tp(s->U);
     T* V = tp(s->V);
-    const bool fork = s->side != nullptr;
-    cudaError_t ev = cudaSuccess;
-    if (fork) {
-      cudaError_t e = cudaEventRecord(s->ev_fork, st);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
-      if (e != cudaSuccess) return e;
-      ev = side(StreamOps<T>{s, s->side, 1}, m, tp(s->Xl), V, tp(s->Vh), blk(4));
-      const cudaError_t ej = cudaEventRecord(s->ev_join, s->side);
-      if (ev == cudaSuccess) ev = ej;
-    }
-    cudaError_t e = side(*this, n, tp(s->Xk), U, tp(s->Uh), blk(3));
-    if (fork) {  // join before anything can return (a capture must end with the side stream joined)
-      const cudaError_t ew = cudaStreamWaitEvent(st, s->ev_join, 0);
-      if (e == cudaSuccess) e = (ev != cudaSuccess) ? ev : ew;
-      return e;
-    }
-    if (e != cudaSuccess) return e;
-    return side(*this, m, tp(s->Xl), V, tp(s->Vh), blk(4));
+    return fork_join([&](const StreamOps<T>& o) { return side(o, n, tp(s->Xk), U, tp(s->Uh), blk(3)); },
+                     [&](const StreamOps<T>& o) { return side(o, m, tp(s->Xl), V, tp(s->Vh), blk(4)); });
   }
 
   // one fused L-flow stage on this object's stream
@@ -2437,8 +2446,8 @@ struct StreamOps {
     cudaMemsetAsync(blk(4), 0, sizeof(double) * (size_t)w * R, st);
     cudaMemcpyAsync(blk(5), blk(18), sizeof(double) * (size_t)w * w, cudaMemcpyDeviceToDevice, st);
     if ((e = core(w)) != cudaSuccess) return e;
-    if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
-    return mul(m, w, R, Vh, m, blk(9), w, T(0), V, m);
+    return fork_join([&](const StreamOps<T>& o) { return o.mul(n, w, R, Uh, n, blk(8), w, T(0), U, n); },
+                     [&](const StreamOps<T>& o) { return o.mul(m, w, R, Vh, m, blk(9), w, T(0), V, m); });
   }
 
   cudaError_t core(int w) const {
@@ -2548,8 +2557,8 @@ struct StreamOps {
     if ((e = gram(n, w, w, Uh, n, tp(s->Zp), n, 1.0, 0.0, blk(5), w)) != cudaSuccess) return e;
     if ((e = core(w)) != cudaSuccess) return e;
     // U1 = Uhat P1, V1 = Vhat Q1
-    if ((e = mul(n, w, R, Uh, n, blk(8), w, T(0), U, n)) != cudaSuccess) return e;
-    return mul(m, w, R, Vh, m, blk(9), w, T(0), V, m);
+    return fork_join([&](const StreamOps<T>& o) { return o.mul(n, w, R, Uh, n, blk(8), w, T(0), U, n); },
+                     [&](const StreamOps<T>& o) { return o.mul(m, w, R, Vh, m, blk(9), w, T(0), V, m); });
   }
 };
 
