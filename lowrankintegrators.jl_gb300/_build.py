@@ -1,9 +1,10 @@
 """Builds the in-tree CUDA library ``_build/liblri_gb300.so`` for sm_103a.
 
-Eleven translation units (FP32, FP64 and double-float engines, the FP32 and
+Twelve translation units (FP32, FP64 and double-float engines, the FP32 and
 double-float engines sized for two CTAs per SM, host C ABI,
 the allocation-free entry point, the discrete adjoint, the large-stream
-engine, its tensor-core snapshot passes, its cluster core SVD) compile in parallel with nvcc and
+engine, its tensor-core snapshot passes, its cluster core SVD, the large
+Burgers engine's tensor-core Khatri-Rao products) compile in parallel with nvcc and
 link into one shared library.  The library is rebuilt
 when a source or the public header is newer than it.
 """
@@ -21,7 +22,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "liblri_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "lri.h")
 
 SOURCES = ["engine_f32.cu", "engine_f64.cu", "engine_df.cu", "engine_f32_occ2.cu", "engine_df_occ2.cu", "api.cpp",
-           "noalloc.cu", "adjoint.cu", "stream.cu", "tc_pass.cu", "core_svd.cu"]
+           "noalloc.cu", "adjoint.cu", "stream.cu", "tc_pass.cu", "core_svd.cu", "tc_kr.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 

@@ -37,6 +37,7 @@
 #include "../../include/lri.h"
 #include "core_svd.h"
 #include "engine.cuh"
+#include "tc_kr.h"
 #include "tc_pass.h"
 
 namespace lri {
@@ -2013,6 +2014,10 @@ struct lri_stream {
   // fused RK-stage kernels for the current rank: 0 none (rank > 32), 1 the K
   // and L stages (rank <= 32), 2 also the S stage (rank <= 16)
   int fused = 0;
+  // FP32 Burgers engines: the Khatri-Rao products of the unfused flows
+  // (active width above 32) on the tensor cores (tc_kr.cu)
+  bool kr_ok = false, use_kr = false;
+  lri::TcKr kr;
   double* fgp = nullptr;  // the fused S stage's per-tile partials: ceil(n / FUSED_BMH) x (2R)^2 FP64
 };
 
@@ -2151,8 +2156,11 @@ struct StreamOps {
                                        Tout);
     return cudaGetLastError();
   }
+  // the tensor-core Khatri-Rao products (FP32 Burgers engines, X == Y)
+  bool kr_tc() const { return std::is_same<T, float>::value && s->use_kr; }
   int kz(int N, int aug) const {
     const int R = (int)s->R, ka = aug ? 2 * R : R;
+    if (kr_tc()) return tc_kr_splits(N, R, aug, std::max(1, s->sms), kZmax);
     const int tiles = ((N + KrTile<T>::BM - 1) / KrTile<T>::BM) * ((ka + 63) / 64);
     return std::max(1, std::min(kZmax, (2 * 152 + tiles - 1) / tiles));
   }
@@ -2161,6 +2169,12 @@ struct StreamOps {
   cudaError_t apply(int N, int aug, const T* X, const T* Y, const T* Tp, T* part, double scale = 1.0,
                     int accum = 0) const {
     const int R = (int)s->R, ka = aug ? 2 * R : R;
+    if constexpr (std::is_same<T, float>::value) {
+      const int k = (Tp == tp(s->tv)) ? 0 : (Tp == tp(s->tl)) ? 1 : (Tp == tp(s->th)) ? 2 : -1;
+      if (kr_tc() && X == Y && k >= 0)
+        return tc_kr_apply(&s->kr, k, N, aug, s->d_rank, X, part, kz(N, aug), scale, accum, s->d_status, ST_TIMEOUT,
+                           st);
+    }
     constexpr int BM = KrTile<T>::BM;
     static std::atomic<uint64_t> attr_same{0}, attr_diff{0};
     const int mx = (int)(2 * (2 * 64) * BM * sizeof(T));
@@ -2270,6 +2284,12 @@ struct StreamOps {
                      [&](const StreamOps<T>& o) { return side(o, m, tp(s->Xl), V, tp(s->Vh), blk(4)); });
   }
 
+  // TF32 split of flow tensor k for the tensor-core products
+  cudaError_t kr_split(int k, const T* Tp, int aug) const {
+    if constexpr (std::is_same<T, float>::value) return tc_kr_split(&s->kr, k, Tp, s->d_rank, aug, st);
+    return cudaSuccess;
+  }
+
   // one fused L-flow stage on this object's stream
   cudaError_t l_stage_fused(const T* Z, const double* Axx, bool nonlin, const RkStage<T>& rk) const {
     const int m = (int)s->m, R = (int)s->R;
@@ -2319,6 +2339,7 @@ struct StreamOps {
     scale_rows<T><<<g, 256, 0, st>>>(m, R, V, nu, P0);
     if ((e = gram(m, R, R, V, m, P0, m, 1.0, 0.0, Nnu, R)) != cudaSuccess) return e;
     if (nonlin && (e = tensor(m, 0, V, V, V, 1.0, 0, tp(s->tv))) != cudaSuccess) return e;
+    if (nonlin && kr_tc() && (e = kr_split(0, tp(s->tv), 0)) != cudaSuccess) return e;
     // operators of the L substep (U0 fixed): A_xx = U0^T Dxx U0,
     // T_L = alpha sym(KR(Dx U0, U0))^T U0 - beta KR(U0, U0)^T Dx U0
     double* Axx = blk(14);
@@ -2326,6 +2347,7 @@ struct StreamOps {
     if ((e = gram(n, R, R, U, n, P0, n, 1.0, 0.0, Axx, R)) != cudaSuccess) return e;
     if (ba != 0.0 && (e = tensor(n, 0, P1, U, U, ba, 0, tp(s->tl))) != cudaSuccess) return e;
     if (bb != 0.0 && (e = tensor(n, 0, U, U, P1, -bb, ba != 0.0, tp(s->tl))) != cudaSuccess) return e;
+    if (nonlin && kr_tc() && (e = kr_split(1, tp(s->tl), 0)) != cudaSuccess) return e;
     // K step: K0 = U0 S0, K' = (Dxx K) N_nu + alpha KR(Dx K, K) T'_V + beta Dx(KR(K, K) T'_V);
     // L step: L0 = V0 S0^T, L' = diag(nu) L A_xx + KR(L, L) T'_L.  The two
     // flows are independent (both start from the old factors): with the
@@ -2392,6 +2414,7 @@ struct StreamOps {
     scale_rows<T><<<g, 256, 0, st>>>(m, w, Vh, nu, P0);
     if ((e = gram(m, w, w, Vh, m, P0, m, 1.0, 0.0, Nnuh, w)) != cudaSuccess) return e;
     if (nonlin && (e = tensor(m, 1, Vh, Vh, Vh, 1.0, 0, tp(s->th))) != cudaSuccess) return e;
+    if (nonlin && kr_tc() && (e = kr_split(2, tp(s->th), 1)) != cudaSuccess) return e;
     // S step on the augmented bases from S~0 = Mh S0 Nh^T (FP64 w x w):
     // S' = A_xx S N_nu + Uhat^T [alpha KR(Dx A, A) T'_Vhat + beta Dx(KR(A, A) T'_Vhat)], A = Uhat S
     small_msn<<<1, 1024, 0, st>>>(w, R, blk(3), blk(16), blk(4), Stmp, blk(18));
@@ -2711,6 +2734,10 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
   alloc((void**)&s->fgp, sizeof(double) * ((n + lri::FUSED_BMH - 1) / lri::FUSED_BMH) * 4 * R * R);
+  if (e == cudaSuccess && dtype == LRI_F32 && lri::tc_kr_supported((int)R)) {
+    e = lri::tc_kr_init(&s->kr, (int)R);
+    s->kr_ok = s->use_kr = (e == cudaSuccess);
+  }
   if (e != cudaSuccess) {
     lri_stream_destroy(s);
     *out = nullptr;
@@ -2780,6 +2807,7 @@ lri_status lri_stream_destroy(lri_stream* s) {
   cudaFree(s->Xk);
   cudaFree(s->Xl);
   cudaFree(s->Zp);
+  lri::tc_kr_free(&s->kr);
   cudaFree(s->part);
   cudaFree(s->part2);
   cudaFree(s->small2);

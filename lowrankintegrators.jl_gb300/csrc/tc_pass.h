@@ -1,7 +1,8 @@
 // tc_pass.h - snapshot passes of the data substeps on the tensor cores
 // (tcgen05 + TMA, sm_103a): out = dY X or dY^T X with dY = A1 - A0 formed in
-// shared memory, FP32 data split into TF32 hi + lo parts (3xTF32 products,
-// FP32 accumulation in tensor memory).
+// registers and stored into tensor memory as the A operand, FP32 data split
+// into TF32 hi + lo parts (3xTF32 products, FP32 accumulation in tensor
+// memory).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -50,5 +51,13 @@ cudaError_t tc_pass_set_tiles(TcPass* t, int splits_rows, int splits_cols, int s
 cudaError_t tc_pass_run(TcPass* t, int trans, const float* A1, const float* A0, const float* X, int64_t ldx,
                         const int32_t* rank, int ncols, float* out, int64_t ldo, float* kd, uint32_t* status,
                         uint32_t status_timeout, cudaStream_t st);
+
+// 2-D FP32 tensor map (CUtensorMap storage) of a column-major rows x cols
+// matrix with ld = rows (a multiple of 4), box box0 x box1, optionally with
+// the 128-byte swizzle; false when the driver's encoder is missing or
+// rejects the shape.
+bool tc_encode_2d(void* out, const void* ptr, uint64_t rows, uint64_t cols, uint32_t box0, uint32_t box1,
+                  bool swizzle);
+bool tc_encoder_available();
 
 }  // namespace lri
