@@ -19,7 +19,7 @@
 //   warps 0-3  thread i forms row i of the chunk's A operand, Y_ia Y_ib for
 //              the 32 pairs (a changes rarely: one shared-memory read per
 //              pair), splits it into TF32 hi + lo and stores both into
-//              tensor memory (tcgen05.st; two A slots);
+//              tensor memory (tcgen05.st; four A slots);
 //   warp 5     allocates tensor memory and issues per 8-wide K slice
 //              tcgen05.mma.kind::tf32 (A from tensor memory, B from shared
 //              memory, M = 128, N = 64): hi*hi into one accumulator, hi*lo
@@ -53,14 +53,17 @@ constexpr int KR_THREADS = 192;       // warps 0-3 transform/drain/epilogue, 4 T
 constexpr int KR_STAGES = 4;
 constexpr int KR_DRAIN = 4;           // chunks per accumulator block
 constexpr int KR_DRAIN_LAG = 2;       // chunks of the next block queued before a drain
-constexpr int KR_A_SLOTS = 2;
+constexpr int KR_A_SLOTS = 4;                    // A operand slots: the transform runs up to 3 chunks ahead
 constexpr int KR_KMAX = 128;          // active columns (2 r_max, r_max <= 64)
 constexpr uint32_t KR_TILE_BYTES = KR_BN * KR_BK * 4;  // one B tile (hi or lo): 8 KB
 constexpr int KR_CTRL_BYTES = 1024;
-constexpr uint32_t KR_TMEM_COLS = 512;  // 2 x (64 main + 64 correction) + 2 x 64 A columns
+constexpr uint32_t KR_TMEM_COLS = 512;  // 2 x (64 main + 64 correction) + 4 x 64 A columns
 constexpr long long KR_WAIT_CYCLES = 4000000000LL;
-// shared memory: the row tile (KR_KMAX x 128 FP32), the stages, control
-constexpr int KR_SMEM = KR_KMAX * KR_BM * 4 + KR_STAGES * 2 * KR_TILE_BYTES + KR_CTRL_BYTES + 1024;
+constexpr int KR_PMAX = KR_KMAX * (KR_KMAX + 1) / 2;  // packed pairs at the widest panel
+// shared memory: the stages, the row tile (KR_KMAX x 128 FP32), the pair
+// table (a | b << 8 per pair, 16 bits), control
+constexpr int KR_TAB_BYTES = ((KR_PMAX * 2 + 1023) / 1024) * 1024;
+constexpr int KR_SMEM = KR_STAGES * 2 * KR_TILE_BYTES + KR_KMAX * KR_BM * 4 + KR_TAB_BYTES + KR_CTRL_BYTES + 1024;
 
 struct KrArgs {
   int N, R, aug, kz;
@@ -94,7 +97,8 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
                                                          ~static_cast<uintptr_t>(1023));
   unsigned char* stages = base;                                       // KR_STAGES x (hi, lo) B tiles
   float* ys = reinterpret_cast<float*>(base + KR_STAGES * 2 * KR_TILE_BYTES);  // [column][128 rows]
-  unsigned char* ctrl = reinterpret_cast<unsigned char*>(ys + KR_KMAX * KR_BM);
+  uint16_t* tab = reinterpret_cast<uint16_t*>(ys + KR_KMAX * KR_BM);           // pair p -> a | b << 8
+  unsigned char* ctrl = reinterpret_cast<unsigned char*>(tab) + KR_TAB_BYTES;
   const uint32_t bar0 = smem_u32(ctrl);
   auto full = [&](int s) { return bar0 + 8u * s; };
   auto tfull = [&](int s) { return bar0 + 8u * (KR_STAGES + s); };
@@ -129,6 +133,11 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
         if (e < total) ys[e] = v[u];
       }
     }
+  }
+  // pair table: row a of the triangle starts at a ka - a (a - 1) / 2
+  for (int pa = tid; pa < ka; pa += KR_THREADS) {
+    const int st0 = pa * ka - pa * (pa - 1) / 2;
+    for (int pb = pa; pb < ka; ++pb) tab[st0 + pb - pa] = (uint16_t)(pa | (pb << 8));
   }
   if (tid == 0) {
     for (int s = 0; s < KR_STAGES; ++s) {
@@ -237,28 +246,21 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
       mbar_arrive(acc_empty(b));
       return true;
     };
-    // pair of the chunk's first entry: (pa, pb) with p = start(pa) + pb - pa
-    int pa = 0, pb = 0;
-    {
-      const int p0 = kc0 * KR_BK;
-      while (pa + 1 < ka && (pa + 1) * ka - (pa + 1) * pa / 2 <= p0) ++pa;
-      pb = pa + (p0 - (pa * ka - pa * (pa - 1) / 2));
-    }
     const float* yrow = ys + tid;  // column c of this row at yrow[c * KR_BM]
     for (int it = 0; it < nk; ++it) {
       const int p0 = (kc0 + it) * KR_BK;
       float h[KR_BK], l[KR_BK];
-      float ya = (pa < ka) ? yrow[pa * KR_BM] : 0.0f;
+      // the chunk's pairs from the table (a broadcast read each): independent
+      // entries, so their shared-memory reads overlap
 #pragma unroll
       for (int j = 0; j < KR_BK; ++j) {
+        const int p = p0 + j;
         float v = 0.0f;
-        if (p0 + j < np) v = ya * yrow[pb * KR_BM];  // (pa, pb) stay inside the triangle while p < np
-        split(v, h[j], l[j]);
-        if (++pb >= ka) {  // next row of the pair triangle
-          ++pa;
-          pb = pa;
-          ya = (pa < ka) ? yrow[pa * KR_BM] : 0.0f;
+        if (p < np) {
+          const uint32_t ab = tab[p];
+          v = yrow[(ab & 0xffu) * KR_BM] * yrow[(ab >> 8) * KR_BM];
         }
+        split(v, h[j], l[j]);
       }
       if (it >= KR_A_SLOTS) {
         const bool okA = wait(aempty(it % KR_A_SLOTS), (uint32_t)(it / KR_A_SLOTS - 1) & 1u);
