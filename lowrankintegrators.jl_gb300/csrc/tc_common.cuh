@@ -150,5 +150,29 @@ __device__ __forceinline__ bool bar_any(bool flag) {
   return out != 0;
 }
 
+// the same over the first nthreads threads (a multiple of 32) of the CTA
+__device__ __forceinline__ bool bar_any_n(bool flag, int nthreads) {
+  uint32_t out;
+  asm volatile(
+      "{\n.reg .pred p, q;\n"
+      "setp.ne.u32 p, %1, 0;\n"
+      "bar.red.or.pred q, 1, %2, p;\n"
+      "selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(out)
+      : "r"((uint32_t)flag), "r"(nthreads)
+      : "memory");
+  return out != 0;
+}
+
+// a warp's 32 lanes x 16 consecutive columns: thread t writes lane (base + t)
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+      : "memory");
+}
+
 }  // namespace
 }  // namespace lri

@@ -13,21 +13,23 @@
 // chunks (32 pairs each):
 //   all warps  load the tile's rows of Y (every active column) into shared
 //              memory once;
-//   warp 4     TMA producer: per chunk, the chunk's 32 rows of the TF32 hi and
+//   warp 8     TMA producer: per chunk, the chunk's 32 rows of the TF32 hi and
 //              lo copies of T' (split once per step by tc_kr_split), 64
 //              columns, into a 4-stage mbarrier pipeline;
-//   warps 0-3  thread i forms row i of the chunk's A operand, Y_ia Y_ib for
-//              the 32 pairs (a changes rarely: one shared-memory read per
-//              pair), splits it into TF32 hi + lo and stores both into
+//   warps 0-7  two warpgroups, one per half of the chunk's 32 pairs: thread
+//              i of a group forms row i of its 16 A columns, Y_ia Y_ib from
+//              a pair table (independent entries: the shared-memory reads
+//              overlap), splits them into TF32 hi + lo and stores both into
 //              tensor memory (tcgen05.st; four A slots);
-//   warp 5     allocates tensor memory and issues per 8-wide K slice
+//   warp 9     allocates tensor memory and issues per 8-wide K slice
 //              tcgen05.mma.kind::tf32 (A from tensor memory, B from shared
 //              memory, M = 128, N = 64): hi*hi into one accumulator, hi*lo
 //              + lo*hi into a correction accumulator;
-//   warps 0-3  drain the accumulators into FP32 registers every 4 chunks
-//              (two accumulator buffers: the tensor cores' FP32 accumulation
-//              truncates, so the number of MMAs summed in one accumulator
-//              stays at 12) and finally write the CTA's partial.
+//   warps 0-7  drain the accumulators into FP32 registers every 4 chunks,
+//              each warpgroup 32 of the 64 columns (two accumulator buffers:
+//              the tensor cores' FP32 accumulation truncates, so the number
+//              of MMAs summed in one accumulator stays at 12) and finally
+//              write the CTA's partial.
 // Every mbarrier wait is bounded; a wait that gives up sets a status bit, the
 // CTA stops issuing work, waits (bounded) for its copies and MMAs in flight,
 // frees its tensor memory and returns.
@@ -49,7 +51,8 @@ namespace {
 constexpr int KR_BM = 128;            // rows per CTA (UMMA M)
 constexpr int KR_BN = 64;             // output columns per CTA (UMMA N)
 constexpr int KR_BK = 32;             // pairs per chunk: one 128-byte swizzle row of FP32
-constexpr int KR_THREADS = 192;       // warps 0-3 transform/drain/epilogue, 4 TMA, 5 MMA
+constexpr int KR_THREADS = 320;       // warps 0-7 transform/drain/epilogue, 8 TMA, 9 MMA
+constexpr int KR_TX = 256;            // transform threads: two warpgroups, one per half of a chunk's pairs
 constexpr int KR_STAGES = 4;
 constexpr int KR_DRAIN = 4;           // chunks per accumulator block
 constexpr int KR_DRAIN_LAG = 2;       // chunks of the next block queued before a drain
@@ -142,19 +145,19 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
   if (tid == 0) {
     for (int s = 0; s < KR_STAGES; ++s) {
       mbar_init(full(s), 1);
-      mbar_init(tfull(s), 128);
+      mbar_init(tfull(s), KR_TX);
       mbar_init(empty(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(acc_full(b), 1);
-      mbar_init(acc_empty(b), 128);
+      mbar_init(acc_empty(b), KR_TX);
     }
     for (int t = 0; t < KR_A_SLOTS; ++t) mbar_init(aempty(t), 1);
     mbar_init(done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(KR_TMEM_COLS)
                  : "memory");
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
   const uint32_t a_col = 4u * KR_BN;  // A slots after the two accumulator buffers
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       int last_par[KR_STAGES];
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
           if (last_par[s] >= 0) wait(full(s), (uint32_t)last_par[s], KR_WAIT_CYCLES / 4);
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_tf32(KR_BM, KR_BN);
@@ -221,21 +224,23 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
     }
     __syncwarp();
   } else {
-    // -------- A operand, drains, epilogue (warps 0-3; thread tid = row tid) --------
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    float acc[KR_BN];
+    // -------- A operand, drains, epilogue (warps 0-7: group g = half of the pairs and columns) --------
+    const int g = tid >> 7, row_t = tid & 127;  // tensor-memory lane = row_t (warp % 4 picks the quarter)
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    constexpr int HN = KR_BN / 2, HK = KR_BK / 2;
+    float acc[HN];
 #pragma unroll
-    for (int c = 0; c < KR_BN; ++c) acc[c] = 0.0f;
+    for (int c = 0; c < HN; ++c) acc[c] = 0.0f;
     bool aborted = false;
     int drained = 0;
     auto drain = [&](int k) {
       const int b = k & 1;
       const bool ok = wait(acc_full(b), (uint32_t)(k >> 1) & 1u);
-      if (bar_any(!ok)) return false;
+      if (bar_any_n(!ok, KR_TX)) return false;
       tc_fence_after();
-      const uint32_t dmain = tmem + lane_base + (uint32_t)(2 * b * KR_BN), dcorr = dmain + (uint32_t)KR_BN;
+      const uint32_t dmain = tmem + lane_base + (uint32_t)(2 * b * KR_BN + HN * g), dcorr = dmain + (uint32_t)KR_BN;
 #pragma unroll
-      for (int cc = 0; cc < KR_BN; cc += 16) {
+      for (int cc = 0; cc < HN; cc += 16) {
         float v[16], w[16];
         tmem_ld16(dmain + (uint32_t)cc, v);
         tmem_ld16(dcorr + (uint32_t)cc, w);
@@ -246,14 +251,14 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
       mbar_arrive(acc_empty(b));
       return true;
     };
-    const float* yrow = ys + tid;  // column c of this row at yrow[c * KR_BM]
+    const float* yrow = ys + row_t;  // column c of this row at yrow[c * KR_BM]
     for (int it = 0; it < nk; ++it) {
-      const int p0 = (kc0 + it) * KR_BK;
-      float h[KR_BK], l[KR_BK];
-      // the chunk's pairs from the table (a broadcast read each): independent
+      const int p0 = (kc0 + it) * KR_BK + HK * g;  // this group's 16 pairs
+      float h[HK], l[HK];
+      // the pairs from the table (a broadcast read each): independent
       // entries, so their shared-memory reads overlap
 #pragma unroll
-      for (int j = 0; j < KR_BK; ++j) {
+      for (int j = 0; j < HK; ++j) {
         const int p = p0 + j;
         float v = 0.0f;
         if (p < np) {
@@ -264,15 +269,16 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
       }
       if (it >= KR_A_SLOTS) {
         const bool okA = wait(aempty(it % KR_A_SLOTS), (uint32_t)(it / KR_A_SLOTS - 1) & 1u);
-        if (bar_any(!okA)) {
+        if (bar_any_n(!okA, KR_TX)) {
           aborted = true;
           break;
         }
         tc_fence_after();
       }
-      const uint32_t ta = tmem + lane_base + a_col + (uint32_t)(64 * (it % KR_A_SLOTS));
-      tmem_st32(ta, h);
-      tmem_st32(ta + 32u, l);
+      // slot: hi in columns [0, 32), lo in [32, 64); this group's 16 of each
+      const uint32_t ta = tmem + lane_base + a_col + (uint32_t)(64 * (it % KR_A_SLOTS) + HK * g);
+      tmem_st16(ta, h);
+      tmem_st16(ta + 32u, l);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       tc_fence_before();
       mbar_arrive(tfull(it % KR_STAGES));
@@ -289,12 +295,12 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
       ++drained;
     }
     if (!aborted) {
-      const int row = i0 + tid;
+      const int row = i0 + row_t;
       if (row < a.N) {
         float* dst = a.part + (int64_t)z * a.N * (2 * a.R);
 #pragma unroll
-        for (int cc = 0; cc < KR_BN; ++cc) {
-          const int c = c0 + cc;
+        for (int cc = 0; cc < HN; ++cc) {
+          const int c = c0 + HN * g + cc;
           if (c < ka) {
             float* d = dst + row + (int64_t)kr_col(c, r, a.R, a.aug) * a.N;
             *d = a.accum ? fmaf(a.scale, acc[cc], *d) : a.scale * acc[cc];
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(KR_THREADS, 1)
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 5) {
+  if (warp == 9) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(KR_TMEM_COLS) : "memory");
   }
