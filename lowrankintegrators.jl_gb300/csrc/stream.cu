@@ -1995,6 +1995,8 @@ struct lri_stream {
   void* kgp = nullptr;  // split partials of the tensor sums (ceil(max(n, m) / KR_ROWS) x PP x 2R) and of gram_act
   void* kap = nullptr;  // pair-split partials of the Khatri-Rao products: 2 x kZmax x max(n, m) x 2R
   void* pw = nullptr;   // 3 work panels of max(n, m) x 2R
+  void* pw2 = nullptr;     // the side stream's L-flow product panel, max(n, m) x 2R
+  void* kap2nd = nullptr;  // the side stream's L-flow Khatri-Rao partials, kZmax x max(n, m) x 2R
   // one captured Burgers step (launch shapes depend on r_max only; the rank
   // is read on the device), replayed while dt and the bound factors stay
   cudaStream_t cap = nullptr;
@@ -2298,10 +2300,27 @@ struct StreamOps {
         s->d_status, rk);
     return cudaGetLastError();
   }
-  // the whole L substep flow with the fused stages (Lp holds L0 and its RK panels)
-  cudaError_t l_flow_fused(T* Lp, const double* Axx, bool nonlin) const {
-    return rk_panel((int64_t)s->m * s->R, Lp,
-                    [&](const T* Z, const RkStage<T>& rk) { return l_stage_fused(Z, Axx, nonlin, rk); });
+  // the whole L substep flow (Lp holds L0 and its RK panels): the fused
+  // stages, or the product panel, the Khatri-Rao partials and the combine
+  // (with the side stream's own panel and partials for scratch set 1)
+  cudaError_t l_flow(T* Lp, const double* Axx, bool nonlin) const {
+    if (s->fused >= 1)
+      return rk_panel((int64_t)s->m * s->R, Lp,
+                      [&](const T* Z, const RkStage<T>& rk) { return l_stage_fused(Z, Axx, nonlin, rk); });
+    const int m = (int)s->m, R = (int)s->R, w = 2 * R;
+    const int64_t nm = std::max(s->n, s->m);
+    T* P2 = sid ? tp(s->pw2) : tp(s->pw) + 2 * nm * w;
+    T* kap1 = tp(sid ? s->kap2nd : s->kap);
+    const T* nu = static_cast<const T*>(s->nu);
+    const int zl = kz(m, 0);
+    return rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
+      panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
+      cudaError_t e2 = cudaGetLastError();
+      if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
+      if (e2 != cudaSuccess) return e2;
+      flow_combine_rows<T><<<304, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, rk);
+      return cudaGetLastError();
+    });
   }
 
   cudaError_t burgers_step() const {
@@ -2356,12 +2375,12 @@ struct StreamOps {
     T* Lp = tp(s->Lp);
     if ((e = mul(n, R, R, U, n, blk(16), R, T(0), Kp, n)) != cudaSuccess) return e;
     if ((e = mul(m, R, R, V, m, blk(17), R, T(0), Lp, m)) != cudaSuccess) return e;
-    const bool fork = s->fused >= 1 && s->side;
+    const bool fork = s->side != nullptr && (s->fused >= 1 || s->pw2 != nullptr);
     cudaError_t el = cudaSuccess;
     if (fork) {
       if ((e = cudaEventRecord(s->ev_fork, st)) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(s->side, s->ev_fork, 0)) != cudaSuccess) return e;
-      el = StreamOps<T>{s, s->side}.l_flow_fused(Lp, Axx, nonlin);
+      el = StreamOps<T>{s, s->side, 1}.l_flow(Lp, Axx, nonlin);
       const cudaError_t ej = cudaEventRecord(s->ev_join, s->side);
       if (el == cudaSuccess) el = ej;
     }
@@ -2388,19 +2407,7 @@ struct StreamOps {
       if (e == cudaSuccess) e = (el != cudaSuccess) ? el : ew;
     }
     if (e != cudaSuccess) return e;
-    if (!fork) {
-      const int zl = kz(m, 0);
-      e = rk_panel((int64_t)m * R, Lp, [&](const T* Z, const RkStage<T>& rk) {
-        if (s->fused >= 1) return l_stage_fused(Z, Axx, nonlin, rk);
-        panel_mul_act<T><<<dim3((m + 31) / 32, (R + 63) / 64), 256, 0, st>>>(m, R, 0, s->d_rank, Z, Axx, R, P2);
-        cudaError_t e2 = cudaGetLastError();
-        if (e2 == cudaSuccess && nonlin) e2 = apply(m, 0, Z, Z, tp(s->tl), kap1);
-        if (e2 != cudaSuccess) return e2;
-        flow_combine_rows<T><<<g, 256, 0, st>>>(m, R, s->d_rank, nu, P2, nonlin ? kap1 : nullptr, zl, rk);
-        return cudaGetLastError();
-      });
-      if (e != cudaSuccess) return e;
-    }
+    if (!fork && (e = l_flow(Lp, Axx, nonlin)) != cudaSuccess) return e;
     // augmented bases Uhat = [U0 | orth((I - U0 U0^T) K1)], Vhat likewise; Mh, Nh
     copy_cols<T><<<304, 256, 0, st>>>(n, R, Kp, n, Xk, n);
     copy_cols<T><<<304, 256, 0, st>>>(m, R, Lp, m, Xl, m);
@@ -2733,6 +2740,8 @@ lri_status lri_burgers_create(lri_stream** out, int32_t dtype, int64_t n, int64_
                                    (int64_t)sizeof(double) * ((n + GA_ROWS - 1) / GA_ROWS) * 4 * R * R));
   alloc(&s->kap, s->es * 2 * kZmax * nm * 2 * R);
   alloc(&s->pw, s->es * 3 * nm * 2 * R);
+  alloc(&s->pw2, s->es * nm * 2 * R);
+  alloc(&s->kap2nd, s->es * kZmax * nm * 2 * R);
   alloc((void**)&s->fgp, sizeof(double) * ((n + lri::FUSED_BMH - 1) / lri::FUSED_BMH) * 4 * R * R);
   if (e == cudaSuccess && dtype == LRI_F32 && lri::tc_kr_supported((int)R)) {
     e = lri::tc_kr_init(&s->kr, (int)R);
@@ -2799,6 +2808,8 @@ lri_status lri_stream_destroy(lri_stream* s) {
   cudaFree(s->kgp);
   cudaFree(s->kap);
   cudaFree(s->pw);
+  cudaFree(s->pw2);
+  cudaFree(s->kap2nd);
   cudaFree(s->fgp);
   cudaFree(s->d_rank);
   cudaFree(s->d_status);
