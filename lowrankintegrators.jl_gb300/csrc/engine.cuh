@@ -799,6 +799,267 @@ __device__ bool fused_substep(int N, int r, const T* X, int ldx, const T* C, int
   return true;
 }
 
+// Register-resident K (or L) substep of the Sylvester flow for short panels
+// (N <= NT rows, r <= RR columns): thread i keeps row i of the state in
+// registers for the whole substep interval, so the ns*nsub Horner
+// applications
+//   w <- g_j y + h L(w),   L(w) = (T w) G + w P^T   (G = I: orthonormal form)
+// read and write global memory only at the start and the end.  Rows reach
+// their neighbours (the tridiagonal T) through a double-buffered
+// column-major copy in shared memory with a zero row on each side: one
+// barrier per application.  Every thread carries a row, so all eight warps
+// feed the arithmetic pipe (in FP64 the SM's few FP64 units are the bound of
+// this path; the tiled products leave most warps idle on such panels).
+// Literal form (FP64, G = X^T X): G = I + E with E applied in FP32 when
+// max|E| <= 2^-36 (the basis is orthonormal to working precision), which
+// keeps the E term's FP32 rounding below 2^-54 of T w and removes a third of
+// the FP64 multiply-adds; otherwise the full G product.  y stays in shared
+// memory (registers go to w and the accumulators).
+template <typename T, int RR, bool ORTHO>
+__device__ __noinline__ void reg_substep_rr(int N, int r, T* Y, const T* tri, const T* G, const T* P, int ldp, const double* gam,
+                               int ns, int nsub, T h, T* stage) {
+  const int tid = threadIdx.x;
+  const int LDZ = N + 2;
+  T* zb0 = stage;                  // zb[k*LDZ + 1 + i] = w(i, k); entries 0 and N+1 stay zero
+  T* zb1 = zb0 + RR * LDZ;
+  T* ys = zb1 + RR * LDZ;          // ys[k*N + i] = y(i, k)
+  T* Ps = ys + RR * N;             // Ps[k*RR + c] = P(c, k)
+  T* Gs = Ps + RR * RR;            // Gs[k*RR + c] = G(k, c)
+  float* Es = reinterpret_cast<float*>(Gs + RR * RR);  // Es[k*RR + c] = G(k, c) - [k == c]
+  int full = 0;
+  for (int e = tid; e < RR * RR; e += NT) {
+    const int k = e / RR, c = e - k * RR;
+    T pv = T(0);
+    if (k < r && c < r) pv = P[c + (int64_t)k * ldp];
+    Ps[e] = pv;
+    if constexpr (!ORTHO) {
+      const T gv = (k < r && c < r) ? G[k + (int64_t)c * ldp] : T(0);
+      const T ev = gv - ((k == c && k < r) ? T(1) : T(0));
+      Gs[e] = gv;
+      Es[e] = (float)ev;
+      if (!(fabs(ev) <= T(0x1p-36))) full = 1;  // NaN included
+    }
+  }
+  // the zero rows at both ends of both buffers (disjoint from the rows below)
+  for (int e = tid; e < 4 * RR; e += NT) {
+    const int b = e / (2 * RR), k = (e >> 1) % RR;
+    (b ? zb1 : zb0)[k * LDZ + ((e & 1) ? N + 1 : 0)] = T(0);
+  }
+  const bool own = tid < N;
+  T w[RR];
+  T cs = T(0), cd = T(0), cp = T(0);
+#pragma unroll
+  for (int k = 0; k < RR; ++k) w[k] = (own && k < r) ? Y[tid + (int64_t)k * N] : T(0);
+  if (own) {
+    cd = tri[N + tid];
+    if (tid > 0) cs = tri[tid];
+    if (tid + 1 < N) cp = tri[2 * N + tid];
+#pragma unroll
+    for (int k = 0; k < RR; ++k) {
+      zb0[k * LDZ + 1 + tid] = w[k];
+      ys[k * N + tid] = w[k];
+    }
+  }
+  const bool full_g = __syncthreads_or(full) != 0;
+  T* zin = zb0;
+  T* zout = zb1;
+  for (int sub = 0; sub < nsub; ++sub) {
+    T hw = h * T(gam[ns]);
+    for (int j = ns - 1; j >= 0; --j) {
+      const T gj = (j == 0) ? T(1) : T(gam[j]);
+      if (own) {
+        T acc[RR];
+        if constexpr (ORTHO) {
+#pragma unroll
+          for (int c = 0; c < RR; ++c) acc[c] = T(0);
+#pragma unroll
+          for (int k = 0; k < RR; ++k)
+#pragma unroll
+            for (int c = 0; c < RR; ++c) acc[c] = fma_acc(w[k], Ps[k * RR + c], acc[c]);
+#pragma unroll
+          for (int c = 0; c < RR; ++c) {
+            const T tz = fma(cs, zin[c * LDZ + tid], fma(cp, zin[c * LDZ + tid + 2], cd * w[c]));
+            acc[c] = fma(hw, tz + renorm(acc[c]), gj * ys[c * N + tid]);
+          }
+        } else {
+          // acc = T w (the stencil rows), then acc G + w P^T
+#pragma unroll
+          for (int k = 0; k < RR; ++k)
+            acc[k] = fma(cs, zin[k * LDZ + tid], fma(cp, zin[k * LDZ + tid + 2], cd * w[k]));
+          bool in_range = true;
+#pragma unroll
+          for (int k = 0; k < RR; ++k) in_range = in_range && (fabs(acc[k]) < T(0x1p100));
+          if (!full_g && in_range) {
+            float e[RR];
+#pragma unroll
+            for (int c = 0; c < RR; ++c) e[c] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < RR; ++k) {
+              const float tk = (float)acc[k];
+#pragma unroll
+              for (int c = 0; c < RR; ++c) e[c] = fmaf(tk, Es[k * RR + c], e[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < RR; ++c) acc[c] += T(e[c]);
+          } else {
+            T tz[RR];
+#pragma unroll
+            for (int k = 0; k < RR; ++k) tz[k] = acc[k];
+#pragma unroll
+            for (int c = 0; c < RR; ++c) acc[c] = T(0);
+#pragma unroll
+            for (int k = 0; k < RR; ++k)
+#pragma unroll
+              for (int c = 0; c < RR; ++c) acc[c] = fma(tz[k], Gs[k * RR + c], acc[c]);
+          }
+#pragma unroll
+          for (int k = 0; k < RR; ++k)
+#pragma unroll
+            for (int c = 0; c < RR; ++c) acc[c] = fma(w[k], Ps[k * RR + c], acc[c]);
+#pragma unroll
+          for (int c = 0; c < RR; ++c) acc[c] = fma(hw, acc[c], gj * ys[c * N + tid]);
+        }
+#pragma unroll
+        for (int c = 0; c < RR; ++c) {
+          w[c] = acc[c];
+          zout[c * LDZ + 1 + tid] = acc[c];
+        }
+        // the substep's result is the next substep's base (only this
+        // thread reads its own row of y)
+        if (j == 0 && sub + 1 < nsub) {
+#pragma unroll
+          for (int c = 0; c < RR; ++c) ys[c * N + tid] = acc[c];
+        }
+      }
+      __syncthreads();
+      T* t = zin;
+      zin = zout;
+      zout = t;
+      hw = h;
+    }
+  }
+  if (own) {
+    for (int k = 0; k < r; ++k) Y[tid + (int64_t)k * N] = w[k];
+  }
+  __syncthreads();
+}
+
+// Dispatch of reg_substep_rr by panel width; false when the panel does not
+// fit the path (more than NT rows or 8 columns, or the staging area).
+template <typename T, bool ORTHO>
+__device__ bool reg_substep(int N, int r, T* Y, const T* tri, const T* G, const T* P, int ldp, const double* gam,
+                            int ns, int nsub, T h, T* stage) {
+  if (N > NT || r > 8) return false;
+  const int RR = (r <= 4) ? 4 : 8;
+  const int64_t need = (int64_t)RR * (2 * (N + 2) + N) + 3 * RR * RR;
+  if (need > Stage<T>::ELEMS) return false;
+  if (RR == 4)
+    reg_substep_rr<T, 4, ORTHO>(N, r, Y, tri, G, P, ldp, gam, ns, nsub, h, stage);
+  else
+    reg_substep_rr<T, 8, ORTHO>(N, r, Y, tri, G, P, ldp, gam, ns, nsub, h, stage);
+  return true;
+}
+
+// S substep of the Sylvester flow on a small p x q core (p*q <= NT, p, q <=
+// 16): thread i + j*p keeps entry (i, j) of the state and of the RK
+// accumulator in registers; the stage inputs alternate between two
+// shared-memory copies, so a stage costs one barrier (orthonormal form
+//   k = sign (P_U Z + Z P_V^T))
+// or two (literal form, k = sign (P_U (Z G_V) + G_U (Z P_V^T)), whose two
+// inner products go through shared memory first).  The RK update is the
+// stage-by-stage scheme of the panel path (same operations per entry).
+// St, G_U, P_U, G_V, P_V: column-major with leading dimension W.
+template <typename T, bool ORTHO>
+__device__ __noinline__ void core_small(int p, int q, int W, T* St, T sign, const T* GU, const T* PU, const T* GV,
+                                        const T* PV, const Scheme& sc, T h, T* stage) {
+  const int tid = threadIdx.x;
+  const int pq = p * q;
+  T* Zb0 = stage;               // Zb[i + k*p] = Z(i, k)
+  T* Zb1 = Zb0 + pq;
+  T* T1s = Zb1 + pq;            // T1s[k + j*p] = (Z G_V)(k, j)
+  T* T2s = T1s + pq;            // T2s[k + j*p] = (Z P_V^T)(k, j)
+  T* PUs = T2s + pq;            // PUs[i + k*p] = P_U(i, k)
+  T* GUs = PUs + p * p;
+  T* PVs = GUs + p * p;         // PVs[j + k*q] = P_V(j, k)
+  T* GVs = PVs + q * q;         // GVs[k + j*q] = G_V(k, j)
+  for (int e = tid; e < p * p; e += NT) {
+    const int i = e % p, k = e / p;
+    PUs[e] = PU[i + (int64_t)k * W];
+    if constexpr (!ORTHO) GUs[e] = GU[i + (int64_t)k * W];
+  }
+  for (int e = tid; e < q * q; e += NT) {
+    const int a = e % q, b = e / q;
+    PVs[e] = PV[a + (int64_t)b * W];
+    if constexpr (!ORTHO) GVs[e] = GV[a + (int64_t)b * W];
+  }
+  const bool own = tid < pq;
+  const int i = own ? tid % p : 0, j = own ? tid / p : 0;
+  T st = T(0), sa = T(0);
+  if (own) {
+    st = St[i + (int64_t)j * W];
+    Zb0[i + j * p] = st;
+  }
+  __syncthreads();
+  const int ns = sc.nstages;
+  int cur = 0;
+  for (int sub = 0; sub < sc.nsub; ++sub) {
+    for (int s = 0; s < ns; ++s) {
+      const T* Z = cur ? Zb1 : Zb0;
+      T* Zo = cur ? Zb0 : Zb1;
+      T kv = T(0);
+      if constexpr (ORTHO) {
+        if (own) {
+          T a0 = T(0), a1 = T(0);
+          for (int k = 0; k < p; ++k) a0 = fma(PUs[i + k * p], Z[k + j * p], a0);
+          for (int k = 0; k < q; ++k) a1 = fma(Z[i + k * p], PVs[j + k * q], a1);
+          kv = sign * (a0 + a1);
+        }
+      } else {
+        if (own) {
+          T t1 = T(0), t2 = T(0);
+          for (int k = 0; k < q; ++k) {
+            const T z = Z[i + k * p];
+            t1 = fma(z, GVs[k + j * q], t1);
+            t2 = fma(z, PVs[j + k * q], t2);
+          }
+          T1s[i + j * p] = t1;
+          T2s[i + j * p] = t2;
+        }
+        __syncthreads();
+        if (own) {
+          T a0 = T(0), a1 = T(0);
+          for (int k = 0; k < p; ++k) {
+            a0 = fma(PUs[i + k * p], T1s[k + j * p], a0);
+            a1 = fma(GUs[i + k * p], T2s[k + j * p], a1);
+          }
+          kv = sign * (a0 + a1);
+        }
+      }
+      if (own) {
+        const T bs = T(sc.b[s]);
+        const T an = (s + 1 < ns) ? T(sc.a[s + 1]) : T(0);
+        if (ns == 1) {
+          st = fma(h * bs, kv, st);
+          Zo[i + j * p] = st;
+        } else if (s == 0) {
+          sa = bs * kv;
+          Zo[i + j * p] = fma(h * an, kv, st);
+        } else if (s + 1 < ns) {
+          sa = fma(bs, kv, sa);
+          Zo[i + j * p] = fma(h * an, kv, st);
+        } else {
+          st = fma(h, fma(bs, kv, sa), st);
+          Zo[i + j * p] = st;
+        }
+      }
+      __syncthreads();
+      cur ^= 1;
+    }
+  }
+  if (own) St[i + (int64_t)j * W] = st;
+  __syncthreads();
+}
+
 // W loader: column-major matrix W (ld ldw0) or its transpose.
 template <typename T>
 struct LoadSmall {

@@ -272,6 +272,8 @@ __device__ void substep_side(const StepArgs<T>& g, const Inst<T>& I, const Side<
   double gam[5];
   horner_coeffs(sc, gam);
   const T h = T(dt / sc.nsub);
+  // short panels: the whole substep interval with the rows in registers
+  if (reg_substep<T, ortho>(N, r, Y, sd.tri, G, P, I.W, gam, ns, sc.nsub, h, sm.stage)) return;
   T* Zb[2] = {sd.PZ0, sd.PZ1};
   for (int sub = 0; sub < sc.nsub; ++sub) {
     // the first application acts on gamma_ns * y: fold gamma_ns into h
@@ -348,6 +350,12 @@ __device__ __noinline__ void substep_core(const StepArgs<T>& g, const Inst<T>& I
         __syncthreads();
       }
     }
+    return;
+  }
+  if (p * q <= NT && p <= 16 && q <= 16) {
+    // small cores: state in registers, one or two barriers per stage
+    core_small<T, AssumeOrthonormal<T>::value>(p, q, W, St, sign, GUp, GUp + (int64_t)p * W, GVp,
+                                               GVp + (int64_t)q * W, sc, T(dt / sc.nsub), sm.stage);
     return;
   }
   const T* GU = GUp;
