@@ -1044,10 +1044,22 @@ def bug_gradient(prob: MatrixDEProblem, alg: UnconventionalAlgorithm, dt: float,
         Ubar, Sbar, Vbar = col(Ub), col(Sb), col(Vb)
         thb = torch.zeros(n, dtype=torch.float64, device=dev)
         ptr = lambda x: C.c_void_p(x.data_ptr())
-        stream = b._stream()
-        for ci in reversed(range(len(ckpts))):
-            k0 = ci * c
-            k1 = min(k, k0 + c)
+        # The replay of a segment depends only on its checkpoint, so segment
+        # ci - 1 is replayed on the current stream while the reverse steps of
+        # segment ci run on a side stream (the reverse step has its own
+        # workspace and reads the replayed inputs only).  The host keeps at
+        # most two segments ahead of the reverse sweep, so the saved inputs
+        # stay O(checkpoint_every) steps.
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(main)
+        side_ptr = C.c_void_p(side.cuda_stream)
+        swept = {}  # segment -> event recorded after its reverse steps
+
+        def replay(ci):
+            k0, k1 = ci * c, min(k, ci * c + c)
+            if ci + 2 in swept:
+                swept.pop(ci + 2).synchronize()
             for dst, src in zip((b.U, b.S, b.V), ckpts[ci]):
                 dst.copy_(src)
             b.bind()  # the cached projections belong to the checkpoint's bases
@@ -1055,10 +1067,26 @@ def bug_gradient(prob: MatrixDEProblem, alg: UnconventionalAlgorithm, dt: float,
             for j in range(k0, k1):
                 inputs.append((b.U.clone(), b.S.clone(), b.V.clone()))
                 b.step(t0 + j * dt, dt, 1)
+            ready = torch.cuda.Event()
+            ready.record(main)
+            return inputs, ready
+
+        nxt = replay(len(ckpts) - 1)
+        for ci in reversed(range(len(ckpts))):
+            inputs, ready = nxt
+            side.wait_event(ready)
             for (U0, S0, V0) in reversed(inputs):
+                for x in (U0, S0, V0):
+                    x.record_stream(side)
                 _native.check(b.lib.lri_batch_adjoint_step(b.handle, float(dt), ptr(U0), ptr(S0), ptr(V0),
-                                                           ptr(Ubar), ptr(Sbar), ptr(Vbar), ptr(thb), stream),
+                                                           ptr(Ubar), ptr(Sbar), ptr(Vbar), ptr(thb), side_ptr),
                               "lri_batch_adjoint_step")
+            ev = torch.cuda.Event()
+            ev.record(side)
+            swept[ci] = ev
+            del inputs
+            nxt = replay(ci - 1) if ci > 0 else None
+        main.wait_stream(side)
         b.check_status()
         grads = SVDLikeRepresentation(Ubar.cpu().numpy().reshape((r, n)).T.copy(),
                                       Sbar.cpu().numpy().reshape((r, r)).T.copy(),
