@@ -264,7 +264,10 @@ LRI_API lri_status lri_bug_step_noalloc(int32_t dtype, int64_t n, int64_t m, int
  *                   accumulates d loss / d theta
  * Each instance recomputes its step in stage form (RK stage inputs, both
  * QRs, basis changes, projections, S stages) and sweeps back through it;
- * the thin-QR adjoint is (Q_bar + Q copyltu(-Q_bar^T Q)) R^{-T}.  The
+ * the thin-QR adjoint is (Q_bar + Q copyltu(-Q_bar^T Q)) R^{-T}.  While
+ * twice the instance count fits the device's SMs, each instance runs on a
+ * 2-CTA thread-block cluster (the K side on one SM, the L side on another);
+ * larger batches take one CTA per instance.  The
  * workspace comes from lri_batch_adjoint_prepare (LRI_ERR_STATE without it);
  * the step allocates nothing.  Schemes with nstages * nsub > 16 and other
  * batch kinds return LRI_ERR_UNSUPPORTED. */
