@@ -72,6 +72,7 @@ struct StepArgs {
   double tol;
   Scheme sK, sL, sS;
   double bh, balpha, bbeta;  // local flows: h, p0, p1 (Burgers: h, alpha, beta)
+  int32_t split;             // set by the launcher: one 2-CTA cluster per instance (FP64 BUG, Sylvester)
 };
 
 // Registered local flow maps (flows.cuh): count and names.

@@ -12,6 +12,10 @@
 //   data substeps src/integrators/data_integrator.jl:13-16 (u += sign*left'*Δy*right)
 //   K/L/S rhs     src/integrators/unconventional.jl:52-54,62-64,72-74
 #pragma once
+#include <cooperative_groups.h>
+
+#include <type_traits>
+
 #include "engine.cuh"
 #include "engine_api.h"
 
@@ -646,6 +650,62 @@ __device__ __noinline__ void bug_step(const StepArgs<T>& g, Inst<T>& I, int r, S
   check_finite<T>(g, I.S, r, I.rcap);
 }
 
+// BUG step of one FP64 Sylvester instance on a 2-CTA thread-block cluster
+// (batches small enough for two SMs per instance): the K and L steps read
+// only the old factors, so CTA 0 runs the K step and CTA 1 the L step; then
+// each swaps in its new basis and its projections; then CTA 0 runs the S
+// step.  The same operations as bug_step's literal (FP64) form.  Cluster
+// barriers (each after a __threadfence) separate the three phases, and both
+// CTAs reach both barriers.
+template <typename T>
+__device__ __noinline__ void bug_step_pair(const StepArgs<T>& g, Inst<T>& I, int r, Smem<T>& sm) {
+  namespace cg = cooperative_groups;
+  const int n = I.n, m = I.m, W = I.W;
+  const bool kside = cg::this_cluster().block_rank() == 0;
+  T* GU = I.blk(B_GU);
+  T* GV = I.blk(B_GV);
+  T* Mm = I.blk(B_M);
+  T* Nm = I.blk(B_N);
+  T* St = I.blk(B_ST);
+  T* T1 = I.blk(B_T1);
+  // both CTAs read the flag before the first barrier; CTA 0 sets it after
+  const bool fresh = g.proj_valid[I.inst] == 0;
+  if (kside) {
+    // K step (unconventional.jl:136-142) with the projections of the old V
+    if (fresh) projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+    k_step<T>(g, I, I.k, 0, I.U, I.S, I.rcap, false, I.k.PY, r, GV, I.V, g.sK, g.dt, sm);
+    orth_panel<T>(I, I.k.PY, n, r, I.k.PQ, nullptr, 0, sm);
+    tile_gram<T>(n, r, r, sm.stage, RowLoadPanel<T>{I.k.PQ, n, r}, RowLoadPanel<T>{I.U, n, r}, Mm, W, T(1), T(0));
+  } else {
+    // L step (unconventional.jl:144-150) with the projections of the old U
+    if (fresh) projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    k_step<T>(g, I, I.l, 1, I.V, I.S, I.rcap, true, I.l.PY, r, GU, I.U, g.sL, g.dt, sm);
+    orth_panel<T>(I, I.l.PY, m, r, I.l.PQ, nullptr, 0, sm);
+    tile_gram<T>(m, r, r, sm.stage, RowLoadPanel<T>{I.l.PQ, m, r}, RowLoadPanel<T>{I.V, m, r}, Nm, W, T(1), T(0));
+  }
+  __threadfence();
+  cg::this_cluster().sync();
+  // basis swap (unconventional.jl:151-152) and the new bases' projections
+  if (kside) {
+    copy_mat<T>(n, r, I.k.PQ, n, I.U, n);
+    projections<T>(I, I.U, n, r, I.k.tri, GU, sm);
+    if (threadIdx.x == 0) g.proj_valid[I.inst] = 1;
+  } else {
+    copy_mat<T>(m, r, I.l.PQ, m, I.V, m);
+    projections<T>(I, I.V, m, r, I.l.tri, GV, sm);
+  }
+  __threadfence();
+  cg::this_cluster().sync();
+  // S step on the new bases (unconventional.jl:154-156): S0 = M S N^T
+  if (kside) {
+    small_gemm<T>(r, r, r, T(1), I.S, I.rcap, false, Nm, W, true, T(0), T1, W);
+    small_gemm<T>(r, r, r, T(1), Mm, W, false, T1, W, false, T(0), St, W);
+    substep_core<T>(g, I, St, r, r, T(1), GU, GV, I.U, I.V, g.sS, g.dt, sm);
+    copy_mat<T>(r, r, St, W, I.S, I.rcap);
+    check_finite<T>(g, I.S, r, I.rcap);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Rank-adaptive BUG step
 // ---------------------------------------------------------------------------
@@ -887,7 +947,7 @@ template <typename T, int MINB>
 __global__ void __launch_bounds__(NT, MINB) step_kernel(StepArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem<T>& sm = *reinterpret_cast<Smem<T>*>(smem_raw);
-  const int inst = g.order[blockIdx.x];
+  const int inst = g.order[g.split ? (blockIdx.x >> 1) : blockIdx.x];
   const InstDesc d = g.inst[inst];
   Inst<T> I;
   I.n = d.n; I.m = d.m; I.rcap = d.rcap; I.W = d.wcap; I.inst = inst;
@@ -913,7 +973,15 @@ __global__ void __launch_bounds__(NT, MINB) step_kernel(StepArgs<T> g) {
     return;
   }
   if (g.alg == ALG_BUG) {
-    bug_step<T>(g, I, r, sm);
+    if constexpr (std::is_same<T, double>::value) {
+      if (g.split) {
+        bug_step_pair<T>(g, I, r, sm);
+      } else {
+        bug_step<T>(g, I, r, sm);
+      }
+    } else {
+      bug_step<T>(g, I, r, sm);
+    }
   } else if (g.alg == ALG_GREEDY) {
     greedy_step<T>(g, I, r, sm);
   } else if (g.alg == ALG_RA_BUG) {
@@ -941,12 +1009,46 @@ size_t step_smem_bytes() {
   return sizeof(Smem<T>);
 }
 
+// FP64 BUG steps of the Sylvester flow in batches small enough that every
+// instance can have two SMs run as one 2-CTA cluster per instance
+// (bug_step_pair).  The pair's CTAs ask for more shared memory than two CTAs
+// of an SM can hold, so the K and L steps run on two SMs, each with its own
+// FP64 units.
+constexpr int kPairSmem = 120 * 1024;
+
 template <typename T, int MINB>
 cudaError_t launch_step_occ(const StepArgs<T>& g, int count, cudaStream_t stream) {
   const size_t smem = sizeof(Smem<T>);
+  constexpr bool f64 = std::is_same<T, double>::value;
+  static_assert(sizeof(Smem<T>) <= kPairSmem, "pair launch smem below the kernel's");
   static std::atomic<uint64_t> attr_done{0};
-  cudaError_t e = set_smem_limit(step_kernel<T, MINB>, (int)smem, attr_done);
+  cudaError_t e = set_smem_limit(step_kernel<T, MINB>, f64 ? kPairSmem : (int)smem, attr_done);
   if (e != cudaSuccess) return e;
+  if (f64 && g.alg == ALG_BUG && g.op == OP_SYLVESTER) {
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (2 * count <= sms) {
+      StepArgs<T> gp = g;
+      gp.split = 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * count, 1, 1);
+      cfg.blockDim = dim3(NT, 1, 1);
+      cfg.dynamicSmemBytes = kPairSmem;
+      cfg.stream = stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 2;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      e = cudaLaunchKernelEx(&cfg, step_kernel<T, MINB>, gp);
+      if (e != cudaSuccess) return e;
+      return cudaGetLastError();
+    }
+  }
   step_kernel<T, MINB><<<count, NT, smem, stream>>>(g);
   return cudaGetLastError();
 }
