@@ -698,9 +698,10 @@ def leg_laplace(warmup):
             "accuracy": {"steps": k_acc, "rel_fro_vs_fp64_oracle": err, "oracle_self_sensitivity": sens,
                          "bound": max(1e-11, 100.0 * sens),
                          "passed": bool(err <= max(1e-11, 100.0 * sens))},
-            "roofline": {"bound": "latency", "note": "one instance of 66 KB state: a single CTA runs the whole "
-                                                     "step (one SM); flops per step %.3g, %.3f TFLOP/s"
-                                                     % (flops, flops / (ms * 1e-3) / 1e12)},
+            "roofline": {"bound": "latency", "note": "one instance of 66 KB state on a 2-CTA cluster (FP64: the K "
+                                                     "and L steps on two SMs, the S step on the first; the "
+                                                     "double-float form on one CTA); flops per step %.3g, "
+                                                     "%.3f TFLOP/s" % (flops, flops / (ms * 1e-3) / 1e12)},
             "gpu_launches": nsteps,
             "clocks": clocks,
             "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": 1, "kind": "port",
